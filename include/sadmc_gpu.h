@@ -1,0 +1,182 @@
+/*
+ * sadmc_gpu.h - C ABI of the GB300 flat-histogram Monte Carlo hot path.
+ *
+ * One handle owns a batch of independent walkers of one system kind and one method, all
+ * resident on the current CUDA device.  The entry points replace, for a whole batch at
+ * once, the per-walker Rust surface of the reference (droundy/sad-monte-carlo):
+ *
+ *   trait System / ConfirmSystem / MovableSystem      src/system/mod.rs:54-120
+ *   trait MonteCarlo, EnergyMC<S>                      src/mc/mod.rs:37-144,
+ *                                                      src/mc/energy.rs:166-210, 827-990
+ *
+ * Conventions.  Every function returns 0 (SADMC_OK) or a negative SADMC_ERR_* code and
+ * never aborts; sadmc_last_error() describes the last failure of the calling thread.
+ * The library owns all device memory; callers own the host arrays they pass.  Calls are
+ * synchronous unless named *_async.  One handle per host thread (like EnergyMC's
+ * &mut self); the library starts no threads.  Energies are in units of epsilon, lengths
+ * in sigma (src/system/units.rs).
+ */
+#ifndef SADMC_GPU_H
+#define SADMC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SADMC_OK 0
+#define SADMC_ERR_INVALID (-1)   /* bad argument or configuration */
+#define SADMC_ERR_CUDA (-2)      /* CUDA runtime error (device missing, launch failure) */
+#define SADMC_ERR_STATE (-3)     /* call out of order (e.g. run before initialize) */
+#define SADMC_ERR_NOMEM (-4)     /* device allocation failed */
+
+/* System kinds: src/system/{ising,lj,wca,optsquare}.rs */
+#define SADMC_ISING 0
+#define SADMC_LJ 1
+#define SADMC_WCA 2
+#define SADMC_SW 3 /* square well with a hard core (optsquare::SquareWell) */
+
+/* Methods: MethodParams, src/mc/energy.rs:42-69 */
+#define SADMC_SAD 0
+#define SADMC_SAMC 1
+#define SADMC_WL 2
+#define SADMC_INV_T_WL 3
+#define SADMC_CANONICAL 4
+
+/* Per-walker status bits (device status words; the reference panics instead). */
+#define SADMC_ST_BIN_RANGE 1u       /* proposal outside the preallocated bins: rejected */
+#define SADMC_ST_NAN_GAMMA 2u       /* gamma was NaN (energy.rs:30-33) */
+#define SADMC_ST_DRIFT 4u           /* incremental E drifted beyond drift_tol (verify_energy) */
+#define SADMC_ST_CELL_OVERFLOW 8u   /* a subcell bucket overflowed */
+#define SADMC_ST_TIMEOUT 16u        /* a bounded device wait gave up */
+#define SADMC_ST_DESCENT_FAILED 32u /* initial descent did not reach max_allowed_energy */
+#define SADMC_ST_BAD_INPUT 64u      /* geometry rejected (fewer than 3 subcells per axis) */
+
+/* Configuration: EnergyMCParams (energy.rs:81-97) plus the batch and system parameters
+ * (LjParams lj.rs:14-19, WcaNParams wca.rs:371-380, SquareWellNParams optsquare.rs:336-345,
+ * IsingParams ising.rs:12-15). */
+typedef struct sadmc_config {
+  int32_t system;            /* SADMC_ISING .. SADMC_SW */
+  int32_t method;            /* SADMC_SAD .. SADMC_CANONICAL */
+  int32_t n_walkers;
+  int32_t max_atoms;         /* largest N over the walkers (Ising: the lattice width L) */
+  double min_T;              /* SAD minimum temperature (default 0.2, energy.rs:102-104) */
+  double t0;                 /* SAMC t0 */
+  int32_t has_min_gamma;     /* WL: begin a production run below min_gamma */
+  int32_t pad0;
+  double min_gamma;
+  double T;                  /* canonical temperature */
+  int32_t has_energy_bin;    /* energy_bin; default System::delta_energy() or 1.0 */
+  int32_t pad1;
+  double energy_bin;
+  int32_t has_min_allowed, has_max_allowed;
+  double min_allowed, max_allowed;
+  double e_lo, e_hi;         /* energies the preallocated bins must cover */
+  int32_t acceptance_rate_mode; /* MoveParams::AcceptanceRate(target_rate) */
+  int32_t pad2;
+  double target_rate;
+  double translation_scale;  /* initial rms step (MoveParams::TranslationScale, 0.05) */
+  double well_width;         /* square-well lambda (optsquare default 1.3) */
+  uint64_t seed;             /* Philox key; walker w draws from stream (seed, w) */
+  uint64_t descent_limit;    /* initial descent proposals per walker (energy.rs:841: 1e8) */
+  int32_t lanes_per_walker;  /* lanes cooperating on one walker; 0 = autotuned default */
+  int32_t resum_interval;    /* moves between FP64 energy re-sums (LJ, WCA); 0 = 2048 */
+  double drift_tol;          /* SADMC_ST_DRIFT threshold on |E - E_fp64| (0 = 1e-6*N) */
+} sadmc_config;
+
+/* Per-walker geometry (walkers of one handle may differ in N and box). */
+typedef struct sadmc_geometry {
+  int32_t n;                 /* atoms (Ising: L, must equal max_atoms) */
+  int32_t pad;
+  double radius;             /* LJ spherical wall radius (Lj::max_radius) */
+  double box[3];             /* WCA / square-well periodic box (Cell::box_diagonal) */
+} sadmc_geometry;
+
+/* An injected proposal (the parity hook for MovableSystem::plan_move): atom `which`
+ * displaced by scale * g (Ising: the site (i, j)). */
+typedef struct sadmc_proposal {
+  int32_t which;
+  int32_t j;
+  double g[3];
+  double scale;
+} sadmc_proposal;
+
+typedef struct sadmc_handle sadmc_handle;
+
+int32_t sadmc_version(void);
+const char* sadmc_last_error(void);
+
+/* Allocate a batch (EnergyMC::from_params without the initial state).  geom has
+ * cfg->n_walkers entries. */
+int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_handle** out);
+int32_t sadmc_destroy(sadmc_handle* h);
+
+/* Upload configurations for walkers [walker_begin, walker_begin + count): positions as
+ * packed x,y,z doubles (walker after walker, geom[w].n atoms each), Ising spins as +-1
+ * values (L*L per walker, index i + j*L).  Periodic positions must lie in [0, box). */
+int32_t sadmc_upload_state(sadmc_handle* h, int32_t walker_begin, int32_t count,
+                           const double* state);
+int32_t sadmc_read_state(sadmc_handle* h, int32_t walker_begin, int32_t count, double* state);
+
+/* EnergyMC::from_params (energy.rs:830-898): FP64 energies, the downhill descent below
+ * max_allowed_energy when set, and bins anchored at (round(E/w) - 0.5) w. */
+int32_t sadmc_initialize(sadmc_handle* h);
+
+/* `moves` calls of MonteCarlo::move_once (energy.rs:904-974) on every walker. */
+int32_t sadmc_run(sadmc_handle* h, uint64_t moves);
+int32_t sadmc_run_async(sadmc_handle* h, uint64_t moves, void* cuda_stream);
+int32_t sadmc_synchronize(sadmc_handle* h);
+
+/* System::energy (cached) and System::compute_energy (FP64 full re-sum), per walker. */
+int32_t sadmc_energy(sadmc_handle* h, double* E);
+int32_t sadmc_compute_energy(sadmc_handle* h, double* E);
+
+/* MovableSystem::plan_move with an injected proposal and ConfirmSystem::confirm.
+ * Bins and counters are not touched. */
+int32_t sadmc_plan_move_injected(sadmc_handle* h, int32_t walker, const sadmc_proposal* p,
+                                 double* e_out, int32_t* possible);
+int32_t sadmc_confirm(sadmc_handle* h, int32_t walker);
+
+/* Bins of one walker in the reference's layout (energy.rs:145-163, 202-205): nbins
+ * entries starting at bins_min. */
+int32_t sadmc_nbins(sadmc_handle* h, int32_t walker, int64_t* nbins, double* bins_min,
+                    double* width);
+int32_t sadmc_read_bins(sadmc_handle* h, int32_t walker, double* lnw, uint64_t* histogram,
+                        uint64_t* t_found, double* energy_total, double* energy_squared_total,
+                        uint64_t* round_trips, uint8_t* visited_since_maxentropy);
+/* Wang-Landau per-stage histogram (Method::WL::hist), *n entries from *min_energy. */
+int32_t sadmc_read_wl_hist(sadmc_handle* h, int32_t walker, uint64_t* hist, int64_t* n,
+                           double* min_energy);
+
+/* Scalar state of one walker, SADMC_N_SCALARS doubles in this order: moves, accepted,
+ * acceptance_rate, translation_scale, method, too_lo, too_hi, tL, tF, num_states,
+ * highest_hist, latest_parameter, gamma, lowest_hist, wl_highest_hist, total_hist,
+ * wl_num_states, min_energy, t0, max_S, max_S_index, drift, status, energy. */
+#define SADMC_N_SCALARS 24
+int32_t sadmc_read_scalars(sadmc_handle* h, int32_t walker, double* out);
+/* MonteCarlo::num_moves / num_accepted_moves summed over walkers. */
+int32_t sadmc_counters(sadmc_handle* h, uint64_t* moves, uint64_t* accepted);
+int32_t sadmc_status(sadmc_handle* h, uint32_t* per_walker_flags);
+
+/* Record (E at move start, proposed E) for the next `capacity` moves of every walker;
+ * 0 disables.  Used to replay a GPU trajectory through the FP64 oracle. */
+int32_t sadmc_set_trace(sadmc_handle* h, uint64_t capacity);
+int32_t sadmc_read_trace(sadmc_handle* h, int32_t walker, double* e1, double* e2,
+                         uint64_t* count);
+
+/* Lanes per walker in use; sadmc_autotune times the candidates on a snapshot of the
+ * batch (`moves` moves each), keeps the fastest and restores the snapshot. */
+int32_t sadmc_lanes_per_walker(sadmc_handle* h);
+int32_t sadmc_autotune(sadmc_handle* h, uint64_t moves, int32_t* best_lpw, double* best_ms);
+
+/* Heat capacity C(T) = (<E^2> - <E>^2) / T^2 with P ~ exp(S - E/T - max), FP64 on the
+ * device (plotting/final_heat_capacity.py:79-88).  Host arrays. */
+int32_t sadmc_heat_capacity(const double* T, int32_t nT, const double* E, const double* S,
+                            int32_t n, double* C);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SADMC_GPU_H */

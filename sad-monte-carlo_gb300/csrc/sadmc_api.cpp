@@ -1,0 +1,633 @@
+// Host implementation of the C ABI in include/sadmc_gpu.h.
+#include "../../include/sadmc_gpu.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sadmc_launch.h"
+#include "sadmc_types.h"
+
+using namespace sadmc;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int32_t fail(int32_t code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                  \
+  do {                                                                                  \
+    cudaError_t _e = (expr);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return fail(SADMC_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));  \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t n) {
+  return cudaMalloc((void**)p, n * sizeof(T) + 16);
+}
+
+int pad_atoms(int n) {
+  for (int p : {32, 64, 128, 256})
+    if (n <= p) return p;
+  return -1;
+}
+
+bool valid_lpw_lj(int lpw, int np) {
+  switch (np) {
+    case 32: return lpw == 32 || lpw == 16 || lpw == 8 || lpw == 4;
+    case 64: return lpw == 32 || lpw == 16 || lpw == 8;
+    default: return lpw == 32;
+  }
+}
+
+}  // namespace
+
+struct sadmc_handle {
+  sadmc_config cfg{};
+  std::vector<sadmc_geometry> geom;
+  int W = 0, nb = 0, np = 0, L = 0, lpw = 0;
+  double width = 1.0;
+  bool uploaded = false, initialized = false;
+  cudaStream_t stream = nullptr;
+  WalkerCore* d_cores = nullptr;
+  BinPlanes planes{};
+  void* plane_mem = nullptr;
+  float* d_pos = nullptr;      // LJ: [W][6][np]
+  int8_t* d_spins = nullptr;   // Ising: [W][L*L]
+  double* d_tmp = nullptr;     // [W] + 2 scratch doubles
+  TraceRec* d_trace = nullptr;
+  uint64_t trace_cap = 0, trace_t0 = 0;
+  uint64_t moves_done = 0;
+  int pend_walker = -1;
+  sadmc_proposal pend{};
+  std::vector<WalkerCore> h_cores;
+
+  FhParams fh_params() const {
+    FhParams P{};
+    P.width = width;
+    P.inv_width = 1.0 / width;
+    P.nbins = nb;
+    P.has_min_allowed = cfg.has_min_allowed;
+    P.has_max_allowed = cfg.has_max_allowed;
+    P.acc_mode = cfg.acceptance_rate_mode;
+    P.min_allowed = cfg.min_allowed;
+    P.max_allowed = cfg.max_allowed;
+    P.target_rate = cfg.target_rate;
+    return P;
+  }
+  int resum() const { return cfg.resum_interval > 0 ? cfg.resum_interval : 2048; }
+  double drift_tol() const {
+    return cfg.drift_tol > 0 ? cfg.drift_tol : 1e-6 * (double)std::max(1, cfg.max_atoms);
+  }
+  int32_t pull_cores() {
+    h_cores.resize(W);
+    CUDA_TRY(cudaMemcpyAsync(h_cores.data(), d_cores, sizeof(WalkerCore) * W,
+                             cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return SADMC_OK;
+  }
+  int32_t push_cores() {
+    CUDA_TRY(cudaMemcpyAsync(d_cores, h_cores.data(), sizeof(WalkerCore) * W,
+                             cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return SADMC_OK;
+  }
+  cudaError_t launch_move(const MoveLaunch& m) {
+    switch (cfg.system) {
+      case SADMC_LJ: return launch_lj_move(m, LjSys{d_pos, np, 0.0 + radius2()}, lpw, stream);
+      case SADMC_ISING: return launch_ising_move(m, IsingSys{d_spins, L}, lpw, stream);
+      default: return cudaErrorNotSupported;
+    }
+  }
+  // Before sadmc_initialize the cores only carry each walker's N (and E when planned).
+  int32_t prep_cores() {
+    if (initialized) return SADMC_OK;
+    if ((int)h_cores.size() != W) {
+      h_cores.assign(W, WalkerCore{});
+      for (int w = 0; w < W; ++w) { h_cores[w].n = geom[w].n; h_cores[w].kind = M_DESCENT; }
+      return push_cores();
+    }
+    return SADMC_OK;
+  }
+  double radius2() const { return geom.empty() ? 0.0 : geom[0].radius * geom[0].radius; }
+  cudaError_t launch_energy(double* out) {
+    switch (cfg.system) {
+      case SADMC_LJ: return launch_lj_energy(d_cores, LjSys{d_pos, np, radius2()}, W, out, stream);
+      case SADMC_ISING: return launch_ising_energy(IsingSys{d_spins, L}, W, out, stream);
+      default: return cudaErrorNotSupported;
+    }
+  }
+  MoveLaunch base_launch() const {
+    MoveLaunch m{};
+    m.cores = d_cores;
+    m.P = fh_params();
+    m.B = planes;
+    m.n_walkers = W;
+    m.seed = cfg.seed;
+    m.trace = d_trace;
+    m.trace_cap = trace_cap;
+    m.trace_t0 = trace_t0;
+    m.resum_interval = resum();
+    m.drift_tol = drift_tol();
+    return m;
+  }
+};
+
+extern "C" {
+
+int32_t sadmc_version(void) { return 1; }
+const char* sadmc_last_error(void) { return g_last_error.c_str(); }
+
+int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_handle** out) {
+  if (!cfg || !geom || !out) return fail(SADMC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  const sadmc_config& c = *cfg;
+  if (c.n_walkers <= 0) return fail(SADMC_ERR_INVALID, "n_walkers must be positive");
+  if (c.system < SADMC_ISING || c.system > SADMC_SW) return fail(SADMC_ERR_INVALID, "unknown system");
+  if (c.method < SADMC_SAD || c.method > SADMC_CANONICAL) return fail(SADMC_ERR_INVALID, "unknown method");
+  if (!(c.e_hi > c.e_lo)) return fail(SADMC_ERR_INVALID, "e_hi must exceed e_lo");
+  if (c.system != SADMC_ISING && c.system != SADMC_LJ)
+    return fail(SADMC_ERR_INVALID, "system not available in this build");
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    return fail(SADMC_ERR_CUDA, "no CUDA device");
+  auto* h = new sadmc_handle();
+  h->cfg = c;
+  h->W = c.n_walkers;
+  h->geom.assign(geom, geom + c.n_walkers);
+  // bin width: energy_bin, else System::delta_energy() (Ising 4, square well 1), else 1
+  // (energy.rs:831-833)
+  h->width = c.has_energy_bin ? c.energy_bin : (c.system == SADMC_ISING ? 4.0 : (c.system == SADMC_SW ? 1.0 : 1.0));
+  if (!(h->width > 0)) { delete h; return fail(SADMC_ERR_INVALID, "energy_bin must be positive"); }
+  double nbd = std::ceil((c.e_hi - c.e_lo) / h->width) + 4.0;
+  if (nbd > (double)(1 << 24)) { delete h; return fail(SADMC_ERR_INVALID, "too many bins"); }
+  h->nb = (int)nbd;
+  if (c.system == SADMC_ISING) {
+    h->L = c.max_atoms;
+    if (h->L < 2) { delete h; return fail(SADMC_ERR_INVALID, "Ising needs L > 1 (ising.rs:39)"); }
+    for (int w = 0; w < h->W; ++w)
+      if (geom[w].n != h->L) { delete h; return fail(SADMC_ERR_INVALID, "Ising walkers must share L"); }
+    h->lpw = c.lanes_per_walker ? c.lanes_per_walker : (h->W == 1 ? 32 : 1);
+    if (h->lpw != 1 && h->lpw != 32) { delete h; return fail(SADMC_ERR_INVALID, "Ising lanes_per_walker must be 1 or 32"); }
+  } else {
+    int mx = 0;
+    for (int w = 0; w < h->W; ++w) {
+      if (geom[w].n < 2) { delete h; return fail(SADMC_ERR_INVALID, "walkers need at least 2 atoms"); }
+      mx = std::max(mx, (int)geom[w].n);
+      if (geom[w].radius != geom[0].radius) { delete h; return fail(SADMC_ERR_INVALID, "LJ walkers must share the wall radius"); }
+    }
+    h->np = pad_atoms(mx);
+    if (h->np < 0) { delete h; return fail(SADMC_ERR_INVALID, "at most 256 atoms per LJ walker"); }
+    h->lpw = c.lanes_per_walker ? c.lanes_per_walker : (h->np <= 64 ? 8 : 32);
+    if (!valid_lpw_lj(h->lpw, h->np)) { delete h; return fail(SADMC_ERR_INVALID, "unsupported lanes_per_walker"); }
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete h; return fail(SADMC_ERR_CUDA, cudaGetErrorString(e)); }
+  const size_t plane = (size_t)h->W * (size_t)h->nb;
+  bool ok = dalloc(&h->d_cores, h->W) == cudaSuccess && dalloc(&h->d_tmp, h->W + 2) == cudaSuccess &&
+            cudaMalloc(&h->plane_mem, plane * 8 * 8) == cudaSuccess;
+  if (ok) {
+    char* b = (char*)h->plane_mem;
+    h->planes.lnw = (double*)(b + 0 * plane * 8);
+    h->planes.hist = (uint64_t*)(b + 1 * plane * 8);
+    h->planes.t_found = (uint64_t*)(b + 2 * plane * 8);
+    h->planes.sumE = (double*)(b + 3 * plane * 8);
+    h->planes.sumE2 = (double*)(b + 4 * plane * 8);
+    h->planes.round_trips = (uint64_t*)(b + 5 * plane * 8);
+    h->planes.visit_stamp = (uint64_t*)(b + 6 * plane * 8);
+    h->planes.wl_hist = (uint64_t*)(b + 7 * plane * 8);
+    if (c.system == SADMC_ISING) ok = dalloc(&h->d_spins, (size_t)h->W * h->L * h->L) == cudaSuccess;
+    else ok = dalloc(&h->d_pos, (size_t)h->W * 6 * h->np) == cudaSuccess;
+  }
+  if (!ok) {
+    sadmc_destroy(h);
+    return fail(SADMC_ERR_NOMEM, "device allocation failed");
+  }
+  if (h->d_pos) cudaMemsetAsync(h->d_pos, 0, sizeof(float) * (size_t)h->W * 6 * h->np, h->stream);
+  *out = h;
+  return SADMC_OK;
+}
+
+int32_t sadmc_destroy(sadmc_handle* h) {
+  if (!h) return SADMC_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->d_cores);
+  cudaFree(h->d_tmp);
+  cudaFree(h->plane_mem);
+  cudaFree(h->d_pos);
+  cudaFree(h->d_spins);
+  cudaFree(h->d_trace);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return SADMC_OK;
+}
+
+int32_t sadmc_upload_state(sadmc_handle* h, int32_t begin, int32_t count, const double* state) {
+  if (!h || !state || begin < 0 || count < 0 || begin + count > h->W)
+    return fail(SADMC_ERR_INVALID, "bad walker range");
+  if (h->cfg.system == SADMC_ISING) {
+    const size_t n = (size_t)h->L * h->L;
+    std::vector<int8_t> s(n * count);
+    for (size_t k = 0; k < s.size(); ++k) s[k] = (int8_t)(state[k] > 0 ? 1 : -1);
+    CUDA_TRY(cudaMemcpyAsync(h->d_spins + (size_t)begin * n, s.data(), s.size(), cudaMemcpyHostToDevice, h->stream));
+  } else {
+    const int np = h->np;
+    std::vector<float> p((size_t)count * 6 * np, 0.0f);
+    size_t off = 0;
+    for (int w = 0; w < count; ++w) {
+      const int n = h->geom[begin + w].n;
+      float* q = p.data() + (size_t)w * 6 * np;
+      for (int j = 0; j < n; ++j)
+        for (int a = 0; a < 3; ++a) {
+          const double x = state[off + 3 * j + a];
+          const float hi = (float)x;
+          q[a * np + j] = hi;
+          q[(3 + a) * np + j] = (float)(x - (double)hi);
+        }
+      off += 3 * (size_t)n;
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->d_pos + (size_t)begin * 6 * np, p.data(), p.size() * sizeof(float),
+                             cudaMemcpyHostToDevice, h->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->uploaded = true;
+  h->initialized = false;
+  h->h_cores.clear();
+  return SADMC_OK;
+}
+
+int32_t sadmc_read_state(sadmc_handle* h, int32_t begin, int32_t count, double* state) {
+  if (!h || !state || begin < 0 || count < 0 || begin + count > h->W)
+    return fail(SADMC_ERR_INVALID, "bad walker range");
+  if (h->cfg.system == SADMC_ISING) {
+    const size_t n = (size_t)h->L * h->L;
+    std::vector<int8_t> s(n * count);
+    CUDA_TRY(cudaMemcpyAsync(s.data(), h->d_spins + (size_t)begin * n, s.size(), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (size_t k = 0; k < s.size(); ++k) state[k] = s[k];
+  } else {
+    const int np = h->np;
+    std::vector<float> p((size_t)count * 6 * np);
+    CUDA_TRY(cudaMemcpyAsync(p.data(), h->d_pos + (size_t)begin * 6 * np, p.size() * sizeof(float),
+                             cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    size_t off = 0;
+    for (int w = 0; w < count; ++w) {
+      const int n = h->geom[begin + w].n;
+      const float* q = p.data() + (size_t)w * 6 * np;
+      for (int j = 0; j < n; ++j)
+        for (int a = 0; a < 3; ++a)
+          state[off + 3 * j + a] = (double)q[a * np + j] + (double)q[(3 + a) * np + j];
+      off += 3 * (size_t)n;
+    }
+  }
+  return SADMC_OK;
+}
+
+int32_t sadmc_initialize(sadmc_handle* h) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (!h->uploaded) return fail(SADMC_ERR_STATE, "upload a state first");
+  const sadmc_config& c = h->cfg;
+  h->h_cores.assign(h->W, WalkerCore{});
+  for (int w = 0; w < h->W; ++w) {
+    h->h_cores[w].n = h->geom[w].n;
+    h->h_cores[w].kind = M_DESCENT;
+  }
+  int32_t r = h->push_cores();
+  if (r) return r;
+  CUDA_TRY(h->launch_energy(h->d_tmp));
+  std::vector<double> E(h->W);
+  CUDA_TRY(cudaMemcpyAsync(E.data(), h->d_tmp, sizeof(double) * h->W, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  for (int w = 0; w < h->W; ++w) h->h_cores[w].E = E[w];
+  if (c.has_max_allowed && c.system == SADMC_LJ) {
+    // from_params descent (energy.rs:840-851)
+    r = h->push_cores();
+    if (r) return r;
+    MoveLaunch m = h->base_launch();
+    m.trace = nullptr;
+    m.descent = 1;
+    m.descent_limit = c.descent_limit ? c.descent_limit : 100000000ull;
+    m.descent_max = c.max_allowed;
+    uint64_t left = m.descent_limit;
+    while (left > 0) {
+      m.n_moves = std::min<uint64_t>(left, 1ull << 16);
+      CUDA_TRY(h->launch_move(m));
+      r = h->pull_cores();
+      if (r) return r;
+      bool all = true;
+      for (int w = 0; w < h->W; ++w)
+        if (!(h->h_cores[w].E < c.max_allowed) && h->h_cores[w].pad2 < m.descent_limit) all = false;
+      if (all) break;
+      left -= m.n_moves;
+    }
+  }
+  // EnergyMC fields (energy.rs:852-898) and Method::new (energy.rs:247-313)
+  const double wdt = h->width;
+  const bool both = c.has_min_allowed && c.has_max_allowed;
+  for (int w = 0; w < h->W; ++w) {
+    WalkerCore k{};
+    const WalkerCore& o = h->h_cores[w];
+    const double e0 = o.E;
+    const double emin = (std::round(e0 / wdt) - 0.5) * wdt;
+    const double g0d = std::floor((emin - c.e_lo) / wdt) + 2.0;
+    if (!(g0d >= 0.0 && g0d < (double)h->nb))
+      return fail(SADMC_ERR_INVALID, "walker " + std::to_string(w) + " starts at E=" +
+                                         std::to_string(e0) + ", outside [e_lo, e_hi]");
+    k.E = e0;
+    k.acc_rate = 0.5;
+    k.tscale = c.translation_scale;
+    k.cur_min = emin;
+    k.too_lo = e0; k.too_hi = e0; k.latest_param = 0.0; k.min_T = c.min_T;
+    k.gamma = 1.0;
+    k.wl_num_states = both ? (c.max_allowed - c.min_allowed) / wdt : 1.0;
+    k.min_energy = e0;
+    k.t0 = c.t0;
+    k.max_S = 0.0;
+    k.drift = 0.0;
+    k.temperature = c.T;
+    k.win_tmax = 0;
+    k.moves = 0; k.accepted = 0; k.tL = 0; k.tF = 0; k.num_states = 1; k.highest_hist = 1;
+    k.lowest_hist = both ? 0 : 1; k.wl_highest_hist = 1; k.total_hist = 0;
+    k.kind = c.method;
+    k.b_lo = k.b_hi = (int)g0d;
+    k.wl_lo = 0; k.wl_hi = -1;
+    k.max_S_local = 0;
+    k.fill_val = 0;
+    k.fill_gen = 1;
+    k.status = o.status & ST_DESCENT_FAILED;
+    k.n = h->geom[w].n;
+    k.has_min_gamma = (c.method == SADMC_WL) ? c.has_min_gamma : 0;
+    k.min_gamma = c.min_gamma;
+    k.pad2 = o.pad2;
+    h->h_cores[w] = k;
+  }
+  r = h->push_cores();
+  if (r) return r;
+  CUDA_TRY(launch_init_planes(h->d_cores, h->planes, h->nb, h->W, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->moves_done = 0;
+  h->initialized = true;
+  return SADMC_OK;
+}
+
+int32_t sadmc_run_async(sadmc_handle* h, uint64_t moves, void* stream) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  cudaStream_t keep = h->stream;
+  h->stream = st;
+  MoveLaunch m = h->base_launch();
+  const uint64_t chunk = 8192;
+  uint64_t left = moves;
+  while (left > 0) {
+    m.n_moves = std::min(left, chunk);
+    cudaError_t e = h->launch_move(m);
+    if (e != cudaSuccess) { h->stream = keep; return fail(SADMC_ERR_CUDA, cudaGetErrorString(e)); }
+    left -= m.n_moves;
+  }
+  h->stream = keep;
+  h->moves_done += moves;
+  return SADMC_OK;
+}
+
+int32_t sadmc_run(sadmc_handle* h, uint64_t moves) {
+  int32_t r = sadmc_run_async(h, moves, nullptr);
+  if (r) return r;
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return SADMC_OK;
+}
+
+int32_t sadmc_synchronize(sadmc_handle* h) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return SADMC_OK;
+}
+
+int32_t sadmc_energy(sadmc_handle* h, double* E) {
+  if (!h || !E) return fail(SADMC_ERR_INVALID, "null argument");
+  int32_t r = h->pull_cores();
+  if (r) return r;
+  for (int w = 0; w < h->W; ++w) E[w] = h->h_cores[w].E;
+  return SADMC_OK;
+}
+
+int32_t sadmc_compute_energy(sadmc_handle* h, double* E) {
+  if (!h || !E) return fail(SADMC_ERR_INVALID, "null argument");
+  if (!h->uploaded) return fail(SADMC_ERR_STATE, "upload a state first");
+  int32_t r = h->prep_cores();
+  if (r) return r;
+  CUDA_TRY(h->launch_energy(h->d_tmp));
+  CUDA_TRY(cudaMemcpyAsync(E, h->d_tmp, sizeof(double) * h->W, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return SADMC_OK;
+}
+
+int32_t sadmc_plan_move_injected(sadmc_handle* h, int32_t walker, const sadmc_proposal* p,
+                                 double* e_out, int32_t* possible) {
+  if (!h || !p || !e_out || !possible || walker < 0 || walker >= h->W)
+    return fail(SADMC_ERR_INVALID, "bad argument");
+  if (h->cfg.system != SADMC_LJ) return fail(SADMC_ERR_INVALID, "injected plans: LJ only in this build");
+  if (p->which < 0 || p->which >= h->geom[walker].n) return fail(SADMC_ERR_INVALID, "bad atom index");
+  if (!h->uploaded) return fail(SADMC_ERR_STATE, "upload a state first");
+  int32_t r = h->prep_cores();
+  if (r) return r;
+  if (!h->initialized) {  // plan against System::energy() of the uploaded state
+    CUDA_TRY(h->launch_energy(h->d_tmp));
+    std::vector<double> E(h->W);
+    CUDA_TRY(cudaMemcpyAsync(E.data(), h->d_tmp, sizeof(double) * h->W, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (int w = 0; w < h->W; ++w) h->h_cores[w].E = E[w];
+    r = h->push_cores();
+    if (r) return r;
+  }
+  CUDA_TRY(launch_lj_plan(h->d_cores, LjSys{h->d_pos, h->np, h->radius2()}, walker, p->which,
+                          (float)p->g[0], (float)p->g[1], (float)p->g[2], p->scale, 0, h->d_tmp,
+                          h->stream));
+  double o[2];
+  CUDA_TRY(cudaMemcpyAsync(o, h->d_tmp, sizeof(o), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  *e_out = o[0];
+  *possible = o[1] != 0.0;
+  h->pend_walker = *possible ? walker : -1;
+  h->pend = *p;
+  return SADMC_OK;
+}
+
+int32_t sadmc_confirm(sadmc_handle* h, int32_t walker) {
+  if (!h || walker < 0 || walker >= h->W) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (h->pend_walker != walker) return SADMC_OK;  // ConfirmSystem::confirm with no change
+  const sadmc_proposal& p = h->pend;
+  CUDA_TRY(launch_lj_plan(h->d_cores, LjSys{h->d_pos, h->np, h->radius2()}, walker, p.which,
+                          (float)p.g[0], (float)p.g[1], (float)p.g[2], p.scale, 1, h->d_tmp,
+                          h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->pend_walker = -1;
+  return SADMC_OK;
+}
+
+int32_t sadmc_nbins(sadmc_handle* h, int32_t walker, int64_t* nbins, double* bins_min, double* width) {
+  if (!h || walker < 0 || walker >= h->W) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  WalkerCore k;
+  CUDA_TRY(cudaMemcpyAsync(&k, h->d_cores + walker, sizeof(k), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (nbins) *nbins = k.b_hi - k.b_lo + 1;
+  if (bins_min) *bins_min = k.cur_min;
+  if (width) *width = h->width;
+  return SADMC_OK;
+}
+
+int32_t sadmc_read_bins(sadmc_handle* h, int32_t walker, double* lnw, uint64_t* hist,
+                        uint64_t* t_found, double* sumE, double* sumE2, uint64_t* rt,
+                        uint8_t* visited) {
+  if (!h || walker < 0 || walker >= h->W) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  WalkerCore k;
+  CUDA_TRY(cudaMemcpyAsync(&k, h->d_cores + walker, sizeof(k), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const size_t n = (size_t)(k.b_hi - k.b_lo + 1);
+  const size_t off = (size_t)walker * h->nb + k.b_lo;
+  auto get = [&](void* dst, const void* src) -> cudaError_t {
+    if (!dst) return cudaSuccess;
+    return cudaMemcpyAsync(dst, (const char*)src + off * 8, n * 8, cudaMemcpyDeviceToHost, h->stream);
+  };
+  CUDA_TRY(get(lnw, h->planes.lnw));
+  CUDA_TRY(get(hist, h->planes.hist));
+  CUDA_TRY(get(t_found, h->planes.t_found));
+  CUDA_TRY(get(sumE, h->planes.sumE));
+  CUDA_TRY(get(sumE2, h->planes.sumE2));
+  CUDA_TRY(get(rt, h->planes.round_trips));
+  std::vector<uint64_t> st(visited ? n : 0);
+  if (visited) CUDA_TRY(get(st.data(), h->planes.visit_stamp));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (visited)
+    for (size_t i = 0; i < n; ++i) visited[i] = st[i] == k.fill_gen ? 1 : (uint8_t)(k.fill_val != 0);
+  // the cached current bin lives in the planes after each launch (flushed on store)
+  return SADMC_OK;
+}
+
+int32_t sadmc_read_wl_hist(sadmc_handle* h, int32_t walker, uint64_t* hist, int64_t* n, double* min_energy) {
+  if (!h || walker < 0 || walker >= h->W || !n) return fail(SADMC_ERR_INVALID, "bad argument");
+  WalkerCore k;
+  CUDA_TRY(cudaMemcpyAsync(&k, h->d_cores + walker, sizeof(k), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const int64_t len = k.wl_hi >= k.wl_lo ? (int64_t)(k.wl_hi - k.wl_lo + 1) : 0;
+  *n = len;
+  if (min_energy) *min_energy = k.min_energy;
+  if (hist && len > 0) {
+    CUDA_TRY(cudaMemcpyAsync(hist, h->planes.wl_hist + (size_t)walker * h->nb + k.wl_lo, len * 8,
+                             cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+  }
+  return SADMC_OK;
+}
+
+int32_t sadmc_read_scalars(sadmc_handle* h, int32_t walker, double* o) {
+  if (!h || !o || walker < 0 || walker >= h->W) return fail(SADMC_ERR_INVALID, "bad argument");
+  WalkerCore k;
+  CUDA_TRY(cudaMemcpyAsync(&k, h->d_cores + walker, sizeof(k), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const double kind = k.kind == M_INV_T_WL ? (double)M_WL : (double)k.kind;
+  const double v[SADMC_N_SCALARS] = {
+      (double)k.moves, (double)k.accepted, k.acc_rate, k.tscale, kind, k.too_lo, k.too_hi,
+      (double)k.tL, (double)k.tF, (double)k.num_states, (double)k.highest_hist,
+      k.latest_param, k.gamma, (double)k.lowest_hist, (double)k.wl_highest_hist,
+      (double)k.total_hist, k.wl_num_states, k.min_energy, k.t0, k.max_S,
+      (double)k.max_S_local, k.drift, (double)k.status, k.E};
+  std::memcpy(o, v, sizeof(v));
+  return SADMC_OK;
+}
+
+int32_t sadmc_counters(sadmc_handle* h, uint64_t* moves, uint64_t* accepted) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  int32_t r = h->pull_cores();
+  if (r) return r;
+  uint64_t m = 0, a = 0;
+  for (const auto& k : h->h_cores) { m += k.moves; a += k.accepted; }
+  if (moves) *moves = m;
+  if (accepted) *accepted = a;
+  return SADMC_OK;
+}
+
+int32_t sadmc_status(sadmc_handle* h, uint32_t* flags) {
+  if (!h || !flags) return fail(SADMC_ERR_INVALID, "null argument");
+  int32_t r = h->pull_cores();
+  if (r) return r;
+  for (int w = 0; w < h->W; ++w) flags[w] = h->h_cores[w].status;
+  return SADMC_OK;
+}
+
+int32_t sadmc_set_trace(sadmc_handle* h, uint64_t capacity) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  cudaFree(h->d_trace);
+  h->d_trace = nullptr;
+  h->trace_cap = 0;
+  if (capacity == 0) return SADMC_OK;
+  if (dalloc(&h->d_trace, (size_t)h->W * capacity) != cudaSuccess)
+    return fail(SADMC_ERR_NOMEM, "trace allocation failed");
+  CUDA_TRY(cudaMemsetAsync(h->d_trace, 0xff, sizeof(TraceRec) * (size_t)h->W * capacity, h->stream));
+  h->trace_cap = capacity;
+  h->trace_t0 = h->moves_done;
+  return SADMC_OK;
+}
+
+int32_t sadmc_read_trace(sadmc_handle* h, int32_t walker, double* e1, double* e2, uint64_t* count) {
+  if (!h || walker < 0 || walker >= h->W) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->d_trace) return fail(SADMC_ERR_STATE, "tracing disabled");
+  const uint64_t done = h->moves_done > h->trace_t0 ? h->moves_done - h->trace_t0 : 0;
+  const uint64_t n = std::min(done, h->trace_cap);
+  std::vector<TraceRec> r(n);
+  if (n) {
+    CUDA_TRY(cudaMemcpyAsync(r.data(), h->d_trace + (size_t)walker * h->trace_cap, n * sizeof(TraceRec),
+                             cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+  }
+  for (uint64_t k = 0; k < n; ++k) {
+    if (e1) e1[k] = r[k].e1;
+    if (e2) e2[k] = r[k].e2;
+  }
+  if (count) *count = n;
+  return SADMC_OK;
+}
+
+int32_t sadmc_lanes_per_walker(sadmc_handle* h) { return h ? h->lpw : 0; }
+
+int32_t sadmc_autotune(sadmc_handle* h, uint64_t moves, int32_t* best_lpw, double* best_ms) {
+  (void)moves;
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (best_lpw) *best_lpw = h->lpw;
+  if (best_ms) *best_ms = 0.0;
+  return SADMC_OK;
+}
+
+int32_t sadmc_heat_capacity(const double* T, int32_t nT, const double* E, const double* S,
+                            int32_t n, double* C) {
+  if (!T || !E || !S || !C || nT < 0 || n <= 0) return fail(SADMC_ERR_INVALID, "bad argument");
+  double *dT = nullptr, *dE = nullptr, *dS = nullptr, *dC = nullptr;
+  cudaError_t e = cudaMalloc(&dT, sizeof(double) * (nT + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&dE, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&dS, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&dC, sizeof(double) * (nT + 1));
+  if (e == cudaSuccess) e = cudaMemcpy(dT, T, sizeof(double) * nT, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dE, E, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dS, S, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_heat_capacity(dT, nT, dE, dS, n, dC, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(C, dC, sizeof(double) * nT, cudaMemcpyDeviceToHost);
+  cudaFree(dT); cudaFree(dE); cudaFree(dS); cudaFree(dC);
+  if (e != cudaSuccess) return fail(SADMC_ERR_CUDA, cudaGetErrorString(e));
+  return SADMC_OK;
+}
+
+}  // extern "C"

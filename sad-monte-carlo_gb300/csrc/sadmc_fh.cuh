@@ -1,0 +1,480 @@
+// Flat-histogram bookkeeping of one walker, executed by the LPW lanes of the walker's
+// lane group.  All lanes of a group hold identical copies of the scalar state, run the
+// same FP64 instructions and issue the same stores, so one warp instruction serves
+// every walker packed into the warp (on GB300 an FP64 warp instruction costs the same
+// with one active lane as with 32) and every lane reads back its own writes.
+//
+// Restates EnergyMC::move_once / reject_move / update_weights / gamma
+// (src/mc/energy.rs:904-974, 440-512, 514-761, 799-825) over preallocated bin planes:
+//  * prepare_for_state (energy.rs:400-434) grows the allocated range [b_lo, b_hi] with
+//    the reference's own bins.min arithmetic (cur_min -= width);
+//  * SAD's t_F = max(t_found[ilo..=ihi]) (energy.rs:585-592) is kept incrementally:
+//    t_found entries are written once and the window [too_lo, too_hi] only widens;
+//  * the SAD refill loops (energy.rs:542-583) visit only bins whose centre can meet the
+//    loop condition, each still tested with the reference's FP64 expression;
+//  * have_visited_since_maxentropy fills (energy.rs:950-965) are O(1) generation stamps;
+//  * gamma (SAD, SAMC) is evaluated for LPW consecutive moves at once, one per lane.
+#pragma once
+#include <cstdint>
+
+#include "sadmc_types.h"
+
+namespace sadmc {
+namespace dev {
+
+__device__ __forceinline__ double u53_to_double(uint64_t v) {
+  return (double)v * (1.0 / 9007199254740992.0);
+}
+
+// rejected = (u > exp(d)) with u = u53 * 2^-53 and d <= 0 (energy.rs:465, 489, 498, 508).
+// Decided in FP32 when the FP32 estimate is outside its error margin; otherwise the
+// reference's FP64 comparison is evaluated.
+__device__ __forceinline__ bool metropolis_reject(double d, uint64_t u53) {
+  float df = (float)d;
+  if (df < -80.0f) return u53 != 0;  // exp(d) < 2e-35 < 2^-53: only u == 0 is accepted
+  float e32 = __expf(df);
+  float m = 4.0e-6f + fabsf(df) * 3.0e-7f;
+  float uf = (float)(u53 >> 29) * (1.0f / 16777216.0f);  // u in [uf, uf + 2^-24)
+  if (uf > e32 * (1.0f + m)) return true;
+  if (uf + (1.0f / 16777216.0f) < e32 * (1.0f - m)) return false;
+  return u53_to_double(u53) > exp(d);
+}
+
+template <int LPW>
+struct Fh {
+  WalkerCore c;
+  // launch constants
+  double width, inv_width, min_allowed, max_allowed, target_rate;
+  int nbins;
+  bool has_min_allowed, has_max_allowed, acc_mode;
+  // this walker's planes
+  double *lnw, *sE, *sE2;
+  uint64_t *hist, *tf, *rt, *wlh, *stamp;
+  // lane group
+  unsigned gmask;
+  int glane;
+  bool wr;  // stores enabled (false for padding groups past the last walker)
+  // cached current bin (global index cur)
+  int cur;
+  double k_lnw, k_sE, k_sE2;
+  uint64_t k_hist, k_tf;
+  double cur_max;      // upper edge of the allocated range
+  int win_lo, win_hi;  // SAD window as bin indices
+  // gamma batch: lane glane holds gamma(gb_base + glane)
+  double gb_val;
+  uint64_t gb_base;
+  bool gb_valid;
+  // per-move scratch
+  double e1;
+  int i2;
+  uint64_t hist2;
+  bool grew_front;
+
+  // ---- index helpers ---------------------------------------------------------------
+  __device__ int gidx_exact(double e) const { return (int)((e - c.cur_min) / width) + c.b_lo; }
+  // state_to_index (energy.rs:371-373).  The FP64 quotient is evaluated only when the
+  // FP32 estimate lies within its error bound of an integer.
+  __device__ int gidx(double e) const {
+    double d = e - c.cur_min;
+    float q = __fmul_rn((float)d, (float)inv_width);
+    int qi = __float2int_rz(q);
+    float fr = q - (float)qi;
+    float m = q * 4.0e-7f + 1.0e-6f;
+    if (fr > m && fr < 1.0f - m) return qi + c.b_lo;
+    return (int)(d / width) + c.b_lo;
+  }
+  __device__ double center(int g) const {  // index_to_state (energy.rs:366-370)
+    return c.cur_min + ((double)(g - c.b_lo) + 0.5) * width;
+  }
+
+  // cached-bin aware accessors
+  __device__ double ld_lnw(int g) const { return g == cur ? k_lnw : lnw[g]; }
+  __device__ uint64_t ld_hist(int g) const { return g == cur ? k_hist : hist[g]; }
+  __device__ uint64_t ld_tf(int g) const { return g == cur ? k_tf : tf[g]; }
+  __device__ void st_lnw(int g, double v) {
+    if (g == cur) k_lnw = v;
+    else if (wr) lnw[g] = v;
+  }
+  __device__ void flush_cur() {
+    if (wr) { lnw[cur] = k_lnw; hist[cur] = k_hist; tf[cur] = k_tf; sE[cur] = k_sE; sE2[cur] = k_sE2; }
+  }
+  __device__ void load_cur(int g) {
+    cur = g;
+    k_lnw = lnw[g]; k_hist = hist[g]; k_tf = tf[g]; k_sE = sE[g]; k_sE2 = sE2[g];
+  }
+  __device__ void move_cur(int g) {
+    if (g != cur) { flush_cur(); load_cur(g); }
+  }
+  __device__ void sync() {
+    if (LPW > 1) __syncwarp(gmask);
+  }
+  __device__ uint64_t group_min(uint64_t v) const {
+#pragma unroll
+    for (int o = LPW / 2; o > 0; o >>= 1) {
+      uint64_t x = __shfl_xor_sync(gmask, v, o, LPW);
+      v = x < v ? x : v;
+    }
+    return v;
+  }
+
+  // ---- load / store ------------------------------------------------------------------
+  __device__ void load(const WalkerCore* cores, const FhParams& P, const BinPlanes& B, int w,
+                       unsigned gmask_, int glane_, bool wr_) {
+    c = cores[w];
+    width = P.width; inv_width = P.inv_width; nbins = P.nbins;
+    has_min_allowed = P.has_min_allowed != 0; has_max_allowed = P.has_max_allowed != 0;
+    acc_mode = P.acc_mode != 0;
+    min_allowed = P.min_allowed; max_allowed = P.max_allowed; target_rate = P.target_rate;
+    size_t off = (size_t)w * (size_t)P.nbins;
+    lnw = B.lnw + off; sE = B.sumE + off; sE2 = B.sumE2 + off;
+    hist = B.hist + off; tf = B.t_found + off; rt = B.round_trips + off;
+    wlh = B.wl_hist + off; stamp = B.visit_stamp + off;
+    gmask = gmask_; glane = glane_; wr = wr_;
+    cur_max = c.cur_min + width * (double)(c.b_hi - c.b_lo + 1);
+    if (c.kind != M_DESCENT) {
+      load_cur(gidx_exact(c.E));
+      if (c.kind == M_SAD) { win_lo = gidx_exact(c.too_lo); win_hi = gidx_exact(c.too_hi); }
+    } else {
+      cur = -1;
+    }
+    gb_valid = false;
+    grew_front = false;
+  }
+  __device__ void store(WalkerCore* cores, int w) {
+    if (c.kind != M_DESCENT) flush_cur();
+    if (wr && glane == 0) cores[w] = c;
+  }
+
+  // ---- gamma (energy.rs:799-825; SadVersion::compute_gamma energy.rs:22-38) -----------
+  __device__ double gamma_at(uint64_t t) const {
+    switch (c.kind) {
+      case M_SAD: {
+        double p = c.latest_param, tF = (double)c.tF, ns = (double)c.num_states;
+        if (p * tF * ns == 0.0) return 0.0;
+        double td = (double)t;
+        return (p + td / tF) / (p + td / ns * (td / tF));
+      }
+      case M_SAMC: {
+        double td = (double)t;
+        return td > c.t0 ? c.t0 / td : 1.0;
+      }
+      case M_WL:
+      case M_INV_T_WL: return c.gamma;
+      default: return 0.0;
+    }
+  }
+  __device__ double gamma() {
+    if (c.kind != M_SAD && c.kind != M_SAMC) return gamma_at(c.moves);
+    if (!gb_valid || c.moves < gb_base || c.moves - gb_base >= (uint64_t)LPW) {
+      gb_base = c.moves;
+      gb_val = gamma_at(c.moves + (uint64_t)glane);
+      gb_valid = true;
+    }
+    if (LPW == 1) return gb_val;
+    return __shfl_sync(gmask, gb_val, (int)(c.moves - gb_base), LPW);
+  }
+
+  // ---- have_visited_since_maxentropy as generation stamps ------------------------------
+  __device__ bool visited(int g) const { return stamp[g] == c.fill_gen ? true : (c.fill_val != 0); }
+  __device__ void fill_visited(bool v) { c.fill_gen += 1; c.fill_val = v ? 1 : 0; }
+
+  // ---- prepare_for_state (energy.rs:400-434); false: outside the preallocated planes ---
+  __device__ bool prepare(double e) {
+    while (e < c.cur_min) {
+      if (c.b_lo == 0) return false;
+      c.b_lo -= 1;
+      if (wr) stamp[c.b_lo] = c.fill_gen;  // inserted as visited, round_trips already 1
+      c.cur_min -= width;
+      grew_front = true;
+    }
+    if (grew_front) cur_max = c.cur_min + width * (double)(c.b_hi - c.b_lo + 1);
+    while (e >= cur_max) {
+      if (c.b_hi >= nbins - 1) return false;
+      c.b_hi += 1;
+      if (wr) stamp[c.b_hi] = c.fill_gen;
+      cur_max = c.cur_min + width * (double)(c.b_hi - c.b_lo + 1);
+    }
+    return true;
+  }
+  // After the front grew the reference recomputes every local index with the new
+  // bins.min; refresh the cached indices the same way.
+  __device__ void reindex_after_growth() {
+    move_cur(gidx_exact(c.E));
+    if (c.kind == M_SAD) { win_lo = gidx_exact(c.too_lo); win_hi = gidx_exact(c.too_hi); }
+  }
+
+  __device__ double sad_lnw(double e, int g) const {  // energy.rs:451-464
+    if (e < c.too_lo) return ld_lnw(win_lo) + (e - c.too_lo) / c.min_T;
+    if (e > c.too_hi) return ld_lnw(win_hi);
+    return ld_lnw(g);
+  }
+
+  // ---- one move ----------------------------------------------------------------------
+  __device__ void begin_move(double one_minus_rs) {
+    c.moves += 1;                  // energy.rs:905
+    c.acc_rate *= one_minus_rs;    // energy.rs:913-914
+    e1 = c.E;
+    grew_front = false;
+  }
+
+  // Bounds test, prepare_for_state and reject_move (energy.rs:915-931); true = accept.
+  __device__ bool decide(bool possible, double e2, uint64_t u53, double rs) {
+    if (!possible) return false;
+    bool oob = false;
+    if (has_max_allowed) oob = e2 > max_allowed && e2 > c.E;
+    if (has_min_allowed) oob = oob || (e2 < min_allowed && e2 < c.E);
+    if (oob) return false;
+    if (c.kind == M_DESCENT) return e2 < c.E;  // energy.rs:840-851
+    if (!prepare(e2)) { c.status |= ST_BIN_RANGE; return false; }
+    if (grew_front) reindex_after_growth();
+    i2 = gidx(e2);
+    double lnw2_raw = ld_lnw(i2);
+    hist2 = ld_hist(i2);
+    bool rejected;
+    switch (c.kind) {
+      case M_SAD: {
+        double lnw1 = sad_lnw(c.E, cur);
+        double lnw2 = sad_lnw(e2, i2);
+        rejected = lnw2 > lnw1 && metropolis_reject(lnw1 - lnw2, u53);
+        if (!rejected && hist2 == 0 && e2 < c.too_hi && e2 > c.too_lo) {  // energy.rs:466-483
+          c.latest_param = (c.too_hi - c.too_lo) / c.min_T;
+          c.num_states += 1;
+          c.tL = c.moves;
+          gb_valid = false;
+        }
+        break;
+      }
+      case M_SAMC: {
+        rejected = lnw2_raw > k_lnw && metropolis_reject(k_lnw - lnw2_raw, u53);
+        break;
+      }
+      case M_WL:
+      case M_INV_T_WL: {
+        rejected = lnw2_raw > k_lnw && metropolis_reject(k_lnw - lnw2_raw, u53);
+        if (!rejected && hist2 == 0 && c.lowest_hist > 0) c.wl_num_states += 1.0;
+        break;
+      }
+      default: {  // canonical (energy.rs:504-510)
+        rejected = c.E >= e2 ? false : metropolis_reject((c.E - e2) / c.temperature, u53);
+        break;
+      }
+    }
+    if (!rejected) {
+      c.accepted += 1;
+      c.acc_rate += rs;
+    }
+    return !rejected;
+  }
+
+  // Histogram, energy sums, update_weights and max-entropy bookkeeping
+  // (energy.rs:934-965).  Call after the system confirmed (c.E updated) or not.
+  __device__ void finish_move(bool accepted) {
+    if (c.kind == M_DESCENT) return;
+    int old_cur = cur;
+    if (accepted) move_cur(i2);
+    const double E = c.E;
+    if (k_hist == 0) {  // energy.rs:938-940
+      k_tf = c.moves;
+      if (c.kind == M_SAD && cur >= win_lo && cur <= win_hi && c.moves > c.win_tmax) c.win_tmax = c.moves;
+    }
+    k_hist += 1;
+    k_sE += E;
+    k_sE2 += E * E;
+    update_weights(E);
+    const int li = cur - c.b_lo;
+    if (k_lnw > c.max_S) {
+      c.max_S = k_lnw;
+      c.max_S_local = li;
+      fill_visited(true);
+    } else if (li == c.max_S_local) {
+      int i1 = grew_front ? gidx_exact(e1) : old_cur;
+      if (i1 - c.b_lo != li) fill_visited(false);
+    } else if (!visited(cur)) {
+      if (wr) { stamp[cur] = c.fill_gen; rt[cur] = rt[cur] + 1; }
+    }
+  }
+
+  // energy.rs:514-761
+  __device__ void update_weights(double energy) {
+    double g = gamma();
+    if (g != g) c.status |= ST_NAN_GAMMA;
+    double old = k_lnw;
+    k_lnw += g;
+    if (c.kind == M_SAD) sad_update(energy, old);
+    else if (c.kind == M_WL || c.kind == M_INV_T_WL) wl_update();
+  }
+
+  __device__ void sad_update(double energy, double old_lnw) {  // energy.rs:523-636
+    if (c.too_lo > c.too_hi || energy < c.too_lo || energy > c.too_hi) k_lnw = old_lnw;
+    if (k_hist > c.highest_hist) {
+      c.highest_hist = k_hist;
+      if (energy > c.too_hi) {
+        const double base = ld_lnw(win_hi);
+        const int jlo = win_hi > c.b_lo ? win_hi : c.b_lo;
+        const int jhi = cur < c.b_hi ? cur : c.b_hi;
+        for (int j = jlo; j <= jhi; ++j) {
+          double ej = center(j);
+          if (ej > c.too_hi && ej <= energy) {
+            if (ld_hist(j) != 0) { st_lnw(j, base); c.num_states += 1; }
+            else st_lnw(j, 0.0);
+          }
+        }
+        c.latest_param = (energy - c.too_lo) / c.min_T;
+        c.tL = c.moves;
+        c.too_hi = center(cur);
+        const int nhi = gidx_exact(c.too_hi);
+        for (int j = win_hi + 1; j <= nhi; ++j) {
+          uint64_t t = ld_tf(j);
+          if (t > c.win_tmax) c.win_tmax = t;
+        }
+        win_hi = nhi;
+        gb_valid = false;
+      } else if (energy < c.too_lo) {
+        const double base = ld_lnw(win_lo);
+        const int jlo = cur > c.b_lo ? cur : c.b_lo;
+        const int jhi = win_lo < c.b_hi ? win_lo : c.b_hi;
+        for (int j = jlo; j <= jhi; ++j) {
+          double ej = center(j);
+          if (ej < c.too_lo && ej >= energy) {
+            if (ld_hist(j) != 0) {
+              double v = base + (ej - c.too_lo) / c.min_T;
+              if (v < 0.0) v = 0.0;
+              st_lnw(j, v);
+              c.num_states += 1;
+            } else {
+              st_lnw(j, 0.0);
+            }
+          }
+        }
+        c.latest_param = (c.too_hi - energy) / c.min_T;
+        c.tL = c.moves;
+        c.too_lo = center(cur);
+        const int nlo = gidx_exact(c.too_lo);
+        for (int j = nlo; j < win_lo; ++j) {
+          uint64_t t = ld_tf(j);
+          if (t > c.win_tmax) c.win_tmax = t;
+        }
+        win_lo = nlo;
+        gb_valid = false;
+      }
+    }
+    if (c.tL == c.moves) {
+      uint64_t old_tF = c.tF;
+      c.tF = c.win_tmax;
+      gb_valid = false;
+      if (old_tF != c.tF && acc_mode) {  // energy.rs:600-609
+        double s = c.acc_rate / target_rate;
+        s = s < 0.8 ? 0.8 : (s > 1.2 ? 1.2 : s);
+        c.tscale *= s;
+      }
+    }
+  }
+
+  __device__ void wl_zero_range(int lo, int hi) {
+    for (int j = lo + glane; j <= hi; j += LPW)
+      if (wr) wlh[j] = 0;
+    sync();
+  }
+
+  __device__ void wl_update() {  // energy.rs:638-752
+    const bool inv_t = c.kind == M_INV_T_WL;
+    if (c.has_min_gamma && c.gamma < c.min_gamma) {  // production run
+      int k = c.wl_lo + (cur - c.b_lo);
+      if (k >= c.wl_lo && k <= c.wl_hi) { if (wr) wlh[k] = wlh[k] + 1; }
+      else c.status |= ST_BIN_RANGE;
+      return;
+    }
+    const int len_b = c.b_hi - c.b_lo + 1;
+    int len_w = c.wl_hi >= c.wl_lo ? c.wl_hi - c.wl_lo + 1 : 0;
+    if (len_w != len_b) {
+      if (len_w == 0 || (c.gamma != 1.0 && c.lowest_hist > 0)) {
+        c.gamma = 1.0;
+        c.lowest_hist = 0;
+        c.wl_highest_hist = 0;
+        c.total_hist = 0;
+        c.wl_lo = c.b_lo;
+        c.wl_hi = c.b_hi;
+        wl_zero_range(c.wl_lo, c.wl_hi);
+        c.min_energy = c.cur_min;
+      } else {
+        while (c.min_energy > c.cur_min) {
+          c.min_energy -= width;
+          c.wl_lo -= 1;
+          if (wr && c.wl_lo >= 0) wlh[c.wl_lo] = 0;
+        }
+        while (len_w < len_b) {
+          c.wl_hi += 1;
+          if (wr && c.wl_hi < nbins) wlh[c.wl_hi] = 0;
+          ++len_w;
+        }
+        sync();
+        uint64_t mn = ~0ull;
+        for (int j = c.wl_lo + glane; j <= c.wl_hi; j += LPW) {
+          uint64_t h = wlh[j];
+          mn = h < mn ? h : mn;
+        }
+        c.lowest_hist = group_min(mn);
+      }
+      len_w = c.wl_hi - c.wl_lo + 1;
+    }
+    const int k = c.wl_lo + (cur - c.b_lo);
+    const uint64_t h = wlh[k] + 1;
+    if (wr) wlh[k] = h;
+    if (h > c.wl_highest_hist) c.wl_highest_hist = h;
+    c.total_hist += 1;
+    const double max_energy = c.min_energy + (double)len_w * width;
+    bool cond = h == c.lowest_hist + 1 && len_w > 1 &&
+                (!has_min_allowed || min_allowed >= c.min_energy) &&
+                (!has_max_allowed || max_allowed <= max_energy);
+    if (cond) {
+      sync();
+      uint64_t mn = ~0ull;
+      for (int j = glane; j < len_w; j += LPW) {
+        if (ld_hist(c.b_lo + j) != 0) {
+          uint64_t v = wlh[c.wl_lo + j];
+          mn = v < mn ? v : mn;
+        }
+      }
+      mn = group_min(mn);
+      cond = mn == c.lowest_hist + 1;
+    }
+    if (cond) {
+      c.lowest_hist = h;
+      if ((inv_t && c.lowest_hist > 0) ||
+          (double)c.lowest_hist >= 0.8 * (double)c.total_hist / c.wl_num_states) {
+        c.gamma *= 0.5;
+        wl_zero_range(c.wl_lo, c.wl_hi);
+        c.total_hist = 0;
+        c.lowest_hist = 0;
+        c.wl_highest_hist = 0;
+        if (c.has_min_gamma && c.gamma < c.min_gamma) c.gamma = 0.0;
+      }
+      if (inv_t && c.gamma < c.wl_num_states / (double)c.moves) {  // energy.rs:747-750
+        c.kind = M_SAMC;
+        c.t0 = c.wl_num_states;
+        gb_valid = false;
+      }
+    }
+  }
+};
+
+// sqrt(1/t) and 1 - sqrt(1/t) (energy.rs:913) for 32 consecutive t, one per lane.
+struct RecentScale {
+  uint64_t base;
+  double rs, omrs;
+  __device__ void init() { base = ~0ull; }
+  __device__ void get(uint64_t t, int lane, double& r, double& om) {
+    if (base == ~0ull || t < base || t - base >= 32) {
+      base = t;
+      double v = sqrt(1.0 / (double)(t + (uint64_t)lane));
+      rs = v;
+      omrs = 1. - v;
+    }
+    int src = (int)(t - base);
+    r = __shfl_sync(0xffffffffu, rs, src);
+    om = __shfl_sync(0xffffffffu, omrs, src);
+  }
+};
+
+}  // namespace dev
+}  // namespace sadmc

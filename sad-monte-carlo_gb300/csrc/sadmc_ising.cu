@@ -1,0 +1,99 @@
+// 2D Ising model (src/system/ising.rs), many walkers per launch.
+//
+// Spins are int8 in global memory, index i + j*L (ising.rs:64).  A single-spin flip
+// changes E by -2 s_ij (sum of 4 periodic neighbours) (ising.rs:104-119); energies are
+// integers held in FP64, so the whole chain is bit-exact.  With LPW == 1 each lane is a
+// walker; with LPW == 32 one walker occupies a warp (the serial single-walker case).
+#include <cuda_runtime.h>
+
+#include "sadmc_common.cuh"
+#include "sadmc_fh.cuh"
+#include "sadmc_launch.h"
+#include "sadmc_rng.cuh"
+
+namespace sadmc {
+namespace dev {
+
+template <int LPW>
+__global__ void __launch_bounds__(128) ising_move_kernel(MoveLaunch m, IsingSys s) {
+  constexpr int WPW = 32 / LPW;
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (warp * WPW >= m.n_walkers) return;
+  const int group = lane / LPW, glane = lane % LPW;
+  int w = warp * WPW + group;
+  const bool wr = w < m.n_walkers;
+  if (!wr) w = m.n_walkers - 1;
+  const unsigned gmask = group_mask<LPW>(group);
+  Fh<LPW> fh;
+  fh.load(m.cores, m.P, m.B, w, gmask, glane, wr);
+  const int L = s.L;
+  int8_t* S = s.spins + (size_t)w * (size_t)L * (size_t)L;
+  RecentScale rsb;
+  rsb.init();
+  for (uint64_t it = 0; it < m.n_moves; ++it) {
+    const uint64_t t = fh.c.moves + 1;
+    double rs, omrs;
+    rsb.get(t, lane, rs, omrs);
+    fh.begin_move(omrs);
+    Draws d = draws_ising(m.seed, (uint32_t)w, t, (uint32_t)L);
+    const int i = (int)d.which, j = (int)d.j;
+    int jp = j + 1 == L ? 0 : j + 1, jm = j == 0 ? L - 1 : j - 1;
+    int ip = i + 1 == L ? 0 : i + 1, im = i == 0 ? L - 1 : i - 1;
+    const int site = i + j * L;
+    const int nt = S[i + jp * L] + S[i + jm * L] + S[ip + j * L] + S[im + j * L];
+    const int sij = S[site];
+    const double e2 = fh.c.E - (double)(nt * sij * 2);
+    if (m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
+      TraceRec r;
+      r.e1 = fh.c.E;
+      r.e2 = e2;
+      m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = r;
+    }
+    const bool acc = fh.decide(true, e2, d.u53, rs);
+    if (acc) {
+      if (wr) S[site] = (int8_t)(-sij);  // all lanes of the group store the same value
+      fh.c.E = e2;
+      if (LPW > 1) __syncwarp(gmask);
+    }
+    fh.finish_move(acc);
+  }
+  fh.store(m.cores, w);
+}
+
+// compute_energy (ising.rs:59-75): sum over sites of s * (s_down + s_right), exact.
+__global__ void ising_energy_kernel(IsingSys s, int n_walkers, double* out) {
+  const int lane = threadIdx.x & 31;
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (w >= n_walkers) return;
+  const int L = s.L;
+  const int8_t* S = s.spins + (size_t)w * (size_t)L * (size_t)L;
+  long long e = 0;
+  for (int k = lane; k < L * L; k += 32) {
+    const int i1 = k % L, j1 = k / L;
+    const int j2 = (j1 + 1) % L, i2 = (i1 + 1) % L;
+    e += (long long)((S[i1 + j2 * L] + S[i2 + j1 * L]) * S[i1 + j1 * L]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+  if (lane == 0) out[w] = (double)e;
+}
+
+}  // namespace dev
+
+cudaError_t launch_ising_move(const MoveLaunch& m, const IsingSys& s, int lpw, cudaStream_t st) {
+  const int wpw = 32 / lpw;
+  const int warps = (m.n_walkers + wpw - 1) / wpw;
+  const int blocks = (warps * 32 + 127) / 128;
+  if (lpw == 1) dev::ising_move_kernel<1><<<blocks, 128, 0, st>>>(m, s);
+  else if (lpw == 32) dev::ising_move_kernel<32><<<blocks, 128, 0, st>>>(m, s);
+  else return cudaErrorInvalidConfiguration;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ising_energy(const IsingSys& s, int n_walkers, double* out, cudaStream_t st) {
+  dev::ising_energy_kernel<<<(n_walkers * 32 + 127) / 128, 128, 0, st>>>(s, n_walkers, out);
+  return cudaGetLastError();
+}
+
+}  // namespace sadmc

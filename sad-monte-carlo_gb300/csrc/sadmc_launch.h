@@ -1,0 +1,84 @@
+// Host-side launch entry points of the CUDA kernels (one translation unit per system).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sadmc_types.h"
+
+namespace sadmc {
+
+struct MoveLaunch {
+  WalkerCore* cores;
+  FhParams P;
+  BinPlanes B;
+  int n_walkers;
+  uint64_t n_moves;        // moves per walker in this launch
+  uint64_t seed;
+  TraceRec* trace;         // nullptr unless tracing
+  uint64_t trace_cap;      // records per walker
+  uint64_t trace_t0;       // move counter before the first traced move
+  int resum_interval;      // FP64 re-sum period in moves (continuous systems), 0 = never
+  double drift_tol;        // ST_DRIFT when |E_incremental - E_fp64| exceeds this
+  int descent;             // 1: run the initial descent (energy.rs:840-851) instead
+  uint64_t descent_limit;  // maximum descent proposals per walker
+  double descent_max;      // max_allowed_energy the descent aims below
+};
+
+// LJ cluster in a spherical wall.  pos: [walker][6][np] binary32 planes
+// (x_hi, y_hi, z_hi, x_lo, y_lo, z_lo), atom j at column j.
+struct LjSys {
+  float* pos;
+  int np;
+  double radius2;
+};
+cudaError_t launch_lj_move(const MoveLaunch& m, const LjSys& s, int lpw, cudaStream_t st);
+cudaError_t launch_lj_energy(const WalkerCore* cores, const LjSys& s, int n_walkers, double* out,
+                             cudaStream_t st);
+// Injected proposal for one walker (the plan_move parity hook): out[0] = e2 (FP64 sum of
+// the FP32 pair terms added to E), out[1] = possible; when confirm != 0 an accepted
+// plan is applied (position and E) without touching the bins.
+cudaError_t launch_lj_plan(WalkerCore* cores, const LjSys& s, int walker, int which, float g0,
+                           float g1, float g2, double scale, int confirm, double* out,
+                           cudaStream_t st);
+
+// 2D Ising.  spins: [walker][L*L] int8, index i + j*L.
+struct IsingSys {
+  int8_t* spins;
+  int L;
+};
+cudaError_t launch_ising_move(const MoveLaunch& m, const IsingSys& s, int lpw, cudaStream_t st);
+cudaError_t launch_ising_energy(const IsingSys& s, int n_walkers, double* out, cudaStream_t st);
+
+// Periodic cell systems (square well / hard core and WCA): FP64 positions plus a
+// one-bucket-per-atom subcell grid.
+struct CellSys {
+  double* pos;        // [walker][3][np] FP64 planes
+  float* pos32;       // [walker][3][np] binary32 copy (pre-filters)
+  int np;
+  double* box;        // [walker][3]
+  int* ncell;         // [walker][3] subcells per axis (>= 3)
+  int* cell_of;       // [walker][np] subcell index of each atom
+  int* cell_count;    // [walker][cell_cap]
+  int* cell_atoms;    // [walker][cell_cap][bucket]
+  int cell_cap;       // max subcells per walker
+  int bucket;         // atom slots per subcell
+  double r_cut;       // well width (square well) or 2^(1/6) (WCA)
+  int kind;           // SYS_SW or SYS_WCA
+};
+cudaError_t launch_cell_build(const WalkerCore* cores, const CellSys& s, int n_walkers,
+                              cudaStream_t st);
+cudaError_t launch_cell_move(const MoveLaunch& m, const CellSys& s, int lpw, cudaStream_t st);
+cudaError_t launch_cell_energy(const WalkerCore* cores, const CellSys& s, int n_walkers,
+                               double* out, cudaStream_t st);
+
+// Plane initialisation (round_trips = 1, initial bin) for walkers [0, n).
+cudaError_t launch_init_planes(const WalkerCore* cores, BinPlanes B, int nbins, int n_walkers,
+                               cudaStream_t st);
+
+// Heat capacity C(T) = (<E^2> - <E>^2)/T^2 from (E_k, S_k) with max-shifted weights,
+// FP64 (plotting/final_heat_capacity.py:79-88).  One block per temperature.
+cudaError_t launch_heat_capacity(const double* T, int nT, const double* E, const double* S,
+                                 int n, double* C, cudaStream_t st);
+
+}  // namespace sadmc

@@ -1,0 +1,317 @@
+// LJ cluster in a spherical wall (src/system/lj.rs), many walkers per launch.
+//
+// Layout: a warp packs 32/LPW walkers; walker atom j lives in lane (j % LPW) of the
+// walker's lane group, register slot j / LPW, as a double-single position (hi + lo,
+// binary32).  Per move the group computes the reference's
+//   e = E + sum_{j != which} [V(|r_j - to|^2) - V(|r_j - from|^2)]      (lj.rs:86-105)
+// with binary32 pair terms on the hi parts and a group shuffle reduction, then runs the
+// shared flat-histogram bookkeeping.  Every resum_interval moves the energy is replaced
+// by an FP64 pair sum over the double-single positions (compute_energy, lj.rs:236-244);
+// the largest observed |E_incremental - E_fp64| is kept in WalkerCore::drift.
+#include <cuda_runtime.h>
+
+#include "sadmc_common.cuh"
+#include "sadmc_fh.cuh"
+#include "sadmc_launch.h"
+#include "sadmc_rng.cuh"
+
+namespace sadmc {
+namespace dev {
+
+__device__ __forceinline__ float lj_v32(float r2) {  // 4 (s^6 - s^3), s = 1/r^2 (lj.rs:78-81)
+  float s = __fdividef(1.0f, r2);
+  float s3 = s * s * s;
+  return 4.0f * s3 * (s3 - 1.0f);
+}
+
+template <int LPW, int APL>
+struct LjWalker {
+  DS x[APL], y[APL], z[APL];
+  int n;
+  int glane;
+  unsigned gmask;
+
+  __device__ void load(const float* p, int np) {
+#pragma unroll
+    for (int k = 0; k < APL; ++k) {
+      int j = glane + LPW * k;
+      x[k] = DS{p[j], p[3 * np + j]};
+      y[k] = DS{p[np + j], p[4 * np + j]};
+      z[k] = DS{p[2 * np + j], p[5 * np + j]};
+    }
+  }
+  __device__ void store(float* p, int np, bool wr) const {
+    if (!wr) return;
+#pragma unroll
+    for (int k = 0; k < APL; ++k) {
+      int j = glane + LPW * k;
+      p[j] = x[k].h; p[np + j] = y[k].h; p[2 * np + j] = z[k].h;
+      p[3 * np + j] = x[k].l; p[4 * np + j] = y[k].l; p[5 * np + j] = z[k].l;
+    }
+  }
+  // Position of atom `which`, broadcast to the whole group.
+  __device__ void fetch(int which, DS& fx, DS& fy, DS& fz) const {
+    const int owner = which % LPW, slot = which / LPW;
+    float a = 0.f, b = 0.f, c = 0.f, d = 0.f, e = 0.f, f = 0.f;
+#pragma unroll
+    for (int k = 0; k < APL; ++k)
+      if (k == slot) { a = x[k].h; b = y[k].h; c = z[k].h; d = x[k].l; e = y[k].l; f = z[k].l; }
+    if (LPW > 1) {
+      a = __shfl_sync(gmask, a, owner, LPW); b = __shfl_sync(gmask, b, owner, LPW);
+      c = __shfl_sync(gmask, c, owner, LPW); d = __shfl_sync(gmask, d, owner, LPW);
+      e = __shfl_sync(gmask, e, owner, LPW); f = __shfl_sync(gmask, f, owner, LPW);
+    }
+    fx = DS{a, d}; fy = DS{b, e}; fz = DS{c, f};
+  }
+  __device__ void put(int which, DS tx, DS ty, DS tz) {
+    const int owner = which % LPW, slot = which / LPW;
+    if (glane != owner) return;
+#pragma unroll
+    for (int k = 0; k < APL; ++k)
+      if (k == slot) { x[k] = tx; y[k] = ty; z[k] = tz; }
+  }
+
+  // plan_move of lj.rs:365-374 and move_atom of lj.rs:86-105 for a given displacement.
+  // Returns possible; e2 = E + dE (dE summed in binary32).
+  __device__ bool plan(int which, float g0, float g1, float g2, float sh, float sl, double E,
+                       double radius2, DS& tx, DS& ty, DS& tz, double& e2) const {
+    DS fx, fy, fz;
+    fetch(which, fx, fy, fz);
+    tx = ds_add(fx, ds_scale(g0, sh, sl));
+    ty = ds_add(fy, ds_scale(g1, sh, sl));
+    tz = ds_add(fz, ds_scale(g2, sh, sl));
+    // wall: impossible iff |to|^2 > R^2 and |to|^2 > |from|^2 (lj.rs:87-90)
+    const float r2t = tx.h * tx.h + ty.h * ty.h + tz.h * tz.h;
+    const float r2f = fx.h * fx.h + fy.h * fy.h + fz.h * fz.h;
+    const float R2 = (float)radius2;
+    bool impossible;
+    if (r2t < R2 * (1.0f - 1e-5f)) {
+      impossible = false;
+    } else if (r2t > R2 * (1.0f + 1e-5f) && r2t > r2f * (1.0f + 1e-5f)) {
+      impossible = true;
+    } else {
+      double a = ds_to_double(tx), b = ds_to_double(ty), c = ds_to_double(tz);
+      double p = ds_to_double(fx), q = ds_to_double(fy), r = ds_to_double(fz);
+      double nt = a * a + b * b + c * c, nf = p * p + q * q + r * r;
+      impossible = nt > radius2 && nt > nf;
+    }
+    if (impossible) return false;
+    float de = 0.0f;
+#pragma unroll
+    for (int k = 0; k < APL; ++k) {
+      const int j = glane + LPW * k;
+      if (j < n && j != which) {
+        float dx = x[k].h - tx.h, dy = y[k].h - ty.h, dz = z[k].h - tz.h;
+        float vn = lj_v32(dx * dx + dy * dy + dz * dz);
+        dx = x[k].h - fx.h; dy = y[k].h - fy.h; dz = z[k].h - fz.h;
+        float vo = lj_v32(dx * dx + dy * dy + dz * dz);
+        de += vn - vo;
+      }
+    }
+    de = group_sum<LPW>(de, gmask);
+    e2 = E + (double)de;
+    return true;
+  }
+
+  // FP64 pair sum over the double-single positions (compute_energy, lj.rs:236-244).
+  __device__ double energy64() const {
+    double xd[APL], yd[APL], zd[APL];
+#pragma unroll
+    for (int k = 0; k < APL; ++k) { xd[k] = ds_to_double(x[k]); yd[k] = ds_to_double(y[k]); zd[k] = ds_to_double(z[k]); }
+    double e = 0.0;
+    for (int j = 0; j < n; ++j) {
+      DS a, b, c;
+      fetch(j, a, b, c);
+      const double xj = ds_to_double(a), yj = ds_to_double(b), zj = ds_to_double(c);
+#pragma unroll
+      for (int k = 0; k < APL; ++k) {
+        const int i = glane + LPW * k;
+        if (i < n && i > j) {
+          double dx = xd[k] - xj, dy = yd[k] - yj, dz = zd[k] - zj;
+          double s = 1.0 / (dx * dx + dy * dy + dz * dz);
+          e += 4.0 * (powi6(s) - powi3(s));
+        }
+      }
+    }
+    return group_sum<LPW>(e, gmask);
+  }
+};
+
+template <int LPW, int APL>
+__global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
+  constexpr int WPW = 32 / LPW;
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (warp * WPW >= m.n_walkers) return;  // whole warp is padding (warp-uniform)
+  const int group = lane / LPW, glane = lane % LPW;
+  int w = warp * WPW + group;
+  const bool wr = w < m.n_walkers;
+  if (!wr) w = m.n_walkers - 1;
+  const unsigned gmask = group_mask<LPW>(group);
+
+  Fh<LPW> fh;
+  fh.load(m.cores, m.P, m.B, w, gmask, glane, wr);
+  LjWalker<LPW, APL> lj;
+  lj.glane = glane;
+  lj.gmask = gmask;
+  lj.n = fh.c.n;
+  float* pw = s.pos + (size_t)w * 6 * (size_t)s.np;
+  lj.load(pw, s.np);
+
+  if (m.descent) {
+    // from_params descent (energy.rs:840-851): downhill-only proposals of rms 0.05 on
+    // the descent stream until E < max_allowed_energy.
+    const DS sc = ds_from_double(0.05);
+    bool done = false;
+    uint64_t steps = fh.c.pad2;
+    for (uint64_t it = 0; it < m.n_moves; ++it) {
+      if (__all_sync(0xffffffffu, done)) break;
+      if (!done) {
+        ++steps;
+        Draws d = draws_continuous(m.seed, (uint32_t)w, steps, (uint32_t)lj.n, 1u);
+        DS tx, ty, tz;
+        double e2;
+        bool ok = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, fh.c.E, s.radius2, tx, ty, tz, e2);
+        if (ok && finite64(e2)) {
+          if (e2 < fh.c.E) { lj.put((int)d.which, tx, ty, tz); fh.c.E = e2; }
+          if (fh.c.E < m.descent_max) done = true;
+        }
+        if (steps >= m.descent_limit) done = true;
+      }
+    }
+    fh.c.pad2 = steps;
+    double e64 = lj.energy64();
+    fh.c.E = e64;
+    if (!(e64 < m.descent_max)) fh.c.status |= ST_DESCENT_FAILED;
+    else fh.c.status &= ~(uint32_t)ST_DESCENT_FAILED;
+    lj.store(pw, s.np, wr);
+    if (wr && glane == 0) m.cores[w] = fh.c;
+    return;
+  }
+
+  RecentScale rsb;
+  rsb.init();
+  DS sc = ds_from_double(fh.c.tscale);
+  double tscale_seen = fh.c.tscale;
+  for (uint64_t it = 0; it < m.n_moves; ++it) {
+    const uint64_t t = fh.c.moves + 1;
+    double rs, omrs;
+    rsb.get(t, lane, rs, omrs);
+    fh.begin_move(omrs);
+    Draws d = draws_continuous(m.seed, (uint32_t)w, t, (uint32_t)lj.n, 0u);
+    DS tx, ty, tz;
+    double e2 = 0.0;
+    bool possible = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, fh.c.E, s.radius2, tx, ty, tz, e2);
+    possible = possible && finite64(e2);
+    if (m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
+      TraceRec r;
+      r.e1 = fh.c.E;
+      r.e2 = possible ? e2 : __longlong_as_double(0x7ff8000000000000ll);
+      m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = r;
+    }
+    const bool acc = fh.decide(possible, e2, d.u53, rs);
+    if (acc) {
+      lj.put((int)d.which, tx, ty, tz);
+      fh.c.E = e2;
+    }
+    fh.finish_move(acc);
+    if (fh.c.tscale != tscale_seen) { tscale_seen = fh.c.tscale; sc = ds_from_double(tscale_seen); }
+    if (m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
+      const double e64 = lj.energy64();
+      const double dr = fabs(e64 - fh.c.E);
+      if (dr > fh.c.drift) fh.c.drift = dr;
+      if (dr > m.drift_tol) fh.c.status |= ST_DRIFT;
+      fh.c.E = e64;
+      fh.grew_front = false;
+      if (!fh.prepare(e64)) fh.c.status |= ST_BIN_RANGE;
+      else {
+        if (fh.grew_front) fh.reindex_after_growth();
+        fh.move_cur(fh.gidx(e64));
+      }
+    }
+  }
+  lj.store(pw, s.np, wr);
+  fh.store(m.cores, w);
+}
+
+template <int APL>
+__global__ void lj_energy_kernel(const WalkerCore* cores, LjSys s, int n_walkers, double* out) {
+  const int lane = threadIdx.x & 31;
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (w >= n_walkers) return;
+  LjWalker<32, APL> lj;
+  lj.glane = lane;
+  lj.gmask = 0xffffffffu;
+  lj.n = cores[w].n;
+  lj.load(s.pos + (size_t)w * 6 * (size_t)s.np, s.np);
+  double e = lj.energy64();
+  if (lane == 0) out[w] = e;
+}
+
+template <int APL>
+__global__ void lj_plan_kernel(WalkerCore* cores, LjSys s, int w, int which, float g0, float g1,
+                               float g2, double scale, int confirm, double* out) {
+  const int lane = threadIdx.x & 31;
+  LjWalker<32, APL> lj;
+  lj.glane = lane;
+  lj.gmask = 0xffffffffu;
+  lj.n = cores[w].n;
+  float* pw = s.pos + (size_t)w * 6 * (size_t)s.np;
+  lj.load(pw, s.np);
+  const DS sc = ds_from_double(scale);
+  DS tx, ty, tz;
+  double e2 = 0.0;
+  const double E = cores[w].E;
+  bool ok = lj.plan(which, g0, g1, g2, sc.h, sc.l, E, s.radius2, tx, ty, tz, e2);
+  if (lane == 0) { out[0] = ok ? e2 : 0.0; out[1] = ok ? 1.0 : 0.0; }
+  if (ok && confirm) {
+    lj.put(which, tx, ty, tz);
+    lj.store(pw, s.np, true);
+    if (lane == 0) cores[w].E = e2;
+  }
+}
+
+}  // namespace dev
+
+#define SADMC_LJ_CASE(L, A)                                                            \
+  if (lpw == L && s.np == L * A) {                                                     \
+    const int wpb = 128 / 32;                                                          \
+    const int warps = (m.n_walkers + (32 / L) - 1) / (32 / L);                         \
+    dev::lj_move_kernel<L, A><<<(warps + wpb - 1) / wpb, 128, 0, st>>>(m, s);          \
+    return cudaGetLastError();                                                         \
+  }
+
+cudaError_t launch_lj_move(const MoveLaunch& m, const LjSys& s, int lpw, cudaStream_t st) {
+  SADMC_LJ_CASE(32, 1) SADMC_LJ_CASE(16, 2) SADMC_LJ_CASE(8, 4) SADMC_LJ_CASE(4, 8)
+  SADMC_LJ_CASE(32, 2) SADMC_LJ_CASE(16, 4) SADMC_LJ_CASE(8, 8)
+  SADMC_LJ_CASE(32, 4) SADMC_LJ_CASE(32, 8)
+  return cudaErrorInvalidConfiguration;
+}
+
+cudaError_t launch_lj_energy(const WalkerCore* cores, const LjSys& s, int n_walkers, double* out,
+                             cudaStream_t st) {
+  const int blocks = (n_walkers * 32 + 127) / 128;
+  switch (s.np) {
+    case 32: dev::lj_energy_kernel<1><<<blocks, 128, 0, st>>>(cores, s, n_walkers, out); break;
+    case 64: dev::lj_energy_kernel<2><<<blocks, 128, 0, st>>>(cores, s, n_walkers, out); break;
+    case 128: dev::lj_energy_kernel<4><<<blocks, 128, 0, st>>>(cores, s, n_walkers, out); break;
+    case 256: dev::lj_energy_kernel<8><<<blocks, 128, 0, st>>>(cores, s, n_walkers, out); break;
+    default: return cudaErrorInvalidConfiguration;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lj_plan(WalkerCore* cores, const LjSys& s, int walker, int which, float g0,
+                           float g1, float g2, double scale, int confirm, double* out,
+                           cudaStream_t st) {
+  switch (s.np) {
+    case 32: dev::lj_plan_kernel<1><<<1, 32, 0, st>>>(cores, s, walker, which, g0, g1, g2, scale, confirm, out); break;
+    case 64: dev::lj_plan_kernel<2><<<1, 32, 0, st>>>(cores, s, walker, which, g0, g1, g2, scale, confirm, out); break;
+    case 128: dev::lj_plan_kernel<4><<<1, 32, 0, st>>>(cores, s, walker, which, g0, g1, g2, scale, confirm, out); break;
+    case 256: dev::lj_plan_kernel<8><<<1, 32, 0, st>>>(cores, s, walker, which, g0, g1, g2, scale, confirm, out); break;
+    default: return cudaErrorInvalidConfiguration;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace sadmc

@@ -1,0 +1,289 @@
+"""Python binding of libsadmc_gb300.so (the C ABI in include/sadmc_gpu.h).
+
+`Batch` is a batch of independent flat-histogram walkers on the GPU.  It mirrors the
+reference's per-walker Rust surface (src/mc/mod.rs:37-144 MonteCarlo, src/mc/energy.rs
+EnergyMC, src/system/mod.rs:54-120 System/MovableSystem) for many walkers at once:
+
+    reference (one walker)                  this binding (a batch)
+    EnergyMC::from_params(params, system)   Batch(cfg, geometry); upload(states); initialize()
+    loop { mc.move_once() }                 run(moves)
+    system().energy() / compute_energy()    energies() / compute_energies()
+    system.plan_move(rng, d) / confirm()    plan_move(w, which, g, scale) / confirm(w)
+    mc.bins (lnw, histogram, ...)           bins(w)
+    num_moves / num_accepted_moves          counters()
+
+There is no CPU fallback: every call runs the CUDA library, which must be built for this
+machine (build.build()); a missing library raises RuntimeError.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libsadmc_gb300.so")
+
+ISING, LJ, WCA, SW = 0, 1, 2, 3
+SAD, SAMC, WL, INV_T_WL, CANONICAL = 0, 1, 2, 3, 4
+
+ST_BIN_RANGE, ST_NAN_GAMMA, ST_DRIFT, ST_CELL_OVERFLOW = 1, 2, 4, 8
+ST_TIMEOUT, ST_DESCENT_FAILED, ST_BAD_INPUT = 16, 32, 64
+
+SCALARS = ["moves", "accepted", "acceptance_rate", "translation_scale", "method_kind",
+           "too_lo", "too_hi", "tL", "tF", "num_states", "highest_hist",
+           "latest_parameter", "gamma", "lowest_hist", "wl_highest_hist", "total_hist",
+           "wl_num_states", "min_energy", "t0", "max_S", "max_S_index", "drift", "status",
+           "energy"]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("system", ctypes.c_int32), ("method", ctypes.c_int32), ("n_walkers", ctypes.c_int32),
+        ("max_atoms", ctypes.c_int32), ("min_T", ctypes.c_double), ("t0", ctypes.c_double),
+        ("has_min_gamma", ctypes.c_int32), ("pad0", ctypes.c_int32),
+        ("min_gamma", ctypes.c_double), ("T", ctypes.c_double),
+        ("has_energy_bin", ctypes.c_int32), ("pad1", ctypes.c_int32),
+        ("energy_bin", ctypes.c_double),
+        ("has_min_allowed", ctypes.c_int32), ("has_max_allowed", ctypes.c_int32),
+        ("min_allowed", ctypes.c_double), ("max_allowed", ctypes.c_double),
+        ("e_lo", ctypes.c_double), ("e_hi", ctypes.c_double),
+        ("acceptance_rate_mode", ctypes.c_int32), ("pad2", ctypes.c_int32),
+        ("target_rate", ctypes.c_double), ("translation_scale", ctypes.c_double),
+        ("well_width", ctypes.c_double), ("seed", ctypes.c_uint64),
+        ("descent_limit", ctypes.c_uint64), ("lanes_per_walker", ctypes.c_int32),
+        ("resum_interval", ctypes.c_int32), ("drift_tol", ctypes.c_double),
+    ]
+
+
+class Geometry(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("pad", ctypes.c_int32), ("radius", ctypes.c_double),
+                ("box", ctypes.c_double * 3)]
+
+
+class Proposal(ctypes.Structure):
+    _fields_ = [("which", ctypes.c_int32), ("j", ctypes.c_int32), ("g", ctypes.c_double * 3),
+                ("scale", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it was not built for this machine)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run build.build() (needs nvcc) first")
+    L = ctypes.CDLL(LIB_PATH)
+    P, I32, U64, D = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint64, ctypes.c_double
+    sig = {
+        "sadmc_version": (I32, []), "sadmc_last_error": (ctypes.c_char_p, []),
+        "sadmc_create": (I32, [P, P, P]), "sadmc_destroy": (I32, [P]),
+        "sadmc_upload_state": (I32, [P, I32, I32, P]),
+        "sadmc_read_state": (I32, [P, I32, I32, P]),
+        "sadmc_initialize": (I32, [P]),
+        "sadmc_run": (I32, [P, U64]), "sadmc_run_async": (I32, [P, U64, P]),
+        "sadmc_synchronize": (I32, [P]),
+        "sadmc_energy": (I32, [P, P]), "sadmc_compute_energy": (I32, [P, P]),
+        "sadmc_plan_move_injected": (I32, [P, I32, P, P, P]),
+        "sadmc_confirm": (I32, [P, I32]),
+        "sadmc_nbins": (I32, [P, I32, P, P, P]),
+        "sadmc_read_bins": (I32, [P, I32, P, P, P, P, P, P, P]),
+        "sadmc_read_wl_hist": (I32, [P, I32, P, P, P]),
+        "sadmc_read_scalars": (I32, [P, I32, P]),
+        "sadmc_counters": (I32, [P, P, P]), "sadmc_status": (I32, [P, P]),
+        "sadmc_set_trace": (I32, [P, U64]), "sadmc_read_trace": (I32, [P, I32, P, P, P]),
+        "sadmc_lanes_per_walker": (I32, [P]), "sadmc_autotune": (I32, [P, U64, P, P]),
+        "sadmc_heat_capacity": (I32, [P, I32, P, P, I32, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype, f.argtypes = res, args
+    _lib = L
+    return L
+
+
+class SadmcError(RuntimeError):
+    pass
+
+
+def _check(rc):
+    if rc != 0:
+        raise SadmcError(f"sadmc error {rc}: {lib().sadmc_last_error().decode()}")
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def make_config(system, n_walkers, max_atoms, *, method=SAD, min_T=0.2, t0=1e4, min_gamma=None,
+                T=1.0, energy_bin=None, min_allowed=None, max_allowed=None, e_lo, e_hi,
+                target_rate=None, translation_scale=0.05, well_width=1.3, seed=0,
+                descent_limit=0, lanes_per_walker=0, resum_interval=0, drift_tol=0.0):
+    c = Config()
+    c.system, c.method, c.n_walkers, c.max_atoms = system, method, n_walkers, max_atoms
+    c.min_T, c.t0 = min_T, t0
+    c.has_min_gamma, c.min_gamma = int(min_gamma is not None), min_gamma or 0.0
+    c.T = T
+    c.has_energy_bin, c.energy_bin = int(energy_bin is not None), energy_bin or 0.0
+    c.has_min_allowed = int(min_allowed is not None)
+    c.min_allowed = 0.0 if min_allowed is None else min_allowed
+    c.has_max_allowed = int(max_allowed is not None)
+    c.max_allowed = 0.0 if max_allowed is None else max_allowed
+    c.e_lo, c.e_hi = e_lo, e_hi
+    c.acceptance_rate_mode = int(target_rate is not None)
+    c.target_rate = target_rate or 0.5
+    c.translation_scale, c.well_width, c.seed = translation_scale, well_width, seed
+    c.descent_limit, c.lanes_per_walker = descent_limit, lanes_per_walker
+    c.resum_interval, c.drift_tol = resum_interval, drift_tol
+    return c
+
+
+class Batch:
+    """A batch of GPU walkers (one sadmc_handle)."""
+
+    def __init__(self, cfg, geometry):
+        """geometry: list of (n, radius, (Lx, Ly, Lz)) per walker."""
+        self.cfg = cfg
+        W = cfg.n_walkers
+        if len(geometry) != W:
+            raise ValueError("one geometry entry per walker")
+        self._geom = (Geometry * W)()
+        for w, (n, radius, box) in enumerate(geometry):
+            self._geom[w].n, self._geom[w].radius = n, radius
+            for a in range(3):
+                self._geom[w].box[a] = box[a]
+        self.n = np.array([g[0] for g in geometry])
+        self.h = ctypes.c_void_p()
+        _check(lib().sadmc_create(ctypes.byref(cfg), self._geom, ctypes.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().sadmc_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def W(self):
+        return self.cfg.n_walkers
+
+    def upload(self, states, begin=0):
+        flat = np.ascontiguousarray(np.concatenate([np.ravel(s) for s in states]), np.float64)
+        _check(lib().sadmc_upload_state(self.h, begin, len(states), _p(flat)))
+
+    def state(self, w):
+        n = int(self.n[w])
+        size = n * n if self.cfg.system == ISING else 3 * n
+        out = np.zeros(size)
+        _check(lib().sadmc_read_state(self.h, w, 1, _p(out)))
+        return out if self.cfg.system == ISING else out.reshape(-1, 3)
+
+    def initialize(self):
+        _check(lib().sadmc_initialize(self.h))
+
+    def run(self, moves):
+        _check(lib().sadmc_run(self.h, int(moves)))
+
+    def run_async(self, moves, stream=None):
+        _check(lib().sadmc_run_async(self.h, int(moves), stream))
+
+    def synchronize(self):
+        _check(lib().sadmc_synchronize(self.h))
+
+    def energies(self):
+        out = np.zeros(self.W)
+        _check(lib().sadmc_energy(self.h, _p(out)))
+        return out
+
+    def compute_energies(self):
+        out = np.zeros(self.W)
+        _check(lib().sadmc_compute_energy(self.h, _p(out)))
+        return out
+
+    def plan_move(self, w, which, g=(0.0, 0.0, 0.0), scale=0.05, j=0):
+        p = Proposal()
+        p.which, p.j, p.scale = which, j, scale
+        for a in range(3):
+            p.g[a] = g[a]
+        e = ctypes.c_double(0.0)
+        ok = ctypes.c_int32(0)
+        _check(lib().sadmc_plan_move_injected(self.h, w, ctypes.byref(p), ctypes.byref(e),
+                                              ctypes.byref(ok)))
+        return e.value if ok.value else None
+
+    def confirm(self, w):
+        _check(lib().sadmc_confirm(self.h, w))
+
+    def bins(self, w):
+        n, mn, wd = ctypes.c_int64(0), ctypes.c_double(0), ctypes.c_double(0)
+        _check(lib().sadmc_nbins(self.h, w, ctypes.byref(n), ctypes.byref(mn), ctypes.byref(wd)))
+        n = n.value
+        lnw, sE, sE2 = np.zeros(n), np.zeros(n), np.zeros(n)
+        hist, tf, rt = (np.zeros(n, np.uint64) for _ in range(3))
+        vis = np.zeros(n, np.uint8)
+        _check(lib().sadmc_read_bins(self.h, w, _p(lnw), _p(hist), _p(tf), _p(sE), _p(sE2),
+                                     _p(rt), _p(vis)))
+        return dict(lnw=lnw, hist=hist, t_found=tf, sumE=sE, sumE2=sE2, round_trips=rt,
+                    visited=vis, min=mn.value, width=wd.value)
+
+    def wl_hist(self, w):
+        n, me = ctypes.c_int64(0), ctypes.c_double(0)
+        _check(lib().sadmc_read_wl_hist(self.h, w, None, ctypes.byref(n), ctypes.byref(me)))
+        out = np.zeros(max(n.value, 1), np.uint64)
+        _check(lib().sadmc_read_wl_hist(self.h, w, _p(out), ctypes.byref(n), ctypes.byref(me)))
+        return out[:n.value], me.value
+
+    def scalars(self, w):
+        o = np.zeros(len(SCALARS))
+        _check(lib().sadmc_read_scalars(self.h, w, _p(o)))
+        return dict(zip(SCALARS, o))
+
+    def counters(self):
+        m, a = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        _check(lib().sadmc_counters(self.h, ctypes.byref(m), ctypes.byref(a)))
+        return m.value, a.value
+
+    def status(self):
+        out = np.zeros(self.W, np.uint32)
+        _check(lib().sadmc_status(self.h, _p(out)))
+        return out
+
+    def set_trace(self, capacity):
+        _check(lib().sadmc_set_trace(self.h, int(capacity)))
+
+    def trace(self, w, capacity):
+        e1, e2 = np.zeros(capacity), np.zeros(capacity)
+        cnt = ctypes.c_uint64(0)
+        _check(lib().sadmc_read_trace(self.h, w, _p(e1), _p(e2), ctypes.byref(cnt)))
+        return e1[:cnt.value], e2[:cnt.value]
+
+    def lanes_per_walker(self):
+        return lib().sadmc_lanes_per_walker(self.h)
+
+    def autotune(self, moves=2048):
+        lpw, ms = ctypes.c_int32(0), ctypes.c_double(0)
+        _check(lib().sadmc_autotune(self.h, int(moves), ctypes.byref(lpw), ctypes.byref(ms)))
+        return lpw.value, ms.value
+
+
+def heat_capacity(T, E, S):
+    """C(T) on the GPU in FP64 (plotting/final_heat_capacity.py:79-88)."""
+    T = np.ascontiguousarray(T, np.float64)
+    E = np.ascontiguousarray(E, np.float64)
+    S = np.ascontiguousarray(S, np.float64)
+    C = np.zeros(len(T))
+    _check(lib().sadmc_heat_capacity(_p(T), len(T), _p(E), _p(S), len(E), _p(C)))
+    return C
+
+
+def cv_from_bins(bins, T):
+    """Heat capacity from a walker's visited bins (centres as E, lnw as S)."""
+    m = bins["hist"] > 0
+    E = bins["min"] + (np.nonzero(m)[0] + 0.5) * bins["width"]
+    return heat_capacity(T, E, bins["lnw"][m])

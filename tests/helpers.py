@@ -1,0 +1,46 @@
+"""Shared set-up for the GPU parity tests: the same seeded inputs for the CUDA batch and
+the FP64 oracle walkers."""
+import numpy as np
+
+BIN_KEYS = ["lnw", "hist", "t_found", "sumE", "sumE2", "round_trips", "visited"]
+EXACT_SCALARS = ["moves", "accepted", "acceptance_rate", "translation_scale", "method_kind",
+                 "too_lo", "too_hi", "tL", "tF", "num_states", "highest_hist",
+                 "latest_parameter", "gamma", "lowest_hist", "wl_highest_hist", "total_hist",
+                 "wl_num_states", "min_energy", "t0", "max_S", "max_S_index", "energy"]
+
+METHOD_KW = {
+    "sad": dict(method=0, min_T=0.2),
+    "samc": dict(method=1, t0=500.0),
+    "wl": dict(method=2),
+    "inv_t_wl": dict(method=3),
+    "canonical": dict(method=4, T=3.0),
+}
+
+
+def ising_spins(L, seed):
+    return np.where(np.random.default_rng(seed).random(L * L) < 0.5, -1.0, 1.0)
+
+
+def assert_bins_equal(gb, ob, keys=BIN_KEYS, label=""):
+    assert gb["min"] == ob["min"], label
+    assert gb["width"] == ob["width"], label
+    for k in keys:
+        a, b = np.asarray(gb[k]), np.asarray(ob[k])
+        assert a.shape == b.shape, (label, k, a.shape, b.shape)
+        if not np.array_equal(a, b):
+            bad = np.nonzero(a != b)[0][:5]
+            raise AssertionError(f"{label} bins[{k}] differ at {bad}: gpu {a[bad]} oracle {b[bad]}")
+
+
+def assert_scalars_equal(gs, os_, keys=EXACT_SCALARS, label=""):
+    for k in keys:
+        assert gs[k] == os_[k], f"{label} scalar {k}: gpu {gs[k]!r} oracle {os_[k]!r}"
+
+
+def lj_configs(oracle, n, radius, seeds):
+    out = []
+    for s in seeds:
+        pos, ok = oracle.init_lj(n, radius, s)
+        assert ok
+        out.append(pos)
+    return out

@@ -1,0 +1,41 @@
+"""CPU checks of the C ABI: the library builds for sm_103a, loads, and exports every
+function that include/sadmc_gpu.h declares (no compute call is made without a GPU)."""
+import ctypes
+import os
+import re
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(REPO, "include", "sadmc_gpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int32_t|const char\*)\s+(sadmc_\w+)\(", text, re.M)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for must in ["sadmc_create", "sadmc_destroy", "sadmc_upload_state", "sadmc_initialize",
+                 "sadmc_run", "sadmc_energy", "sadmc_compute_energy", "sadmc_plan_move_injected",
+                 "sadmc_confirm", "sadmc_read_bins", "sadmc_counters", "sadmc_status"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    import build as B
+    lib_path = B.build()
+    lib = ctypes.CDLL(lib_path)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.sadmc_version.restype = ctypes.c_int32
+    assert lib.sadmc_version() >= 1
+
+
+def test_no_oracle_in_product():
+    """The product sources never include, link or load the oracle."""
+    pkg = os.path.join(REPO, "sad-monte-carlo_gb300")
+    for root, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".cu", ".cuh", ".cpp", ".h", ".py")):
+                text = open(os.path.join(root, f)).read()
+                for pat in (r"import\s+oracle", r"from\s+oracle", r"liboracle", r"#include\s+\S*oracle"):
+                    assert not re.search(pat, text), (f, pat)

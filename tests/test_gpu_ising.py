@@ -1,0 +1,59 @@
+"""GPU Ising kernel against the FP64 oracle: integer energies, so the whole flat-histogram
+chain (spins, bins, SAD/WL/SAMC state) must be bit-identical on the same Philox stream."""
+import numpy as np
+import pytest
+
+from helpers import METHOD_KW, assert_bins_equal, assert_scalars_equal, ising_spins
+
+pytestmark = pytest.mark.gpu
+
+
+def run_pair(gpu, oracle, L, W, moves, method, seed=17, lpw=0, chunks=1):
+    kw = METHOD_KW[method]
+    N = L * L
+    cfg = gpu.make_config(gpu.ISING, W, L, e_lo=-2.0 * N - 4, e_hi=2.0 * N + 4, seed=seed,
+                          lanes_per_walker=lpw, **kw)
+    b = gpu.Batch(cfg, [(L, 0.0, (0, 0, 0))] * W)
+    spins = [ising_spins(L, 1000 + w) for w in range(W)]
+    b.upload(spins)
+    b.initialize()
+    for _ in range(chunks):
+        b.run(moves // chunks)
+    walkers = []
+    okw = {k: v for k, v in kw.items()}
+    for w in range(W):
+        ow = oracle.Walker(oracle.make_config(oracle.ISING, L, seed=seed, walker=w, **okw), spins[w])
+        ow.run(moves)
+        walkers.append(ow)
+    return b, walkers
+
+
+@pytest.mark.parametrize("method", ["sad", "wl", "inv_t_wl", "samc", "canonical"])
+def test_ising_batch_bit_exact(gpu, oracle, method):
+    b, ws = run_pair(gpu, oracle, L=8, W=40, moves=30000, method=method, chunks=3)
+    for w in range(b.W):
+        label = f"{method} walker {w}"
+        assert_bins_equal(b.bins(w), ws[w].bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ws[w].scalars(), label=label)
+        np.testing.assert_array_equal(b.state(w), ws[w].state())
+        if method in ("wl", "inv_t_wl"):
+            gh, gme = b.wl_hist(w)
+            oh, ome = ws[w].wl_hist()
+            if ws[w].scalars()["method_kind"] == 2:
+                np.testing.assert_array_equal(gh, oh)
+                assert gme == ome
+    assert not b.status().any()
+
+
+def test_ising_single_walker_32x32(gpu, oracle):
+    """The one-walker 32x32 SAD chain (one warp per walker)."""
+    b, ws = run_pair(gpu, oracle, L=32, W=1, moves=200000, method="sad", lpw=32)
+    assert_bins_equal(b.bins(0), ws[0].bins(), label="L32")
+    assert_scalars_equal(b.scalars(0), ws[0].scalars(), label="L32")
+    np.testing.assert_array_equal(b.state(0), ws[0].state())
+
+
+def test_ising_energy_matches_compute_energy(gpu, oracle):
+    b, ws = run_pair(gpu, oracle, L=16, W=8, moves=5000, method="sad")
+    np.testing.assert_array_equal(b.energies(), b.compute_energies())
+    np.testing.assert_array_equal(b.energies(), [w.compute_energy() for w in ws])

@@ -1,0 +1,135 @@
+"""CPU tests of the FP64 oracle: the reference's own invariant tests re-run on the
+restatement, the published Philox known answers, and the golden fixtures."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_philox_known_answers(oracle):
+    # Random123 known-answer vectors for philox4x32-10
+    assert [int(x) for x in oracle.philox([0, 0, 0, 0], [0, 0])] == \
+        [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert [int(x) for x in oracle.philox([0xffffffff] * 4, [0xffffffff] * 2)] == \
+        [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert [int(x) for x in oracle.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344],
+                                          [0xa4093822, 0x299f31d0])] == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_normals_are_standard(oracle):
+    rng = np.random.default_rng(0)
+    a = rng.integers(0, 2**32, 200000, dtype=np.uint32)
+    b = rng.integers(0, 2**32, 200000, dtype=np.uint32)
+    z0, z1 = oracle.normal_pairs(a, b)
+    z = np.concatenate([z0, z1]).astype(np.float64)
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01
+    assert abs(((z - z.mean()) ** 4).mean() / z.var() ** 2 - 3.0) < 0.05
+    assert abs(np.corrcoef(z0, z1)[0, 1]) < 0.01
+
+
+@pytest.mark.parametrize("L", [2, 3, 10, 15, 137, 150])
+def test_ising_energy_works(oracle, L):
+    """ising.rs:125-147: energy() == compute_energy() after each of 1e4 flips."""
+    assert oracle.selftest_ising(L, 10000) == 0
+
+
+@pytest.mark.parametrize("n", [3, 50, 100])
+def test_lj_energy_is_right(oracle, n):
+    """lj.rs:380-427: incremental energy passes verify_energy after each move."""
+    radius = 5 * 2 * n ** (1 / 3)
+    pos, ok = oracle.init_lj(n, radius, 1)
+    assert ok
+    w = oracle.Walker(oracle.make_config(oracle.LJ, n, radius=radius), pos)
+    assert w.energy() == w.compute_energy()
+    assert oracle.selftest_moves(w, 1000, 1.0) == 0
+
+
+@pytest.mark.parametrize("n,ff", [(3, 0.1), (50, 0.3), (100, 0.3), (200, 0.3)])
+def test_square_well_energy_is_right(oracle, n, ff):
+    """optsquare.rs:585-618: E == compute_energy exactly after every move."""
+    pos, box = oracle.init_sw_fcc(n, ff, 1.3, 0)
+    w = oracle.Walker(oracle.make_config(oracle.SW, n, box=box), pos)
+    assert w.verify_energy()
+    assert oracle.selftest_moves(w, 1000, 1.0) == 0
+
+
+@pytest.mark.parametrize("n", [100, 200])
+def test_square_well_minimum_images(oracle, n):
+    """optsquare.rs:438-521: closest-distance variants agree; candidates are minimum images."""
+    pos, box = oracle.init_sw_fcc(n, 0.3, 1.3, 0)
+    w = oracle.Walker(oracle.make_config(oracle.SW, n, box=box), pos)
+    assert oracle.selftest_cell(w) == 0
+    oracle.selftest_moves(w, 100000, 1.0)
+    assert oracle.selftest_cell(w) == 0
+
+
+@pytest.mark.parametrize("n,rho", [(50, 0.3), (50, 1.0), (100, 0.3)])
+def test_wca_energy_is_right(oracle, n, rho):
+    """wca.rs:647-694 (including the dense rho = 1.0 case)."""
+    L = (n / rho) ** (1 / 3)
+    pos = np.random.default_rng(n).uniform(0, L, (n, 3))
+    w = oracle.Walker(oracle.make_config(oracle.WCA, n, box=(L, L, L)), pos)
+    assert oracle.selftest_moves(w, 1000, 1.0) == 0
+
+
+def test_max_balls_within(oracle):
+    # optsquare.rs:290-322 counts lattice points of its own construction
+    assert oracle.max_balls_within(1.3) == 6
+
+
+def test_golden_fixtures(oracle):
+    """Values pinned in tests/golden (see make_golden.py)."""
+    with open(os.path.join(GOLDEN, "golden.json")) as fh:
+        g = json.load(fh)
+    for (r2, v) in g["lj_potential"]:
+        assert oracle.lib().orc_lj_potential(r2) == v
+    for (r2, v) in g["wca_potential"]:
+        assert oracle.lib().orc_wca_potential(r2) == v
+    for rec in g["draws"]:
+        idx, gg, u = oracle.draws(rec["system"], rec["n"], rec["seed"], rec["walker"], rec["t"])
+        assert [int(x) for x in idx] == rec["idx"]
+        assert [float(x) for x in gg] == rec["g"]
+        assert u == rec["u"]
+    T = np.array(g["cv"]["T"])
+    C = oracle.heat_capacity(T, np.array(g["cv"]["E"]), np.array(g["cv"]["S"]))
+    np.testing.assert_allclose(C, np.array(g["cv"]["C"]), rtol=1e-12)
+
+
+def test_ising_sad_converges_to_exact_dos(oracle):
+    """Known answer from mathematics: SAD's ln w of a 4x4 Ising lattice approaches the
+    exact ln g(E) (2^16-state enumeration) up to a constant."""
+    with open(os.path.join(GOLDEN, "golden.json")) as fh:
+        g = json.load(fh)["ising4_exact"]
+    E = np.array(g["E"])
+    lng = np.array(g["lng"])
+    spins = np.where(np.random.default_rng(3).random(16) < 0.5, -1.0, 1.0)
+    w = oracle.Walker(oracle.make_config(oracle.ISING, 4, method=oracle.M_WL, seed=5), spins)
+    w.run(3_000_000)
+    b = w.bins()
+    centers = b["min"] + (np.arange(len(b["lnw"])) + 0.5) * b["width"]
+    got = {}
+    for c, l, h in zip(centers, b["lnw"], b["hist"]):
+        if h > 0:
+            got[int(round(c))] = l
+    common = [e for e in E if int(e) in got]
+    assert len(common) == len(E)
+    d = np.array([got[int(e)] for e in common]) - lng
+    assert np.max(np.abs(d - d.mean())) < 0.15
+
+
+def test_heat_capacity_matches_numpy(oracle):
+    rng = np.random.default_rng(1)
+    E = np.sort(rng.uniform(-100, 0, 300))
+    S = rng.uniform(0, 50, 300)
+    T = np.linspace(0.05, 0.5, 40)
+    C = oracle.heat_capacity(T, E, S)
+    for t, c in zip(T, C):  # plotting/final_heat_capacity.py:79-88 stated in numpy
+        b = S - E / t
+        P = np.exp(b - b.max())
+        P = P / P.sum()
+        U = (E * P).sum()
+        assert c == pytest.approx(((E - U) ** 2 * P).sum() / t ** 2, rel=1e-10)
