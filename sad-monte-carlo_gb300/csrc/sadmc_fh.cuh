@@ -99,6 +99,7 @@ struct Fh {
     if (wr) { lnw[cur] = k_lnw; hist[cur] = k_hist; tf[cur] = k_tf; sE[cur] = k_sE; sE2[cur] = k_sE2; }
   }
   __device__ void load_cur(int g) {
+    g = g < 0 ? 0 : (g >= nbins ? nbins - 1 : g);
     cur = g;
     k_lnw = lnw[g]; k_hist = hist[g]; k_tf = tf[g]; k_sE = sE[g]; k_sE2 = sE2[g];
   }
@@ -228,6 +229,10 @@ struct Fh {
     if (!prepare(e2)) { c.status |= ST_BIN_RANGE; return false; }
     if (grew_front) reindex_after_growth();
     i2 = gidx(e2);
+    if (i2 < c.b_lo || i2 > c.b_hi) {  // only reachable through rounding at the range edge
+      c.status |= ST_BIN_RANGE;
+      return false;
+    }
     double lnw2_raw = ld_lnw(i2);
     hist2 = ld_hist(i2);
     bool rejected;
@@ -397,10 +402,11 @@ struct Fh {
         wl_zero_range(c.wl_lo, c.wl_hi);
         c.min_energy = c.cur_min;
       } else {
-        while (c.min_energy > c.cur_min) {
+        for (int guard = 0; c.min_energy > c.cur_min; ++guard) {
+          if (guard > nbins || c.wl_lo <= 0) { c.status |= ST_BIN_RANGE; break; }
           c.min_energy -= width;
           c.wl_lo -= 1;
-          if (wr && c.wl_lo >= 0) wlh[c.wl_lo] = 0;
+          if (wr) wlh[c.wl_lo] = 0;
         }
         while (len_w < len_b) {
           c.wl_hi += 1;
