@@ -1,0 +1,327 @@
+"""Benchmark of the flat-histogram hot path on one GB300.
+
+Workload (C2): LJ cluster N=31 in a sphere of radius 2.5 sigma, plain SAD (min_T 0.2 ...
+see WORKLOAD) over [-134, 0] with 1000 FP64 bins, 4096 independent walkers, Gaussian
+single-atom moves of initial rms 0.1 adapted toward 50% acceptance.  One step = 24,414
+moves of every walker = 1.0e8 moves (the C2 budget).
+
+  value   moves/s with the batch resident in HBM (CUDA events on the launching stream)
+  e2e     moves/s through the C ABI from pinned host buffers: upload configurations,
+          initialize (FP64 energies, descent below E=0, bins), run, read back all ln w
+          and histogram planes -- every step
+  roofline  FP32 pair work of the move kernel (30 (N-1) FLOP per move) against the FP32
+          issue peak; HBM traffic per launch from the committed ncu summary
+
+`--impl reference` times the FP64 CPU oracle (the C++ restatement of the reference's
+Rust path, which cannot be built here) on all host cores on a bounded sample.
+"""
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "sad-monte-carlo_gb300"))
+
+N_ATOMS, RADIUS, WALKERS = 31, 2.5, 4096
+MOVES_PER_STEP = 24414                       # per walker: 4096 * 24414 = 1.0e8 moves
+E_LO, E_HI, NBINS = -134.0, 0.0, 1000
+WIDTH = (E_HI - E_LO) / NBINS                # 0.134
+FLOP_PER_MOVE = 30 * (N_ATOMS - 1)           # 2 (N-1) pair terms x 15 FLOP
+WORKLOAD = (f"C2 LJ{N_ATOMS} cluster (R={RADIUS}), SAD min_T=0.2, {NBINS} bins of "
+            f"{WIDTH:g} over [{E_LO:g},{E_HI:g}], max_allowed_energy 0, {WALKERS} walkers, "
+            f"{MOVES_PER_STEP} moves/walker per step, step 0.1 adapted to 50% acceptance")
+
+
+def lj_configs(n_walkers, seed):
+    """Uniform in the sphere with random sequential rejection of pairs closer than 0.8."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((n_walkers, N_ATOMS, 3))
+    for w in range(n_walkers):
+        pts = []
+        while len(pts) < N_ATOMS:
+            p = rng.uniform(-RADIUS, RADIUS, 3)
+            if p @ p >= RADIUS * RADIUS:
+                continue
+            if pts and np.min(np.sum((np.array(pts) - p) ** 2, axis=1)) < 0.64:
+                continue
+            pts.append(p)
+        out[w] = pts
+    return out
+
+
+def make_batch(G, n_walkers, seed=1, lpw=0):
+    cfg = G.make_config(G.LJ, n_walkers, N_ATOMS, method=G.SAD, min_T=0.2, energy_bin=WIDTH,
+                        max_allowed=0.0, e_lo=E_LO - 2 * WIDTH, e_hi=E_HI + 2 * WIDTH,
+                        target_rate=0.5, translation_scale=0.1, seed=seed,
+                        lanes_per_walker=lpw)
+    return G.Batch(cfg, [(N_ATOMS, RADIUS, (0, 0, 0))] * n_walkers)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out" if os.path.isdir(os.path.join(REPO, "gpurun_out")) else ".",
+                                 ".bench_clocks.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", "0", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def profile_traffic():
+    """DRAM bytes per move-kernel launch from the committed ncu summary, if present."""
+    path = os.path.join(REPO, "profiles", "lj_move_kernel_lj31_4096w.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_sample(threads, walkers=128, moves=100000, seed=7):
+    """The FP64 oracle on host threads, on `walkers` C2 walkers x `moves` moves."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    O.build()
+    confs = lj_configs(walkers, seed)
+    cfgs = [O.make_config(O.LJ, N_ATOMS, radius=RADIUS, method=O.M_SAD, min_T=0.2,
+                          energy_bin=WIDTH, max_allowed=0.0, target_rate=0.5,
+                          translation_scale=0.1, seed=seed, walker=w) for w in range(walkers)]
+    sec, tm, ta = O.bench(cfgs, [c.reshape(-1) for c in confs], moves, threads)
+    return tm / sec, ta / sec, sec, tm
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    walkers, moves = 64, 20000
+    vals = []
+    for k in range(args.warmup + args.steps):
+        v, _, sec, tm = cpu_sample(threads, walkers=walkers, moves=moves, seed=11 + k)
+        if k >= args.warmup:
+            vals.append((v, sec))
+    value = statistics.mean(v for v, _ in vals)
+    line = {
+        "impl": "reference", "metric": "moves/s", "value": value, "unit": "moves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.mean(s for _, s in vals),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded uniform-in-sphere LJ31 configurations)",
+        "config": {"workload": WORKLOAD, "sample": f"{walkers} walkers x {moves} moves per step"},
+        "cpu_baseline": {"value": value, "unit": "moves/s", "cores": threads, "kind": "port",
+                         "sample": f"{walkers} C2 walkers x {moves} moves per step, FP64 C++ "
+                                   "restatement of the reference (Rust toolchain absent)"},
+        "e2e": {"value": value, "unit": "moves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import ctypes
+
+    import torch
+    import sadmc_gb300 as G
+    import build as B
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    B.build()
+    G.lib()
+
+    # ---- device-resident throughput -------------------------------------------------
+    confs = lj_configs(WALKERS, 1000 + rank)
+    b = make_batch(G, WALKERS, seed=1 + rank, lpw=args.lpw)
+    b.upload(list(confs))
+    b.initialize()
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    chunk = 8192
+    launches_per_step = math.ceil(MOVES_PER_STEP / chunk)
+    for _ in range(args.warmup):
+        b.run_async(MOVES_PER_STEP, sp)
+    stream.synchronize()
+    clocks = Clocks()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    m0, a0 = b.counters()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.run_async(MOVES_PER_STEP, sp)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    m1, a1 = b.counters()
+    moves = m1 - m0
+    if moves != WALKERS * MOVES_PER_STEP * args.steps:
+        raise RuntimeError(f"move count {moves} != expected")
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(t.item())
+    value = moves * world / (ms * 1e-3)
+    acc_rate = (a1 - a0) / moves
+    status = b.status()
+    launch_ms = ms / (args.steps * launches_per_step)
+    flop_per_launch = FLOP_PER_MOVE * WALKERS * (MOVES_PER_STEP / launches_per_step)
+    achieved_tflops = flop_per_launch / (launch_ms * 1e-3) / 1e12
+    pk = peaks()
+    sm_mhz = clk.get("sm_max_mhz") or pk.get("sm_max_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # FFMA issue peak, TFLOP/s
+    traffic = profile_traffic()
+    b.close()
+
+    # ---- end to end through the C ABI with host buffers ------------------------------
+    e2e = None
+    if not args.no_e2e:
+        n_e2e = WALKERS
+        host_conf = torch.from_numpy(lj_configs(n_e2e, 5000 + rank).reshape(-1)).pin_memory()
+        be = make_batch(G, n_e2e, seed=7 + rank, lpw=args.lpw)
+        nb = be.plane_bins()
+        lnw_h = torch.empty(n_e2e * nb, dtype=torch.float64).pin_memory()
+        hist_h = torch.empty(n_e2e * nb, dtype=torch.int64).pin_memory()
+        lnw_np, hist_np = lnw_h.numpy(), hist_h.numpy().view(np.uint64)
+        conf_np = host_conf.numpy()
+
+        def e2e_step():
+            be.upload(conf_np)  # all walkers, packed, from pinned memory
+            be.initialize()
+            be.run(MOVES_PER_STEP)
+            be.read_planes(lnw_np, hist_np)
+        for _ in range(max(1, args.warmup // 2)):
+            e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_steps = max(1, args.steps // 2)
+        for _ in range(e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        e2e = {"value": n_e2e * MOVES_PER_STEP * e_steps * world / sec, "unit": "moves/s",
+               "h2d_bytes_per_step": int(conf_np.nbytes),
+               "d2h_bytes_per_step": int(lnw_np.nbytes + hist_np.nbytes),
+               "ms_per_step": 1e3 * sec / e_steps,
+               "includes": "upload, initialize (FP64 energies, descent, bins), run, read planes"}
+        be.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, va, sec, tm = cpu_sample(threads, walkers=128, moves=100000)
+        cpu = {"value": v, "unit": "moves/s", "cores": threads, "kind": "port",
+               "sample": f"128 C2 walkers x 100000 moves ({tm} moves, {sec:.2f} s wall), FP64 "
+                         "C++ restatement of the reference (Rust toolchain absent)"}
+
+    if rank == 0:
+        line = {
+            "metric": "moves/s", "value": value, "unit": "moves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 pair energies, f64 ln g / gamma / energy",
+            "data": "synthetic (seeded uniform-in-sphere LJ31 configurations)",
+            "config": {"workload": WORKLOAD, "walkers": WALKERS, "moves_per_step": WALKERS * MOVES_PER_STEP,
+                       "lanes_per_walker": args.lpw or "default",
+                       "l2": "bin planes 4096 x 1004 x 64 B = 263 MB > 129 MB L2 (inputs larger than L2)"},
+            "accepted_moves_per_s": value * acc_rate,
+            "acceptance": acc_rate,
+            "walkers_with_status": int((status != 0).sum()),
+            "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": achieved_tflops / fp32_peak,
+                         "traffic": traffic,
+                         "note": "30(N-1) FLOP/move algorithmic; peak = 152 SM x 128 FFMA x 2 x "
+                                 "max SM clock (FP32 issue, not in MEASURED_PEAKS.json); the "
+                                 "kernel is FP64/latency bound, see DESIGN.md"},
+            "launch_ms": launch_ms,
+            "clocks": clk,
+            "gpu_launches": args.steps * launches_per_step,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--lpw", type=int, default=0, help="lanes per walker (0: library default)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -145,6 +145,13 @@ int32_t sadmc_nbins(sadmc_handle* h, int32_t walker, int64_t* nbins, double* bin
 int32_t sadmc_read_bins(sadmc_handle* h, int32_t walker, double* lnw, uint64_t* histogram,
                         uint64_t* t_found, double* energy_total, double* energy_squared_total,
                         uint64_t* round_trips, uint8_t* visited_since_maxentropy);
+/* Whole-batch readback of the ln w and histogram planes (the result of a run):
+ * lnw and histogram receive n_walkers * plane_bins values, walker-major; range receives
+ * per walker (first, last) plane index of the allocated bins and bins_min its bins.min.
+ * plane_bins is reported by sadmc_plane_bins. */
+int32_t sadmc_plane_bins(sadmc_handle* h, int64_t* plane_bins);
+int32_t sadmc_read_planes(sadmc_handle* h, double* lnw, uint64_t* histogram, int32_t* range,
+                          double* bins_min);
 /* Wang-Landau per-stage histogram (Method::WL::hist), *n entries from *min_energy. */
 int32_t sadmc_read_wl_hist(sadmc_handle* h, int32_t walker, uint64_t* hist, int64_t* n,
                            double* min_energy);
@@ -169,6 +176,13 @@ int32_t sadmc_read_trace(sadmc_handle* h, int32_t walker, double* e1, double* e2
  * batch (`moves` moves each), keeps the fastest and restores the snapshot. */
 int32_t sadmc_lanes_per_walker(sadmc_handle* h);
 int32_t sadmc_autotune(sadmc_handle* h, uint64_t moves, int32_t* best_lpw, double* best_ms);
+
+/* The counter-based draws the kernels consume for moves t0 .. t0+count-1 of one walker
+ * (Philox4x32-10 keyed by (walker, seed); stream_pair 0 moves, 1 descent): idx2 gets
+ * (atom or i, j) pairs, g3 the three normals, u the Metropolis uniform.  Host arrays.
+ * A diagnostic with no counterpart in the reference, whose xoroshiro stream it replaces. */
+int32_t sadmc_draws(int32_t system, uint32_t n, uint64_t seed, uint32_t walker, uint64_t t0,
+                    int32_t count, uint32_t stream_pair, uint32_t* idx2, float* g3, double* u);
 
 /* Heat capacity C(T) = (<E^2> - <E>^2) / T^2 with P ~ exp(S - E/T - max), FP64 on the
  * device (plotting/final_heat_capacity.py:79-88).  Host arrays. */

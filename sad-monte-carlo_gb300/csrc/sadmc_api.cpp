@@ -65,6 +65,24 @@ struct sadmc_handle {
   void* plane_mem = nullptr;
   float* d_pos = nullptr;      // LJ: [W][6][np]
   int8_t* d_spins = nullptr;   // Ising: [W][L*L]
+  // periodic cell systems (square well, WCA)
+  double* d_pos64 = nullptr;   // [W][3][np]
+  float* d_pos32 = nullptr;    // [W][np] float4
+  double* d_box = nullptr;     // [W][3]
+  int* d_ncell = nullptr;      // [W][3]
+  int* d_cell_of = nullptr;    // [W][np]
+  int* d_cnt = nullptr;        // [W][cell_cap]
+  int* d_atoms = nullptr;      // [W][cell_cap][bucket]
+  int* d_build_status = nullptr;
+  int cell_cap = 0, bucket = 16;
+  double r_cut = 0.0;
+  CellSys cell_sys() const {
+    CellSys c{};
+    c.pos = d_pos64; c.pos32 = d_pos32; c.np = np; c.box = d_box; c.ncell = d_ncell;
+    c.cell_of = d_cell_of; c.cell_count = d_cnt; c.cell_atoms = d_atoms; c.cell_cap = cell_cap;
+    c.bucket = bucket; c.r_cut = r_cut; c.kind = cfg.system; c.build_status = d_build_status;
+    return c;
+  }
   double* d_tmp = nullptr;     // [W] + 2 scratch doubles
   TraceRec* d_trace = nullptr;
   uint64_t trace_cap = 0, trace_t0 = 0;
@@ -107,6 +125,8 @@ struct sadmc_handle {
     switch (cfg.system) {
       case SADMC_LJ: return launch_lj_move(m, LjSys{d_pos, np, 0.0 + radius2()}, lpw, stream);
       case SADMC_ISING: return launch_ising_move(m, IsingSys{d_spins, L}, lpw, stream);
+      case SADMC_SW:
+      case SADMC_WCA: return launch_cell_move(m, cell_sys(), lpw, stream);
       default: return cudaErrorNotSupported;
     }
   }
@@ -125,6 +145,8 @@ struct sadmc_handle {
     switch (cfg.system) {
       case SADMC_LJ: return launch_lj_energy(d_cores, LjSys{d_pos, np, radius2()}, W, out, stream);
       case SADMC_ISING: return launch_ising_energy(IsingSys{d_spins, L}, W, out, stream);
+      case SADMC_SW:
+      case SADMC_WCA: return launch_cell_energy(d_cores, cell_sys(), W, out, stream);
       default: return cudaErrorNotSupported;
     }
   }
@@ -157,8 +179,6 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
   if (c.system < SADMC_ISING || c.system > SADMC_SW) return fail(SADMC_ERR_INVALID, "unknown system");
   if (c.method < SADMC_SAD || c.method > SADMC_CANONICAL) return fail(SADMC_ERR_INVALID, "unknown method");
   if (!(c.e_hi > c.e_lo)) return fail(SADMC_ERR_INVALID, "e_hi must exceed e_lo");
-  if (c.system != SADMC_ISING && c.system != SADMC_LJ)
-    return fail(SADMC_ERR_INVALID, "system not available in this build");
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
     return fail(SADMC_ERR_CUDA, "no CUDA device");
@@ -168,7 +188,7 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
   h->geom.assign(geom, geom + c.n_walkers);
   // bin width: energy_bin, else System::delta_energy() (Ising 4, square well 1), else 1
   // (energy.rs:831-833)
-  h->width = c.has_energy_bin ? c.energy_bin : (c.system == SADMC_ISING ? 4.0 : (c.system == SADMC_SW ? 1.0 : 1.0));
+  h->width = c.has_energy_bin ? c.energy_bin : (c.system == SADMC_ISING ? 4.0 : 1.0);
   if (!(h->width > 0)) { delete h; return fail(SADMC_ERR_INVALID, "energy_bin must be positive"); }
   double nbd = std::ceil((c.e_hi - c.e_lo) / h->width) + 4.0;
   if (nbd > (double)(1 << 24)) { delete h; return fail(SADMC_ERR_INVALID, "too many bins"); }
@@ -180,6 +200,29 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
       if (geom[w].n != h->L) { delete h; return fail(SADMC_ERR_INVALID, "Ising walkers must share L"); }
     h->lpw = c.lanes_per_walker ? c.lanes_per_walker : (h->W == 1 ? 32 : 1);
     if (h->lpw != 1 && h->lpw != 32) { delete h; return fail(SADMC_ERR_INVALID, "Ising lanes_per_walker must be 1 or 32"); }
+  } else if (c.system == SADMC_SW || c.system == SADMC_WCA) {
+    h->r_cut = c.system == SADMC_SW ? c.well_width : std::pow(2.0, 1.0 / 6.0);
+    if (!(h->r_cut > 0)) { delete h; return fail(SADMC_ERR_INVALID, "well_width must be positive"); }
+    int mx = 0, cap = 0;
+    for (int w = 0; w < h->W; ++w) {
+      if (geom[w].n < 2 || geom[w].n > 4096) { delete h; return fail(SADMC_ERR_INVALID, "2..4096 atoms per periodic walker"); }
+      mx = std::max(mx, (int)geom[w].n);
+      int cells = 1;
+      for (int a = 0; a < 3; ++a) {
+        const int nc = (int)std::floor(geom[w].box[a] / h->r_cut);  // optcell.rs:64-66
+        if (nc < 3) {
+          delete h;
+          return fail(SADMC_ERR_INVALID, "walker " + std::to_string(w) +
+                      ": fewer than 3 subcells per axis (the reference double counts there)");
+        }
+        cells *= nc;
+      }
+      cap = std::max(cap, cells);
+    }
+    h->np = (mx + 31) / 32 * 32;
+    h->cell_cap = cap;
+    h->lpw = c.lanes_per_walker ? c.lanes_per_walker : 8;
+    if (h->lpw != 32 && h->lpw != 16 && h->lpw != 8 && h->lpw != 4) { delete h; return fail(SADMC_ERR_INVALID, "unsupported lanes_per_walker"); }
   } else {
     int mx = 0;
     for (int w = 0; w < h->W; ++w) {
@@ -208,7 +251,21 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
     h->planes.visit_stamp = (uint64_t*)(b + 6 * plane * 8);
     h->planes.wl_hist = (uint64_t*)(b + 7 * plane * 8);
     if (c.system == SADMC_ISING) ok = dalloc(&h->d_spins, (size_t)h->W * h->L * h->L) == cudaSuccess;
-    else ok = dalloc(&h->d_pos, (size_t)h->W * 6 * h->np) == cudaSuccess;
+    else if (c.system == SADMC_LJ) ok = dalloc(&h->d_pos, (size_t)h->W * 6 * h->np) == cudaSuccess;
+    else {
+      const size_t W = h->W, np = h->np, cap = h->cell_cap;
+      ok = dalloc(&h->d_pos64, W * 3 * np) == cudaSuccess && dalloc(&h->d_pos32, W * 4 * np) == cudaSuccess &&
+           dalloc(&h->d_box, W * 3) == cudaSuccess && dalloc(&h->d_ncell, W * 3) == cudaSuccess &&
+           dalloc(&h->d_cell_of, W * np) == cudaSuccess && dalloc(&h->d_cnt, W * cap) == cudaSuccess &&
+           dalloc(&h->d_atoms, W * cap * h->bucket) == cudaSuccess &&
+           dalloc(&h->d_build_status, W) == cudaSuccess;
+      if (ok) {
+        std::vector<double> box(W * 3);
+        for (size_t w = 0; w < W; ++w)
+          for (int a = 0; a < 3; ++a) box[3 * w + a] = geom[w].box[a];
+        ok = cudaMemcpy(h->d_box, box.data(), box.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+      }
+    }
   }
   if (!ok) {
     sadmc_destroy(h);
@@ -228,6 +285,8 @@ int32_t sadmc_destroy(sadmc_handle* h) {
   cudaFree(h->d_pos);
   cudaFree(h->d_spins);
   cudaFree(h->d_trace);
+  cudaFree(h->d_pos64); cudaFree(h->d_pos32); cudaFree(h->d_box); cudaFree(h->d_ncell);
+  cudaFree(h->d_cell_of); cudaFree(h->d_cnt); cudaFree(h->d_atoms); cudaFree(h->d_build_status);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return SADMC_OK;
@@ -241,6 +300,29 @@ int32_t sadmc_upload_state(sadmc_handle* h, int32_t begin, int32_t count, const 
     std::vector<int8_t> s(n * count);
     for (size_t k = 0; k < s.size(); ++k) s[k] = (int8_t)(state[k] > 0 ? 1 : -1);
     CUDA_TRY(cudaMemcpyAsync(h->d_spins + (size_t)begin * n, s.data(), s.size(), cudaMemcpyHostToDevice, h->stream));
+  } else if (h->cfg.system == SADMC_SW || h->cfg.system == SADMC_WCA) {
+    const int np = h->np;
+    std::vector<double> p((size_t)count * 3 * np, 0.0);
+    size_t off = 0;
+    for (int w = 0; w < count; ++w) {
+      const int n = h->geom[begin + w].n;
+      double* q = p.data() + (size_t)w * 3 * np;
+      for (int j = 0; j < n; ++j)
+        for (int a = 0; a < 3; ++a) q[a * np + j] = state[off + 3 * j + a];
+      off += 3 * (size_t)n;
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->d_pos64 + (size_t)begin * 3 * np, p.data(), p.size() * sizeof(double),
+                             cudaMemcpyHostToDevice, h->stream));
+    h->h_cores.clear();
+    int32_t r = h->prep_cores();
+    if (r) return r;
+    CUDA_TRY(launch_cell_build(h->d_cores, h->cell_sys(), h->W, h->stream));
+    std::vector<int> st(h->W);
+    CUDA_TRY(cudaMemcpyAsync(st.data(), h->d_build_status, sizeof(int) * h->W, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (int w = 0; w < h->W; ++w)
+      if (st[w]) return fail(SADMC_ERR_INVALID, "walker " + std::to_string(w) +
+                             (st[w] == ST_CELL_OVERFLOW ? ": subcell bucket overflow" : ": position outside [0, box)"));
   } else {
     const int np = h->np;
     std::vector<float> p((size_t)count * 6 * np, 0.0f);
@@ -276,6 +358,20 @@ int32_t sadmc_read_state(sadmc_handle* h, int32_t begin, int32_t count, double* 
     CUDA_TRY(cudaMemcpyAsync(s.data(), h->d_spins + (size_t)begin * n, s.size(), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     for (size_t k = 0; k < s.size(); ++k) state[k] = s[k];
+  } else if (h->cfg.system == SADMC_SW || h->cfg.system == SADMC_WCA) {
+    const int np = h->np;
+    std::vector<double> p((size_t)count * 3 * np);
+    CUDA_TRY(cudaMemcpyAsync(p.data(), h->d_pos64 + (size_t)begin * 3 * np, p.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    size_t off = 0;
+    for (int w = 0; w < count; ++w) {
+      const int n = h->geom[begin + w].n;
+      const double* q = p.data() + (size_t)w * 3 * np;
+      for (int j = 0; j < n; ++j)
+        for (int a = 0; a < 3; ++a) state[off + 3 * j + a] = q[a * np + j];
+      off += 3 * (size_t)n;
+    }
   } else {
     const int np = h->np;
     std::vector<float> p((size_t)count * 6 * np);
@@ -518,6 +614,28 @@ int32_t sadmc_read_bins(sadmc_handle* h, int32_t walker, double* lnw, uint64_t* 
   return SADMC_OK;
 }
 
+int32_t sadmc_plane_bins(sadmc_handle* h, int64_t* plane_bins) {
+  if (!h || !plane_bins) return fail(SADMC_ERR_INVALID, "null argument");
+  *plane_bins = h->nb;
+  return SADMC_OK;
+}
+
+int32_t sadmc_read_planes(sadmc_handle* h, double* lnw, uint64_t* hist, int32_t* range,
+                          double* bins_min) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  const size_t n = (size_t)h->W * (size_t)h->nb;
+  if (lnw) CUDA_TRY(cudaMemcpyAsync(lnw, h->planes.lnw, n * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (hist) CUDA_TRY(cudaMemcpyAsync(hist, h->planes.hist, n * 8, cudaMemcpyDeviceToHost, h->stream));
+  int32_t r = h->pull_cores();
+  if (r) return r;
+  for (int w = 0; w < h->W; ++w) {
+    if (range) { range[2 * w] = h->h_cores[w].b_lo; range[2 * w + 1] = h->h_cores[w].b_hi; }
+    if (bins_min) bins_min[w] = h->h_cores[w].cur_min;
+  }
+  return SADMC_OK;
+}
+
 int32_t sadmc_read_wl_hist(sadmc_handle* h, int32_t walker, uint64_t* hist, int64_t* n, double* min_energy) {
   if (!h || walker < 0 || walker >= h->W || !n) return fail(SADMC_ERR_INVALID, "bad argument");
   WalkerCore k;
@@ -609,6 +727,24 @@ int32_t sadmc_autotune(sadmc_handle* h, uint64_t moves, int32_t* best_lpw, doubl
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
   if (best_lpw) *best_lpw = h->lpw;
   if (best_ms) *best_ms = 0.0;
+  return SADMC_OK;
+}
+
+int32_t sadmc_draws(int32_t system, uint32_t n, uint64_t seed, uint32_t walker, uint64_t t0,
+                    int32_t count, uint32_t stream_pair, uint32_t* idx2, float* g3, double* u) {
+  if (!idx2 || !g3 || !u || count <= 0 || n == 0) return fail(SADMC_ERR_INVALID, "bad argument");
+  uint32_t* di = nullptr;
+  float* dg = nullptr;
+  double* du = nullptr;
+  cudaError_t e = cudaMalloc(&di, sizeof(uint32_t) * 2 * count);
+  if (e == cudaSuccess) e = cudaMalloc(&dg, sizeof(float) * 3 * count);
+  if (e == cudaSuccess) e = cudaMalloc(&du, sizeof(double) * count);
+  if (e == cudaSuccess) e = launch_draws(system, n, seed, walker, t0, count, stream_pair, di, dg, du, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(idx2, di, sizeof(uint32_t) * 2 * count, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(g3, dg, sizeof(float) * 3 * count, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(u, du, sizeof(double) * count, cudaMemcpyDeviceToHost);
+  cudaFree(di); cudaFree(dg); cudaFree(du);
+  if (e != cudaSuccess) return fail(SADMC_ERR_CUDA, cudaGetErrorString(e));
   return SADMC_OK;
 }
 

@@ -1,0 +1,413 @@
+// Periodic fluids with subcell lists: the square well with a hard core
+// (src/system/optsquare.rs, the hard-sphere contact-count system) and the WCA fluid
+// (src/system/wca.rs), many walkers of uneven N and box per launch.
+//
+// Cell list: the reference registers every atom in the 27 subcells around its own
+// (optcell.rs:131-160) and a query reads one list.  Here each atom sits in one bucket of
+// its own subcell and a query walks the 27 buckets around the query point; for each
+// neighbour bucket the periodic image shift is the one the reference stores with the
+// registration (offset -1 / +1 when the unwrapped neighbour index is below 0 / at n_c),
+// so the candidate set and every candidate image position are identical whenever
+// n_c >= 3 (geometries with fewer subcells are rejected: the reference double-counts
+// there, optcell.rs:343-346).
+//
+// Square well: overlap (r^2 < sigma^2) and contact (r^2 < lambda^2) decisions are those
+// of optsquare.rs:74-95 on the FP64 expression (p_j - off*L) - r, x*x + y*y + z*z.  They
+// are taken from binary32 copies when the binary32 r^2 lies outside a proven error
+// margin of both thresholds, else from the FP64 expression itself.  Energies are
+// integers and exact.  WCA: binary32 pair energies (wca.rs:66-76), FP64 re-sum every
+// resum_interval moves.
+#include <cuda_runtime.h>
+
+#include "sadmc_common.cuh"
+#include "sadmc_fh.cuh"
+#include "sadmc_launch.h"
+#include "sadmc_rng.cuh"
+
+namespace sadmc {
+namespace dev {
+
+__device__ __forceinline__ float wca_v32(float r2, float rc2) {
+  if (!(r2 < rc2)) return 0.0f;
+  float s = __fdividef(1.0f, r2);
+  float s3 = s * s * s;
+  return 4.0f * s3 * (s3 - 1.0f) + 1.0f;
+}
+__device__ __forceinline__ double wca_v64(double r2, double rc2) {
+  if (!(r2 < rc2)) return 0.0;
+  double s = 1.0 / r2;
+  return 4.0 * (powi6(s) - powi3(s)) + 1.0;
+}
+
+// floor(x / L * n) of optcell.rs:112-124 with an FP32 pre-filter.
+__device__ __forceinline__ int subcell_axis(double x, double L, int n) {
+  float q = __fmul_rn(__fdiv_rn((float)x, (float)L), (float)n);
+  int qi = __float2int_rd(q);
+  float fr = q - (float)qi;
+  if (fr > 2e-5f && fr < 1.0f - 2e-5f) return qi;
+  int e = (int)floor(x / L * (double)n);
+  // x / L * n rounds up to n only for x within an ulp of L; keep the index in the grid
+  return e < 0 ? 0 : (e >= n ? n - 1 : e);
+}
+
+// put_in_cell (optcell.rs:277-309) for one coordinate; bounded loop (a step of more
+// than 64 boxes is reported through *bad).
+__device__ __forceinline__ double wrap_axis(double r, double L, bool* bad) {
+  int guard = 0;
+  if (r < 0.0) {
+    do { r += L; } while (r < 0.0 && ++guard < 64);
+  } else {
+    while (r >= L && ++guard < 64) r -= L;
+  }
+  if (guard >= 64) *bad = true;
+  return r;
+}
+
+struct CellWalker {
+  double* p;       // [3][np] FP64 planes of this walker
+  float4* p32;     // [np] binary32 copy (w unused)
+  int* cell_of;    // [np]
+  int* cnt;        // [cells]
+  int* atoms;      // [cells][bucket]
+  double L[3];
+  float L32[3];
+  int nc[3];
+  int np, bucket;
+  __device__ int cell_index(int x, int y, int z) const { return (x * nc[1] + y) * nc[2] + z; }
+};
+
+template <int LPW, int KIND>
+struct CellOps {
+  // Sum over the 27 buckets around cell (cx,cy,cz) of query position q (excluding atom
+  // `skip`).  SW: counts contacts, sets *overlap; WCA: binary32 energy.
+  __device__ static void scan(const CellWalker& cw, int k0, int cx, int cy, int cz, double qx,
+                              double qy, double qz, float q32x, float q32y, float q32z, int skip,
+                              double wsqr, float wsqr32, bool newq, int& contacts, bool& overlap,
+                              float& e32, float rc2_32) {
+    // k0: the neighbour offset handled by this lane (0..26)
+    const int dx = k0 / 9 - 1, dy = (k0 / 3) % 3 - 1, dz = k0 % 3 - 1;
+    int ux = cx + dx, uy = cy + dy, uz = cz + dz;
+    int ox = 0, oy = 0, oz = 0;  // reference offset: image = p - off * L
+    if (ux < 0) { ux += cw.nc[0]; ox = 1; } else if (ux >= cw.nc[0]) { ux -= cw.nc[0]; ox = -1; }
+    if (uy < 0) { uy += cw.nc[1]; oy = 1; } else if (uy >= cw.nc[1]) { uy -= cw.nc[1]; oy = -1; }
+    if (uz < 0) { uz += cw.nc[2]; oz = 1; } else if (uz >= cw.nc[2]) { uz -= cw.nc[2]; oz = -1; }
+    const int c = cw.cell_index(ux, uy, uz);
+    const int m = cw.cnt[c];
+    const int* list = cw.atoms + (size_t)c * cw.bucket;
+    const float sx = (float)ox * cw.L32[0], sy = (float)oy * cw.L32[1], sz = (float)oz * cw.L32[2];
+    for (int k = 0; k < m; ++k) {
+      const int j = list[k];
+      if (j == skip) continue;
+      const float4 pj = cw.p32[j];
+      const float ax = (pj.x - sx) - q32x, ay = (pj.y - sy) - q32y, az = (pj.z - sz) - q32z;
+      const float d2 = ax * ax + ay * ay + az * az;
+      if (KIND == SYS_SW) {
+        bool near = fabsf(d2 - 1.0f) < 2e-4f || fabsf(d2 - wsqr32) < 2e-4f;
+        if (!near) {
+          if (d2 < 1.0f) { if (newq) overlap = true; else ++contacts; }
+          else if (d2 < wsqr32) ++contacts;
+        } else {
+          // the reference's FP64 expression (optsquare.rs:78-86)
+          const double bx = (cw.p[j] - (double)ox * cw.L[0]) - qx;
+          const double by = (cw.p[cw.np + j] - (double)oy * cw.L[1]) - qy;
+          const double bz = (cw.p[2 * cw.np + j] - (double)oz * cw.L[2]) - qz;
+          const double e2 = bx * bx + by * by + bz * bz;
+          if (e2 < 1.0) { if (newq) overlap = true; else ++contacts; }
+          else if (e2 < wsqr) ++contacts;
+        }
+      } else {
+        e32 += wca_v32(d2, rc2_32);
+      }
+    }
+  }
+};
+
+template <int LPW, int KIND>
+__global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s) {
+  constexpr int WPW = 32 / LPW;
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (warp * WPW >= m.n_walkers) return;
+  const int group = lane / LPW, glane = lane % LPW;
+  int w = warp * WPW + group;
+  const bool wr = w < m.n_walkers;
+  if (!wr) w = m.n_walkers - 1;
+  const unsigned gmask = group_mask<LPW>(group);
+
+  Fh<LPW> fh;
+  fh.load(m.cores, m.P, m.B, w, gmask, glane, wr);
+  CellWalker cw;
+  cw.np = s.np;
+  cw.bucket = s.bucket;
+  cw.p = s.pos + (size_t)w * 3 * s.np;
+  cw.p32 = reinterpret_cast<float4*>(s.pos32) + (size_t)w * s.np;
+  cw.cell_of = s.cell_of + (size_t)w * s.np;
+  cw.cnt = s.cell_count + (size_t)w * s.cell_cap;
+  cw.atoms = s.cell_atoms + (size_t)w * s.cell_cap * s.bucket;
+  for (int a = 0; a < 3; ++a) {
+    cw.L[a] = s.box[3 * w + a];
+    cw.L32[a] = (float)cw.L[a];
+    cw.nc[a] = s.ncell[3 * w + a];
+  }
+  const int n = fh.c.n;
+  const double rc = s.r_cut;
+  const double wsqr = rc * rc;
+  const float wsqr32 = (float)wsqr;
+  RecentScale rsb;
+  rsb.init();
+  for (uint64_t it = 0; it < m.n_moves; ++it) {
+    const uint64_t t = fh.c.moves + 1;
+    double rs, omrs;
+    rsb.get(t, lane, rs, omrs);
+    fh.begin_move(omrs);
+    const Draws d = draws_continuous(m.seed, (uint32_t)w, t, (uint32_t)n, 0u);
+    const int a = (int)d.which;
+    const double sc = fh.c.tscale;
+    const double fx = cw.p[a], fy = cw.p[s.np + a], fz = cw.p[2 * s.np + a];
+    bool bad = false;
+    // plan_move: put_in_cell(from + g * scale) (optsquare.rs:273-284, wca.rs:342-353)
+    const double tx = wrap_axis(fx + (double)d.g0 * sc, cw.L[0], &bad);
+    const double ty = wrap_axis(fy + (double)d.g1 * sc, cw.L[1], &bad);
+    const double tz = wrap_axis(fz + (double)d.g2 * sc, cw.L[2], &bad);
+    const int nx = subcell_axis(tx, cw.L[0], cw.nc[0]);
+    const int ny = subcell_axis(ty, cw.L[1], cw.nc[1]);
+    const int nz = subcell_axis(tz, cw.L[2], cw.nc[2]);
+    const int old_c = cw.cell_of[a];
+    const int ocx = old_c / (cw.nc[1] * cw.nc[2]), ocy = (old_c / cw.nc[2]) % cw.nc[1], ocz = old_c % cw.nc[2];
+    const float t32x = (float)tx, t32y = (float)ty, t32z = (float)tz;
+    const float4 f32 = cw.p32[a];
+    int cn = 0, co = 0;
+    bool overlap = false;
+    float en = 0.0f, eo = 0.0f;
+    for (int k = glane; k < 54; k += LPW) {
+      if (k < 27)
+        CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, tx, ty, tz, t32x, t32y, t32z, a, wsqr, wsqr32,
+                                 true, cn, overlap, en, wsqr32);
+      else
+        CellOps<LPW, KIND>::scan(cw, k - 27, ocx, ocy, ocz, fx, fy, fz, f32.x, f32.y, f32.z, a,
+                                 wsqr, wsqr32, false, co, overlap, eo, wsqr32);
+    }
+    const int new_c = cw.cell_index(nx, ny, nz);
+    bool possible;
+    double e2;
+    if (KIND == SYS_SW) {
+      // e = E - (contacts at the new position) + (contacts at the old position); the
+      // FP64 sequence of unit steps of optsquare.rs:75-92 is exact on integers
+      const int newc = group_sum<LPW>(cn, gmask);
+      const int oldc = group_sum<LPW>(co, gmask);
+      possible = !__any_sync(gmask, overlap);
+      e2 = fh.c.E - (double)newc + (double)oldc;
+    } else {
+      const float de = group_sum<LPW>(en - eo, gmask);
+      possible = true;
+      e2 = fh.c.E + (double)de;
+    }
+    possible = possible && !bad && finite64(e2);
+    const int new_count = cw.cnt[new_c];
+    if (possible && new_c != old_c && new_count >= cw.bucket) {
+      possible = false;
+      fh.c.status |= ST_CELL_OVERFLOW;
+    }
+    if (m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
+      TraceRec r;
+      r.e1 = fh.c.E;
+      r.e2 = possible ? e2 : __longlong_as_double(0x7ff8000000000000ll);
+      m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = r;
+    }
+    const bool acc = fh.decide(possible, e2, d.u53, rs);
+    if (acc) {
+      // ConfirmSystem::confirm -> Cell::move_atom (optcell.rs:162-175)
+      if (new_c != old_c) {
+        int* lo = cw.atoms + (size_t)old_c * cw.bucket;
+        const int mo = cw.cnt[old_c];
+        int pos = -1;
+        for (int k = glane; k < mo; k += LPW)
+          if (lo[k] == a) pos = k;
+        for (int o = LPW / 2; o > 0; o >>= 1) {
+          int x = __shfl_xor_sync(gmask, pos, o, LPW);
+          pos = x > pos ? x : pos;
+        }
+        __syncwarp(gmask);
+        if (wr && pos >= 0) {
+          lo[pos] = lo[mo - 1];
+          cw.cnt[old_c] = mo - 1;
+          cw.atoms[(size_t)new_c * cw.bucket + new_count] = a;
+          cw.cnt[new_c] = new_count + 1;
+          cw.cell_of[a] = new_c;
+        }
+      }
+      if (wr) {
+        cw.p[a] = tx; cw.p[s.np + a] = ty; cw.p[2 * s.np + a] = tz;
+        cw.p32[a] = make_float4(t32x, t32y, t32z, 0.0f);
+      }
+      __syncwarp(gmask);
+      fh.c.E = e2;
+    }
+    fh.finish_move(acc);
+    if (KIND == SYS_WCA && m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
+      // FP64 re-sum (wca.rs:222-230)
+      double e = 0.0;
+      for (int i = glane; i < n; i += LPW) {
+        const double ix = cw.p[i], iy = cw.p[s.np + i], iz = cw.p[2 * s.np + i];
+        const int ci = cw.cell_of[i];
+        const int cx = ci / (cw.nc[1] * cw.nc[2]), cy = (ci / cw.nc[2]) % cw.nc[1], cz = ci % cw.nc[2];
+        for (int k0 = 0; k0 < 27; ++k0) {
+          const int dx = k0 / 9 - 1, dy = (k0 / 3) % 3 - 1, dz = k0 % 3 - 1;
+          int ux = cx + dx, uy = cy + dy, uz = cz + dz, ox = 0, oy = 0, oz = 0;
+          if (ux < 0) { ux += cw.nc[0]; ox = 1; } else if (ux >= cw.nc[0]) { ux -= cw.nc[0]; ox = -1; }
+          if (uy < 0) { uy += cw.nc[1]; oy = 1; } else if (uy >= cw.nc[1]) { uy -= cw.nc[1]; oy = -1; }
+          if (uz < 0) { uz += cw.nc[2]; oz = 1; } else if (uz >= cw.nc[2]) { uz -= cw.nc[2]; oz = -1; }
+          const int c = cw.cell_index(ux, uy, uz);
+          const int mm = cw.cnt[c];
+          for (int q = 0; q < mm; ++q) {
+            const int j = cw.atoms[(size_t)c * cw.bucket + q];
+            if (j == i) continue;
+            const double bx = (cw.p[j] - (double)ox * cw.L[0]) - ix;
+            const double by = (cw.p[s.np + j] - (double)oy * cw.L[1]) - iy;
+            const double bz = (cw.p[2 * s.np + j] - (double)oz * cw.L[2]) - iz;
+            e += wca_v64(bx * bx + by * by + bz * bz, wsqr);
+          }
+        }
+      }
+      const double e64 = group_sum<LPW>(e, gmask) * 0.5;
+      const double dr = fabs(e64 - fh.c.E);
+      if (dr > fh.c.drift) fh.c.drift = dr;
+      if (dr > m.drift_tol) fh.c.status |= ST_DRIFT;
+      fh.c.E = e64;
+      fh.grew_front = false;
+      if (!fh.prepare(e64)) fh.c.status |= ST_BIN_RANGE;
+      else {
+        if (fh.grew_front) fh.reindex_after_growth();
+        fh.move_cur(fh.gidx(e64));
+      }
+    }
+  }
+  fh.store(m.cores, w);
+}
+
+// Subcell grid of each walker (one thread per walker, atoms in index order):
+// n_c = floor(L / r_cut) per axis (optcell.rs:63-73), subcell of each atom
+// (optcell.rs:112-124) and the binary32 position copy.
+__global__ void cell_build_kernel(const WalkerCore* cores, CellSys s, int n_walkers) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= n_walkers) return;
+  const int n = cores[w].n;
+  const double* p = s.pos + (size_t)w * 3 * s.np;
+  float4* p32 = reinterpret_cast<float4*>(s.pos32) + (size_t)w * s.np;
+  int* cell_of = s.cell_of + (size_t)w * s.np;
+  int* cnt = s.cell_count + (size_t)w * s.cell_cap;
+  int* atoms = s.cell_atoms + (size_t)w * s.cell_cap * s.bucket;
+  double L[3];
+  int nc[3];
+  for (int a = 0; a < 3; ++a) {
+    L[a] = s.box[3 * w + a];
+    nc[a] = (int)floor(L[a] / s.r_cut);
+    s.ncell[3 * w + a] = nc[a];
+  }
+  int* status = s.build_status + w;
+  *status = 0;
+  if (nc[0] < 3 || nc[1] < 3 || nc[2] < 3 || nc[0] * nc[1] * nc[2] > s.cell_cap) {
+    *status = ST_BAD_INPUT;
+    return;
+  }
+  for (int c = 0; c < nc[0] * nc[1] * nc[2]; ++c) cnt[c] = 0;
+  for (int i = 0; i < n; ++i) {
+    const double x = p[i], y = p[s.np + i], z = p[2 * s.np + i];
+    p32[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+    if (!(x >= 0.0 && x < L[0] && y >= 0.0 && y < L[1] && z >= 0.0 && z < L[2])) {
+      *status = ST_BAD_INPUT;
+      return;
+    }
+    const int cx = subcell_axis(x, L[0], nc[0]), cy = subcell_axis(y, L[1], nc[1]),
+              cz = subcell_axis(z, L[2], nc[2]);
+    const int c = (cx * nc[1] + cy) * nc[2] + cz;
+    if (cnt[c] >= s.bucket) { *status = ST_CELL_OVERFLOW; return; }
+    atoms[(size_t)c * s.bucket + cnt[c]] = i;
+    cnt[c] += 1;
+    cell_of[i] = c;
+  }
+}
+
+// compute_energy: WCA (wca.rs:222-230) and square well (optsquare.rs:176-186) in FP64
+// over the same candidate images.  One warp per walker.
+template <int KIND>
+__global__ void cell_energy_kernel(const WalkerCore* cores, CellSys s, int n_walkers, double* out) {
+  const int lane = threadIdx.x & 31;
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (w >= n_walkers) return;
+  const int n = cores[w].n;
+  const double* p = s.pos + (size_t)w * 3 * s.np;
+  const int* cell_of = s.cell_of + (size_t)w * s.np;
+  const int* cnt = s.cell_count + (size_t)w * s.cell_cap;
+  const int* atoms = s.cell_atoms + (size_t)w * s.cell_cap * s.bucket;
+  double L[3];
+  int nc[3];
+  for (int a = 0; a < 3; ++a) { L[a] = s.box[3 * w + a]; nc[a] = s.ncell[3 * w + a]; }
+  const double rc2 = s.r_cut * s.r_cut;
+  double e = 0.0;
+  long long contacts = 0;
+  for (int i = lane; i < n; i += 32) {
+    const double ix = p[i], iy = p[s.np + i], iz = p[2 * s.np + i];
+    const int ci = cell_of[i];
+    const int cx = ci / (nc[1] * nc[2]), cy = (ci / nc[2]) % nc[1], cz = ci % nc[2];
+    for (int k0 = 0; k0 < 27; ++k0) {
+      const int dx = k0 / 9 - 1, dy = (k0 / 3) % 3 - 1, dz = k0 % 3 - 1;
+      int ux = cx + dx, uy = cy + dy, uz = cz + dz, ox = 0, oy = 0, oz = 0;
+      if (ux < 0) { ux += nc[0]; ox = 1; } else if (ux >= nc[0]) { ux -= nc[0]; ox = -1; }
+      if (uy < 0) { uy += nc[1]; oy = 1; } else if (uy >= nc[1]) { uy -= nc[1]; oy = -1; }
+      if (uz < 0) { uz += nc[2]; oz = 1; } else if (uz >= nc[2]) { uz -= nc[2]; oz = -1; }
+      const int c = (ux * nc[1] + uy) * nc[2] + uz;
+      for (int q = 0; q < cnt[c]; ++q) {
+        const int j = atoms[(size_t)c * s.bucket + q];
+        if (j == i) continue;
+        // (r1 - r2) with r2 the image of j (optcell.rs:82-89)
+        const double bx = ix - (p[j] - (double)ox * L[0]);
+        const double by = iy - (p[s.np + j] - (double)oy * L[1]);
+        const double bz = iz - (p[2 * s.np + j] - (double)oz * L[2]);
+        const double d2 = bx * bx + by * by + bz * bz;
+        if (KIND == SYS_SW) { if (d2 < rc2) ++contacts; }
+        else e += wca_v64(d2, rc2);
+      }
+    }
+  }
+  if (KIND == SYS_SW) {
+    for (int o = 16; o > 0; o >>= 1) contacts += __shfl_xor_sync(0xffffffffu, contacts, o);
+    if (lane == 0) out[w] = -(double)contacts * 0.5;
+  } else {
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if (lane == 0) out[w] = e * 0.5;
+  }
+}
+
+}  // namespace dev
+
+#define SADMC_CELL_CASE(L, K)                                                           \
+  if (lpw == L && s.kind == K) {                                                        \
+    const int warps = (m.n_walkers + (32 / L) - 1) / (32 / L);                          \
+    dev::cell_move_kernel<L, K><<<(warps * 32 + 127) / 128, 128, 0, st>>>(m, s);        \
+    return cudaGetLastError();                                                          \
+  }
+
+cudaError_t launch_cell_move(const MoveLaunch& m, const CellSys& s, int lpw, cudaStream_t st) {
+  SADMC_CELL_CASE(32, SYS_SW) SADMC_CELL_CASE(16, SYS_SW) SADMC_CELL_CASE(8, SYS_SW)
+  SADMC_CELL_CASE(4, SYS_SW)
+  SADMC_CELL_CASE(32, SYS_WCA) SADMC_CELL_CASE(16, SYS_WCA) SADMC_CELL_CASE(8, SYS_WCA)
+  SADMC_CELL_CASE(4, SYS_WCA)
+  return cudaErrorInvalidConfiguration;
+}
+
+cudaError_t launch_cell_build(const WalkerCore* cores, const CellSys& s, int n_walkers,
+                              cudaStream_t st) {
+  dev::cell_build_kernel<<<(n_walkers + 127) / 128, 128, 0, st>>>(cores, s, n_walkers);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cell_energy(const WalkerCore* cores, const CellSys& s, int n_walkers,
+                               double* out, cudaStream_t st) {
+  const int blocks = (n_walkers * 32 + 127) / 128;
+  if (s.kind == SYS_SW) dev::cell_energy_kernel<SYS_SW><<<blocks, 128, 0, st>>>(cores, s, n_walkers, out);
+  else dev::cell_energy_kernel<SYS_WCA><<<blocks, 128, 0, st>>>(cores, s, n_walkers, out);
+  return cudaGetLastError();
+}
+
+}  // namespace sadmc

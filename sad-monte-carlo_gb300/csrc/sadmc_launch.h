@@ -54,7 +54,7 @@ cudaError_t launch_ising_energy(const IsingSys& s, int n_walkers, double* out, c
 // one-bucket-per-atom subcell grid.
 struct CellSys {
   double* pos;        // [walker][3][np] FP64 planes
-  float* pos32;       // [walker][3][np] binary32 copy (pre-filters)
+  float* pos32;       // [walker][np] float4 (x, y, z, 0) binary32 copy (pre-filters)
   int np;
   double* box;        // [walker][3]
   int* ncell;         // [walker][3] subcells per axis (>= 3)
@@ -65,6 +65,7 @@ struct CellSys {
   int bucket;         // atom slots per subcell
   double r_cut;       // well width (square well) or 2^(1/6) (WCA)
   int kind;           // SYS_SW or SYS_WCA
+  int* build_status;  // [walker] status of the last cell build
 };
 cudaError_t launch_cell_build(const WalkerCore* cores, const CellSys& s, int n_walkers,
                               cudaStream_t st);
@@ -80,5 +81,10 @@ cudaError_t launch_init_planes(const WalkerCore* cores, BinPlanes B, int nbins, 
 // FP64 (plotting/final_heat_capacity.py:79-88).  One block per temperature.
 cudaError_t launch_heat_capacity(const double* T, int nT, const double* E, const double* S,
                                  int n, double* C, cudaStream_t st);
+
+// The per-move draws of walker `walker` for moves t0 .. t0+count-1 (device pointers).
+cudaError_t launch_draws(int system, uint32_t n, uint64_t seed, uint32_t walker, uint64_t t0,
+                         int count, uint32_t stream_pair, uint32_t* idx2, float* g3, double* u,
+                         cudaStream_t st);
 
 }  // namespace sadmc

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
     // from_params descent (energy.rs:840-851): downhill-only proposals of rms 0.05 on
     // the descent stream until E < max_allowed_energy.
     const DS sc = ds_from_double(0.05);
-    bool done = false;
+    bool done = fh.c.pad1 != 0;  // finished in an earlier launch
     uint64_t steps = fh.c.pad2;
     for (uint64_t it = 0; it < m.n_moves; ++it) {
       if (__all_sync(0xffffffffu, done)) break;
@@ -180,6 +180,7 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
       }
     }
     fh.c.pad2 = steps;
+    fh.c.pad1 = done ? 1 : 0;
     double e64 = lj.energy64();
     fh.c.E = e64;
     if (!(e64 < m.descent_max)) fh.c.status |= ST_DESCENT_FAILED;

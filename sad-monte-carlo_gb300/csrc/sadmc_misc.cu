@@ -1,7 +1,9 @@
 // Plane initialisation and the FP64 heat-capacity reconstruction.
 #include <cuda_runtime.h>
 
+#include "sadmc_fh.cuh"
 #include "sadmc_launch.h"
+#include "sadmc_rng.cuh"
 
 namespace sadmc {
 namespace dev {
@@ -102,4 +104,29 @@ cudaError_t launch_heat_capacity(const double* T, int nT, const double* E, const
   return cudaGetLastError();
 }
 
+}  // namespace sadmc
+
+namespace sadmc {
+namespace dev {
+__global__ void draws_kernel(int system, uint32_t n, uint64_t seed, uint32_t walker, uint64_t t0,
+                             int count, uint32_t stream_pair, uint32_t* idx2, float* g3, double* u) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const uint64_t t = t0 + (uint64_t)k;
+  Draws d = system == SYS_ISING ? draws_ising(seed, walker, t, n)
+                                : draws_continuous(seed, walker, t, n, stream_pair);
+  idx2[2 * k] = d.which;
+  idx2[2 * k + 1] = d.j;
+  g3[3 * k] = d.g0; g3[3 * k + 1] = d.g1; g3[3 * k + 2] = d.g2;
+  u[k] = u53_to_double(d.u53);
+}
+}  // namespace dev
+
+cudaError_t launch_draws(int system, uint32_t n, uint64_t seed, uint32_t walker, uint64_t t0,
+                         int count, uint32_t stream_pair, uint32_t* idx2, float* g3, double* u,
+                         cudaStream_t st) {
+  dev::draws_kernel<<<(count + 127) / 128, 128, 0, st>>>(system, n, seed, walker, t0, count,
+                                                         stream_pair, idx2, g3, u);
+  return cudaGetLastError();
+}
 }  // namespace sadmc

@@ -91,11 +91,14 @@ def lib():
         "sadmc_nbins": (I32, [P, I32, P, P, P]),
         "sadmc_read_bins": (I32, [P, I32, P, P, P, P, P, P, P]),
         "sadmc_read_wl_hist": (I32, [P, I32, P, P, P]),
+        "sadmc_plane_bins": (I32, [P, P]), "sadmc_read_planes": (I32, [P, P, P, P, P]),
         "sadmc_read_scalars": (I32, [P, I32, P]),
         "sadmc_counters": (I32, [P, P, P]), "sadmc_status": (I32, [P, P]),
         "sadmc_set_trace": (I32, [P, U64]), "sadmc_read_trace": (I32, [P, I32, P, P, P]),
         "sadmc_lanes_per_walker": (I32, [P]), "sadmc_autotune": (I32, [P, U64, P, P]),
         "sadmc_heat_capacity": (I32, [P, I32, P, P, I32, P]),
+        "sadmc_draws": (I32, [I32, ctypes.c_uint32, U64, ctypes.c_uint32, U64, I32, ctypes.c_uint32,
+                              P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -173,9 +176,16 @@ class Batch:
     def W(self):
         return self.cfg.n_walkers
 
-    def upload(self, states, begin=0):
-        flat = np.ascontiguousarray(np.concatenate([np.ravel(s) for s in states]), np.float64)
-        _check(lib().sadmc_upload_state(self.h, begin, len(states), _p(flat)))
+    def upload(self, states, begin=0, count=None):
+        """states: a list of per-walker arrays, or one packed float64 array for `count`
+        walkers (positions x,y,z walker after walker; Ising spins L*L per walker)."""
+        if isinstance(states, np.ndarray) and states.ndim == 1:
+            flat = np.ascontiguousarray(states, np.float64)
+            count = self.W - begin if count is None else count
+        else:
+            flat = np.ascontiguousarray(np.concatenate([np.ravel(s) for s in states]), np.float64)
+            count = len(states)
+        _check(lib().sadmc_upload_state(self.h, begin, count, _p(flat)))
 
     def state(self, w):
         n = int(self.n[w])
@@ -232,6 +242,23 @@ class Batch:
         return dict(lnw=lnw, hist=hist, t_found=tf, sumE=sE, sumE2=sE2, round_trips=rt,
                     visited=vis, min=mn.value, width=wd.value)
 
+    def plane_bins(self):
+        n = ctypes.c_int64(0)
+        _check(lib().sadmc_plane_bins(self.h, ctypes.byref(n)))
+        return n.value
+
+    def read_planes(self, lnw=None, hist=None):
+        """Copy the whole ln w / histogram planes into (optionally pinned) host arrays."""
+        nb = self.plane_bins()
+        if lnw is None:
+            lnw = np.zeros(self.W * nb)
+        if hist is None:
+            hist = np.zeros(self.W * nb, np.uint64)
+        rng = np.zeros(2 * self.W, np.int32)
+        mins = np.zeros(self.W)
+        _check(lib().sadmc_read_planes(self.h, _p(lnw), _p(hist), _p(rng), _p(mins)))
+        return lnw, hist, rng.reshape(-1, 2), mins
+
     def wl_hist(self, w):
         n, me = ctypes.c_int64(0), ctypes.c_double(0)
         _check(lib().sadmc_read_wl_hist(self.h, w, None, ctypes.byref(n), ctypes.byref(me)))
@@ -270,6 +297,15 @@ class Batch:
         lpw, ms = ctypes.c_int32(0), ctypes.c_double(0)
         _check(lib().sadmc_autotune(self.h, int(moves), ctypes.byref(lpw), ctypes.byref(ms)))
         return lpw.value, ms.value
+
+
+def draws(system, n, seed, walker, t0, count, stream_pair=0):
+    """The device-side per-move draws (diagnostic): (idx [count,2], g [count,3], u [count])."""
+    idx = np.zeros(2 * count, np.uint32)
+    g = np.zeros(3 * count, np.float32)
+    u = np.zeros(count)
+    _check(lib().sadmc_draws(system, n, seed, walker, t0, count, stream_pair, _p(idx), _p(g), _p(u)))
+    return idx.reshape(-1, 2), g.reshape(-1, 3), u
 
 
 def heat_capacity(T, E, S):

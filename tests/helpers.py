@@ -32,7 +32,19 @@ def assert_bins_equal(gb, ob, keys=BIN_KEYS, label=""):
             raise AssertionError(f"{label} bins[{k}] differ at {bad}: gpu {a[bad]} oracle {b[bad]}")
 
 
-def assert_scalars_equal(gs, os_, keys=EXACT_SCALARS, label=""):
+COMMON_SCALARS = ["moves", "accepted", "acceptance_rate", "translation_scale", "method_kind",
+                  "max_S", "max_S_index", "energy"]
+METHOD_SCALARS = {  # Method fields per variant (energy.rs:212-244)
+    0: ["too_lo", "too_hi", "tL", "tF", "num_states", "highest_hist", "latest_parameter"],
+    1: ["t0"],
+    2: ["gamma", "lowest_hist", "wl_highest_hist", "total_hist", "wl_num_states", "min_energy"],
+    4: [],
+}
+
+
+def assert_scalars_equal(gs, os_, keys=None, label=""):
+    if keys is None:
+        keys = COMMON_SCALARS + METHOD_SCALARS[int(os_["method_kind"])]
     for k in keys:
         assert gs[k] == os_[k], f"{label} scalar {k}: gpu {gs[k]!r} oracle {os_[k]!r}"
 

@@ -1,0 +1,98 @@
+"""GPU periodic-cell kernels against the FP64 oracle.
+
+Square well with a hard core (the contact-count "hard sphere" system): overlap and
+contact decisions are FP64-exact, energies are integers, so the whole run on the same
+Philox stream must be bit-identical.  WCA: binary32 pair energies, checked by trace
+replay like the LJ cluster.
+"""
+import numpy as np
+import pytest
+
+from helpers import assert_bins_equal, assert_scalars_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def sw_walkers(oracle, n, ffs, seed0):
+    out = []
+    for k, ff in enumerate(ffs):
+        pos, box = oracle.init_sw_fcc(n, ff, 1.3, seed0 + k)
+        out.append((pos, box))
+    return out
+
+
+@pytest.mark.parametrize("method,lpw", [("wl", 8), ("sad", 8), ("wl", 32), ("wl", 4), ("samc", 16)])
+def test_square_well_bit_exact(gpu, oracle, method, lpw):
+    n, moves, seed = 108, 20000, 9
+    ffs = [0.30, 0.35, 0.40, 0.45, 0.50, 0.32, 0.38, 0.47]
+    ws = sw_walkers(oracle, n, ffs, 40)
+    W = len(ws)
+    kw = {"wl": dict(method=2), "sad": dict(method=0, min_T=0.5), "samc": dict(method=1, t0=1000.0)}[method]
+    cfg = gpu.make_config(gpu.SW, W, n, e_lo=-6.0 * n - 2, e_hi=2.0, well_width=1.3, seed=seed,
+                          translation_scale=0.05, lanes_per_walker=lpw, **kw)
+    b = gpu.Batch(cfg, [(n, 0.0, box) for _, box in ws])
+    b.upload([p for p, _ in ws])
+    E0 = b.compute_energies()
+    b.initialize()
+    b.run(moves // 2)
+    b.run(moves - moves // 2)
+    for w, (pos, box) in enumerate(ws):
+        ow = oracle.Walker(oracle.make_config(oracle.SW, n, box=box, well_width=1.3, seed=seed,
+                                              walker=w, translation_scale=0.05, **kw), pos)
+        assert ow.energy() == E0[w]
+        ow.run(moves)
+        label = f"sw {method} lpw{lpw} walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_array_equal(b.state(w), ow.state())
+    np.testing.assert_array_equal(b.energies(), b.compute_energies())
+    assert not b.status().any()
+
+
+def test_square_well_rejects_small_boxes(gpu):
+    cfg = gpu.make_config(gpu.SW, 1, 8, e_lo=-50, e_hi=2, well_width=1.3)
+    with pytest.raises(gpu.SadmcError):
+        gpu.Batch(cfg, [(8, 0.0, (3.0, 3.0, 3.0))])  # floor(3/1.3) = 2 subcells
+
+
+def wca_config(n, rho, seed):
+    """Jittered simple-cubic start, no close contacts."""
+    L = (n / rho) ** (1 / 3)
+    m = int(np.ceil(n ** (1 / 3)))
+    rng = np.random.default_rng(seed)
+    g = np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)][:n], float)
+    pos = (g + 0.5 + rng.uniform(-0.05, 0.05, g.shape)) * (L / m)
+    return np.mod(pos, L), (L, L, L)
+
+
+@pytest.mark.parametrize("lpw", [8, 32])
+def test_wca_uneven_trace_replay(gpu, oracle, lpw):
+    specs = [(64, 0.6), (64, 0.9), (128, 0.7), (128, 0.8), (96, 0.75), (64, 0.85)]
+    moves, seed, w_bin = 8000, 4, 0.05
+    confs = [wca_config(n, rho, 10 + k) for k, (n, rho) in enumerate(specs)]
+    W = len(specs)
+    cfg = gpu.make_config(gpu.WCA, W, max(n for n, _ in specs), method=1, t0=500.0,
+                          energy_bin=w_bin, e_lo=-2 * w_bin, e_hi=400.0, max_allowed=380.0,
+                          translation_scale=0.1, seed=seed, lanes_per_walker=lpw,
+                          resum_interval=1000)
+    b = gpu.Batch(cfg, [(n, 0.0, box) for (n, _), (_, box) in zip(specs, confs)])
+    b.upload([p for p, _ in confs])
+    b.initialize()
+    E0 = b.energies()
+    b.set_trace(moves)
+    b.run(moves)
+    for w, ((n, rho), (pos, box)) in enumerate(zip(specs, confs)):
+        e1, e2 = b.trace(w, moves)
+        ow = oracle.Walker(oracle.make_config(oracle.WCA, n, box=box, method=1, t0=500.0,
+                                              energy_bin=w_bin, max_allowed=380.0,
+                                              translation_scale=0.1, seed=seed, walker=w,
+                                              e0=float(E0[w])), pos)
+        disc, mismatch = ow.run_override(e1, e2)
+        assert mismatch == 0, (w, mismatch)
+        assert disc < 1e-3, (w, disc)
+        label = f"wca lpw{lpw} walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-12)
+    np.testing.assert_allclose(b.energies(), b.compute_energies(), atol=1e-3)
+    assert not (b.status() & ~np.uint32(gpu.ST_DESCENT_FAILED)).any()

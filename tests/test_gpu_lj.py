@@ -48,9 +48,7 @@ def test_lj_trace_replay(gpu, oracle, n, lpw):
         assert disc < DE_ABS + DE_REL * 200, f"walker {w}: max |de| {disc}"
         label = f"n{n} lpw{lpw} walker {w}"
         assert_bins_equal(b.bins(w), ow.bins(), label=label)
-        gs, os_ = b.scalars(w), ow.scalars()
-        keys = [k for k in gs if k in os_ and k not in ("drift", "status", "verify_failures", "nan_gamma")]
-        assert_scalars_equal(gs, os_, keys=keys, label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
         np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
     assert not (b.status() & ~np.uint32(gpu.ST_DESCENT_FAILED)).any()
     # incremental energy vs FP64 re-sum of the final configuration
