@@ -407,6 +407,7 @@ struct Fh {
           c.min_energy -= width;
           c.wl_lo -= 1;
           if (wr) wlh[c.wl_lo] = 0;
+          ++len_w;  // hist.insert(0, 0) lengthens hist (energy.rs:678-681)
         }
         while (len_w < len_b) {
           c.wl_hi += 1;

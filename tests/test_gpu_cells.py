@@ -89,7 +89,7 @@ def test_wca_uneven_trace_replay(gpu, oracle, lpw):
                                               e0=float(E0[w])), pos)
         disc, mismatch = ow.run_override(e1, e2)
         assert mismatch == 0, (w, mismatch)
-        assert disc < 1e-3, (w, disc)
+        assert disc < 2e-5, (w, disc)
         label = f"wca lpw{lpw} walker {w}"
         assert_bins_equal(b.bins(w), ow.bins(), label=label)
         assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)

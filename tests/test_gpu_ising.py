@@ -57,3 +57,14 @@ def test_ising_energy_matches_compute_energy(gpu, oracle):
     b, ws = run_pair(gpu, oracle, L=16, W=8, moves=5000, method="sad")
     np.testing.assert_array_equal(b.energies(), b.compute_energies())
     np.testing.assert_array_equal(b.energies(), [w.compute_energy() for w in ws])
+
+
+@pytest.mark.parametrize("system,n", [(0, 8), (0, 32), (1, 31), (1, 1024), (3, 38)])
+def test_device_draws_match_oracle(gpu, oracle, system, n):
+    """The kernels' Philox draws (index, three binary32 normals, 53-bit uniform) equal the
+    oracle's bit for bit."""
+    seed, walker, t0, count = 2**33 + 7, 11, 1, 4000
+    gi, gg, gu = gpu.draws(system, n, seed, walker, t0, count)
+    for k in range(0, count, 7):
+        idx, g, u = oracle.draws(system, n, seed, walker, t0 + k)
+        assert np.array_equal(idx, gi[k]) and np.array_equal(g, gg[k]) and u == gu[k], k

@@ -12,9 +12,11 @@ from helpers import assert_bins_equal, assert_scalars_equal, lj_configs
 
 pytestmark = pytest.mark.gpu
 
-# |e2_gpu - e2_fp64| <= DE_ABS + DE_REL * |e2 - E|: binary32 pair terms on positions
-# rounded to binary32 (relative error ~1e-6 per term) summed over N-1 partners.
+# Binary32 pair terms on positions rounded to binary32 carry ~1e-6 relative error each.
+# Injected proposals: |e2_gpu - e2_fp64| <= DE_ABS + DE_REL * |e2 - E|.  Trace replay: the
+# oracle reports max |e2_gpu - e2_fp64| / (1 + |e1| + |e2|), bounded by REPLAY_REL.
 DE_ABS, DE_REL = 2e-4, 2e-5
+REPLAY_REL = 2e-5
 
 
 def make_batch(gpu, n, W, radius, moves_bins, method=0, seed=3, target_rate=0.5, lpw=0,
@@ -45,7 +47,7 @@ def test_lj_trace_replay(gpu, oracle, n, lpw):
                                               e0=float(E0[w])), confs[w])
         disc, mismatch = ow.run_override(e1, e2)
         assert mismatch == 0, f"walker {w}: possibility differs on {mismatch} moves"
-        assert disc < DE_ABS + DE_REL * 200, f"walker {w}: max |de| {disc}"
+        assert disc < REPLAY_REL, f"walker {w}: max relative |de| {disc}"
         label = f"n{n} lpw{lpw} walker {w}"
         assert_bins_equal(b.bins(w), ow.bins(), label=label)
         assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
