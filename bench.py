@@ -149,7 +149,7 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    walkers, moves = 64, 20000
+    walkers, moves = 256, 100000
     vals = []
     for k in range(args.warmup + args.steps):
         v, _, sec, tm = cpu_sample(threads, walkers=walkers, moves=moves, seed=11 + k)
@@ -272,9 +272,9 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, va, sec, tm = cpu_sample(threads, walkers=128, moves=100000)
+        v, va, sec, tm = cpu_sample(threads, walkers=256, moves=200000)
         cpu = {"value": v, "unit": "moves/s", "cores": threads, "kind": "port",
-               "sample": f"128 C2 walkers x 100000 moves ({tm} moves, {sec:.2f} s wall), FP64 "
+               "sample": f"256 C2 walkers x 200000 moves ({tm} moves, {sec:.2f} s wall), FP64 "
                          "C++ restatement of the reference (Rust toolchain absent)"}
 
     if rank == 0:
@@ -315,8 +315,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--lpw", type=int, default=0, help="lanes per walker (0: library default)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--walkers", type=int, default=WALKERS,
+                    help="walkers (profiling a smaller case; the bench line uses 4096)")
+    ap.add_argument("--moves", type=int, default=MOVES_PER_STEP, help="moves per walker per step")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    global WALKERS, MOVES_PER_STEP
+    WALKERS, MOVES_PER_STEP = args.walkers, args.moves
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -397,11 +397,11 @@ struct EnergyMC {
       double e2 = *e2o;
       if (e2_override) {
         double ge2 = e2_override[moves - 1 - override_base];
-        // |e2_gpu - e2| relative to the magnitude of the pair terms involved, which show
-        // up in E before or after the move (binary32 terms carry ~1e-6 relative error)
+        // |e2_gpu - e2| relative to the sum of |pair terms| of the proposal (binary32
+        // terms carry ~1e-6 relative error each)
         if (ge2 != ge2) ++override_mismatch;  // GPU said impossible, oracle possible
         else max_e2_discrepancy = std::max(max_e2_discrepancy,
-                                           std::fabs(ge2 - e2) / (1.0 + std::fabs(e1) + std::fabs(e2)));
+                                           std::fabs(ge2 - e2) / (1e-3 + sys.last_abs));
         e2 = ge2;
       }
       bool oob = false;

@@ -160,8 +160,8 @@ void orc_run(void* hv, uint64_t nmoves) {
 
 // Replay of a GPU trace: e1[k] (energy at move start) and e2[k] (proposed energy,
 // NaN when impossible) belong to move (moves_at_call + k + 1).  Returns the largest
-// |e2_gpu - e2_oracle| / (1 + |e1| + |e2|); *mismatch counts moves whose possibility
-// differed.
+// |e2_gpu - e2_oracle| / (1e-3 + sum |pair terms|); *mismatch counts moves whose
+// possibility differed.
 double orc_run_override(void* hv, uint64_t nmoves, const double* e1, const double* e2,
                         uint64_t* mismatch) {
   auto* h = (AnyMC*)hv;

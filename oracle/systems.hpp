@@ -30,6 +30,7 @@ inline double powi3(double x) { double x2 = x * x; return x * x2; }
 struct Ising {
   int L = 0;
   double E = 0;
+  double last_abs = 0;
   std::vector<int8_t> S;       // index i + j*L (ising.rs:64)
   bool have_change = false;
   size_t change_site = 0;
@@ -83,6 +84,7 @@ struct Lj {
   double E = 0, error = 0;
   std::vector<V3> pos;
   double max_radius_squared = 0;
+  double last_abs = 0;  // sum of |pair terms| of the last plan (scale of binary32 error)
   bool have_change = false;
   size_t ch_which = 0;
   V3 ch_to{};
@@ -102,9 +104,12 @@ struct Lj {
     if (norm2(r) > max_radius_squared && norm2(r) > prev) return std::nullopt;
     double e = E;
     V3 from = pos[which];
+    last_abs = 0.0;
     for (size_t k = 0; k < pos.size(); ++k) {
       if (k == which) continue;
-      e += lj_potential(norm2(sub(pos[k], r))) - lj_potential(norm2(sub(pos[k], from)));
+      double vn = lj_potential(norm2(sub(pos[k], r))), vo = lj_potential(norm2(sub(pos[k], from)));
+      e += vn - vo;
+      last_abs += std::fabs(vn) + std::fabs(vo);
     }
     have_change = true;
     ch_which = which;
@@ -291,6 +296,7 @@ inline double wca_potential_pressure(double r2) {  // wca.rs:79-92
 
 struct Wca {
   double E = 0, error = 0;
+  double last_abs = 0;
   Cell cell;
   bool have_change = false;
   size_t ch_which = 0;
@@ -357,6 +363,7 @@ struct Wca {
     ch_to = r;
     ch_e = e;
     ch_dabse = dabse;
+    last_abs = dabse;
     return e;
   }
   std::optional<double> plan_move(const Draws& d, double scale) {  // wca.rs:342-353
@@ -401,6 +408,7 @@ inline uint64_t max_balls_within(double distance) {  // optsquare.rs:290-322
 
 struct SquareWell {
   double E = 0;
+  double last_abs = 0;
   Cell cell;
   bool have_change = false;
   size_t ch_which = 0;

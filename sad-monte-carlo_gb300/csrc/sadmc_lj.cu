@@ -174,7 +174,11 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
         bool ok = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, fh.c.E, s.radius2, tx, ty, tz, e2);
         if (ok && finite64(e2)) {
           if (e2 < fh.c.E) { lj.put((int)d.which, tx, ty, tz); fh.c.E = e2; }
-          if (fh.c.E < m.descent_max) done = true;
+          if (fh.c.E < m.descent_max) {
+            // binary32 increments from overlapping starts drift; decide on the FP64 sum
+            fh.c.E = lj.energy64();
+            if (fh.c.E < m.descent_max) done = true;
+          }
         }
         if (steps >= m.descent_limit) done = true;
       }

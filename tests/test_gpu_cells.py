@@ -56,11 +56,12 @@ def test_square_well_rejects_small_boxes(gpu):
 
 
 def wca_config(n, rho, seed):
-    """Jittered simple-cubic start, no close contacts."""
+    """Random subset of a jittered simple-cubic lattice filling the box."""
     L = (n / rho) ** (1 / 3)
     m = int(np.ceil(n ** (1 / 3)))
     rng = np.random.default_rng(seed)
-    g = np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)][:n], float)
+    g = np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)
+    g = g[rng.permutation(len(g))[:n]]
     pos = (g + 0.5 + rng.uniform(-0.05, 0.05, g.shape)) * (L / m)
     return np.mod(pos, L), (L, L, L)
 
@@ -68,11 +69,11 @@ def wca_config(n, rho, seed):
 @pytest.mark.parametrize("lpw", [8, 32])
 def test_wca_uneven_trace_replay(gpu, oracle, lpw):
     specs = [(64, 0.6), (64, 0.9), (128, 0.7), (128, 0.8), (96, 0.75), (64, 0.85)]
-    moves, seed, w_bin = 8000, 4, 0.05
+    moves, seed, w_bin = 8000, 4, 0.5
     confs = [wca_config(n, rho, 10 + k) for k, (n, rho) in enumerate(specs)]
     W = len(specs)
     cfg = gpu.make_config(gpu.WCA, W, max(n for n, _ in specs), method=1, t0=500.0,
-                          energy_bin=w_bin, e_lo=-2 * w_bin, e_hi=400.0, max_allowed=380.0,
+                          energy_bin=w_bin, e_lo=-2 * w_bin, e_hi=4000.0,
                           translation_scale=0.1, seed=seed, lanes_per_walker=lpw,
                           resum_interval=1000)
     b = gpu.Batch(cfg, [(n, 0.0, box) for (n, _), (_, box) in zip(specs, confs)])
@@ -84,7 +85,7 @@ def test_wca_uneven_trace_replay(gpu, oracle, lpw):
     for w, ((n, rho), (pos, box)) in enumerate(zip(specs, confs)):
         e1, e2 = b.trace(w, moves)
         ow = oracle.Walker(oracle.make_config(oracle.WCA, n, box=box, method=1, t0=500.0,
-                                              energy_bin=w_bin, max_allowed=380.0,
+                                              energy_bin=w_bin,
                                               translation_scale=0.1, seed=seed, walker=w,
                                               e0=float(E0[w])), pos)
         disc, mismatch = ow.run_override(e1, e2)

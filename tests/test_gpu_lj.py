@@ -14,7 +14,8 @@ pytestmark = pytest.mark.gpu
 
 # Binary32 pair terms on positions rounded to binary32 carry ~1e-6 relative error each.
 # Injected proposals: |e2_gpu - e2_fp64| <= DE_ABS + DE_REL * |e2 - E|.  Trace replay: the
-# oracle reports max |e2_gpu - e2_fp64| / (1 + |e1| + |e2|), bounded by REPLAY_REL.
+# oracle reports max |e2_gpu - e2_fp64| / (1e-3 + sum of |pair terms| of the proposal),
+# bounded by REPLAY_REL.
 DE_ABS, DE_REL = 2e-4, 2e-5
 REPLAY_REL = 2e-5
 
