@@ -308,6 +308,7 @@ def run_gpu(args):
 
 
 def main():
+    global WALKERS, MOVES_PER_STEP
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -320,7 +321,6 @@ def main():
     ap.add_argument("--moves", type=int, default=MOVES_PER_STEP, help="moves per walker per step")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
-    global WALKERS, MOVES_PER_STEP
     WALKERS, MOVES_PER_STEP = args.walkers, args.moves
     if args.impl == "reference":
         run_reference(args)

@@ -82,7 +82,7 @@ typedef struct sadmc_config {
   uint64_t descent_limit;    /* initial descent proposals per walker (energy.rs:841: 1e8) */
   int32_t lanes_per_walker;  /* lanes cooperating on one walker; 0 = autotuned default */
   int32_t resum_interval;    /* moves between FP64 energy re-sums (LJ, WCA); 0 = 2048 */
-  double drift_tol;          /* SADMC_ST_DRIFT threshold on |E - E_fp64| (0 = 1e-6*N) */
+  double drift_tol;          /* SADMC_ST_DRIFT threshold on |E - E_fp64| (0 = 1e-2) */
 } sadmc_config;
 
 /* Per-walker geometry (walkers of one handle may differ in N and box). */

@@ -106,7 +106,7 @@ struct sadmc_handle {
   }
   int resum() const { return cfg.resum_interval > 0 ? cfg.resum_interval : 2048; }
   double drift_tol() const {
-    return cfg.drift_tol > 0 ? cfg.drift_tol : 1e-6 * (double)std::max(1, cfg.max_atoms);
+    return cfg.drift_tol > 0 ? cfg.drift_tol : 1e-2;
   }
   int32_t pull_cores() {
     h_cores.resize(W);
