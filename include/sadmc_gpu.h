@@ -177,6 +177,16 @@ int32_t sadmc_read_trace(sadmc_handle* h, int32_t walker, double* e1, double* e2
 int32_t sadmc_lanes_per_walker(sadmc_handle* h);
 int32_t sadmc_autotune(sadmc_handle* h, uint64_t moves, int32_t* best_lpw, double* best_ms);
 
+/* Checkpoint / resume of the whole batch (MonteCarlo::checkpoint, src/mc/mod.rs:111-121;
+ * resume by re-entry, mc/mod.rs:55-108).  The file holds the configuration, geometry,
+ * every walker's flat-histogram state, bin planes and system state; it is written to a
+ * temporary name and renamed, so a crash never leaves a partial file (atomicfile.rs:20-76).
+ * Runs continue bit for bit: the random stream is indexed by the move counter. */
+int32_t sadmc_checkpoint(sadmc_handle* h, const char* path);
+int32_t sadmc_resume(const char* path, sadmc_handle** out);
+/* The configuration and per-walker geometry of a handle (geom: n_walkers entries). */
+int32_t sadmc_get_config(sadmc_handle* h, sadmc_config* cfg, sadmc_geometry* geom);
+
 /* The counter-based draws the kernels consume for moves t0 .. t0+count-1 of one walker
  * (Philox4x32-10 keyed by (walker, seed); stream_pair 0 moves, 1 descent): idx2 gets
  * (atom or i, j) pairs, g3 the three normals, u the Metropolis uniform.  Host arrays.

@@ -730,6 +730,109 @@ int32_t sadmc_autotune(sadmc_handle* h, uint64_t moves, int32_t* best_lpw, doubl
   return SADMC_OK;
 }
 
+namespace {
+
+struct DevBuf {
+  void* ptr;
+  size_t bytes;
+};
+
+std::vector<DevBuf> state_buffers(sadmc_handle* h) {
+  const size_t W = h->W, nb = h->nb, np = h->np;
+  std::vector<DevBuf> v = {{h->d_cores, sizeof(WalkerCore) * W}, {h->plane_mem, W * nb * 8 * 8}};
+  switch (h->cfg.system) {
+    case SADMC_ISING: v.push_back({h->d_spins, W * (size_t)h->L * h->L}); break;
+    case SADMC_LJ: v.push_back({h->d_pos, W * 6 * np * sizeof(float)}); break;
+    default:
+      v.push_back({h->d_pos64, W * 3 * np * sizeof(double)});
+      v.push_back({h->d_pos32, W * 4 * np * sizeof(float)});
+      v.push_back({h->d_ncell, W * 3 * sizeof(int)});
+      v.push_back({h->d_cell_of, W * np * sizeof(int)});
+      v.push_back({h->d_cnt, W * (size_t)h->cell_cap * sizeof(int)});
+      v.push_back({h->d_atoms, W * (size_t)h->cell_cap * h->bucket * sizeof(int)});
+      break;
+  }
+  return v;
+}
+
+const char kMagic[8] = {'S', 'A', 'D', 'M', 'C', 'G', 'B', '1'};
+
+}  // namespace
+
+int32_t sadmc_checkpoint(sadmc_handle* h, const char* path) {
+  if (!h || !path) return fail(SADMC_ERR_INVALID, "null argument");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return fail(SADMC_ERR_INVALID, "cannot open " + tmp);
+  bool ok = std::fwrite(kMagic, 1, 8, f) == 8;
+  const int32_t W = h->W;
+  ok = ok && std::fwrite(&h->cfg, sizeof(h->cfg), 1, f) == 1;
+  ok = ok && std::fwrite(&W, sizeof(W), 1, f) == 1;
+  ok = ok && std::fwrite(h->geom.data(), sizeof(sadmc_geometry), W, f) == (size_t)W;
+  ok = ok && std::fwrite(&h->moves_done, sizeof(h->moves_done), 1, f) == 1;
+  ok = ok && std::fwrite(&h->lpw, sizeof(h->lpw), 1, f) == 1;
+  std::vector<char> host;
+  for (const DevBuf& b : state_buffers(h)) {
+    host.resize(b.bytes);
+    if (ok && cudaMemcpy(host.data(), b.ptr, b.bytes, cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
+    const uint64_t n = b.bytes;
+    ok = ok && std::fwrite(&n, sizeof(n), 1, f) == 1 && std::fwrite(host.data(), 1, b.bytes, f) == b.bytes;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok || std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    return fail(SADMC_ERR_INVALID, std::string("checkpoint write failed: ") + path);
+  }
+  return SADMC_OK;
+}
+
+int32_t sadmc_resume(const char* path, sadmc_handle** out) {
+  if (!path || !out) return fail(SADMC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(SADMC_ERR_INVALID, std::string("cannot open ") + path);
+  char magic[8];
+  sadmc_config cfg;
+  int32_t W = 0;
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kMagic, 8) == 0 &&
+            std::fread(&cfg, sizeof(cfg), 1, f) == 1 && std::fread(&W, sizeof(W), 1, f) == 1 &&
+            W == cfg.n_walkers && W > 0;
+  std::vector<sadmc_geometry> geom(ok ? W : 0);
+  uint64_t moves_done = 0;
+  int32_t lpw = 0;
+  ok = ok && std::fread(geom.data(), sizeof(sadmc_geometry), W, f) == (size_t)W &&
+       std::fread(&moves_done, sizeof(moves_done), 1, f) == 1 && std::fread(&lpw, sizeof(lpw), 1, f) == 1;
+  if (!ok) { std::fclose(f); return fail(SADMC_ERR_INVALID, "not a sadmc checkpoint"); }
+  cfg.lanes_per_walker = lpw;
+  sadmc_handle* h = nullptr;
+  int32_t r = sadmc_create(&cfg, geom.data(), &h);
+  if (r) { std::fclose(f); return r; }
+  std::vector<char> host;
+  for (const DevBuf& b : state_buffers(h)) {
+    uint64_t n = 0;
+    if (std::fread(&n, sizeof(n), 1, f) != 1 || n != b.bytes) { ok = false; break; }
+    host.resize(b.bytes);
+    if (std::fread(host.data(), 1, b.bytes, f) != b.bytes ||
+        cudaMemcpy(b.ptr, host.data(), b.bytes, cudaMemcpyHostToDevice) != cudaSuccess) { ok = false; break; }
+  }
+  std::fclose(f);
+  if (!ok) { sadmc_destroy(h); return fail(SADMC_ERR_INVALID, "truncated or mismatched checkpoint"); }
+  h->uploaded = h->initialized = true;
+  h->moves_done = moves_done;
+  h->h_cores.clear();
+  *out = h;
+  return SADMC_OK;
+}
+
+int32_t sadmc_get_config(sadmc_handle* h, sadmc_config* cfg, sadmc_geometry* geom) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (cfg) *cfg = h->cfg;
+  if (geom) std::memcpy(geom, h->geom.data(), sizeof(sadmc_geometry) * h->W);
+  return SADMC_OK;
+}
+
 int32_t sadmc_draws(int32_t system, uint32_t n, uint64_t seed, uint32_t walker, uint64_t t0,
                     int32_t count, uint32_t stream_pair, uint32_t* idx2, float* g3, double* u) {
   if (!idx2 || !g3 || !u || count <= 0 || n == 0) return fail(SADMC_ERR_INVALID, "bad argument");

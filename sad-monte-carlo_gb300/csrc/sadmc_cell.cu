@@ -155,12 +155,14 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
   const float wsqr32 = (float)wsqr;
   RecentScale rsb;
   rsb.init();
+  DrawCache<LPW, false> dc;
+  dc.init();
   for (uint64_t it = 0; it < m.n_moves; ++it) {
     const uint64_t t = fh.c.moves + 1;
     double rs, omrs;
     rsb.get(t, lane, rs, omrs);
     fh.begin_move(omrs);
-    const Draws d = draws_continuous(m.seed, (uint32_t)w, t, (uint32_t)n, 0u);
+    const Draws d = dc.get(m.seed, (uint32_t)w, t, (uint32_t)n, gmask, glane);
     const int a = (int)d.which;
     const double sc = fh.c.tscale;
     const double fx = cw.p[a], fy = cw.p[s.np + a], fz = cw.p[2 * s.np + a];

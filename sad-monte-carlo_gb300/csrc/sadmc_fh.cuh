@@ -69,6 +69,8 @@ struct Fh {
   int i2;
   uint64_t hist2;
   bool grew_front;
+  bool tscale_changed;  // set when the SAD discovery adapted translation_scale
+  bool inverted;        // too_lo > too_hi (never true for SAD; kept exact)
 
   // ---- index helpers ---------------------------------------------------------------
   __device__ int gidx_exact(double e) const { return (int)((e - c.cur_min) / width) + c.b_lo; }
@@ -138,8 +140,10 @@ struct Fh {
     } else {
       cur = -1;
     }
+    inverted = c.too_lo > c.too_hi;
     gb_valid = false;
     grew_front = false;
+    tscale_changed = false;
   }
   __device__ void store(WalkerCore* cores, int w) {
     if (c.kind != M_DESCENT) flush_cur();
@@ -204,9 +208,17 @@ struct Fh {
     if (c.kind == M_SAD) { win_lo = gidx_exact(c.too_lo); win_hi = gidx_exact(c.too_hi); }
   }
 
+  // e < too_lo and e > too_hi from the bin index g of e: the index is monotone in e, so
+  // only e in the window's edge bin needs the FP64 comparison.
+  __device__ bool below(double e, int g) const {
+    return g < win_lo ? true : (g > win_lo ? false : e < c.too_lo);
+  }
+  __device__ bool above(double e, int g) const {
+    return g > win_hi ? true : (g < win_hi ? false : e > c.too_hi);
+  }
   __device__ double sad_lnw(double e, int g) const {  // energy.rs:451-464
-    if (e < c.too_lo) return ld_lnw(win_lo) + (e - c.too_lo) / c.min_T;
-    if (e > c.too_hi) return ld_lnw(win_hi);
+    if (below(e, g)) return ld_lnw(win_lo) + (e - c.too_lo) / c.min_T;
+    if (above(e, g)) return ld_lnw(win_hi);
     return ld_lnw(g);
   }
 
@@ -241,7 +253,8 @@ struct Fh {
         double lnw1 = sad_lnw(c.E, cur);
         double lnw2 = sad_lnw(e2, i2);
         rejected = lnw2 > lnw1 && metropolis_reject(lnw1 - lnw2, u53);
-        if (!rejected && hist2 == 0 && e2 < c.too_hi && e2 > c.too_lo) {  // energy.rs:466-483
+        if (!rejected && hist2 == 0 && !below(e2, i2) && !above(e2, i2) && e2 < c.too_hi &&
+            e2 > c.too_lo) {  // energy.rs:466-483
           c.latest_param = (c.too_hi - c.too_lo) / c.min_T;
           c.num_states += 1;
           c.tL = c.moves;
@@ -310,10 +323,11 @@ struct Fh {
   }
 
   __device__ void sad_update(double energy, double old_lnw) {  // energy.rs:523-636
-    if (c.too_lo > c.too_hi || energy < c.too_lo || energy > c.too_hi) k_lnw = old_lnw;
+    const bool e_below = below(energy, cur), e_above = above(energy, cur);
+    if (inverted || e_below || e_above) k_lnw = old_lnw;
     if (k_hist > c.highest_hist) {
       c.highest_hist = k_hist;
-      if (energy > c.too_hi) {
+      if (e_above) {
         const double base = ld_lnw(win_hi);
         const int jlo = win_hi > c.b_lo ? win_hi : c.b_lo;
         const int jhi = cur < c.b_hi ? cur : c.b_hi;
@@ -327,6 +341,7 @@ struct Fh {
         c.latest_param = (energy - c.too_lo) / c.min_T;
         c.tL = c.moves;
         c.too_hi = center(cur);
+        inverted = c.too_lo > c.too_hi;
         const int nhi = gidx_exact(c.too_hi);
         for (int j = win_hi + 1; j <= nhi; ++j) {
           uint64_t t = ld_tf(j);
@@ -334,7 +349,7 @@ struct Fh {
         }
         win_hi = nhi;
         gb_valid = false;
-      } else if (energy < c.too_lo) {
+      } else if (e_below) {
         const double base = ld_lnw(win_lo);
         const int jlo = cur > c.b_lo ? cur : c.b_lo;
         const int jhi = win_lo < c.b_hi ? win_lo : c.b_hi;
@@ -354,6 +369,7 @@ struct Fh {
         c.latest_param = (c.too_hi - energy) / c.min_T;
         c.tL = c.moves;
         c.too_lo = center(cur);
+        inverted = c.too_lo > c.too_hi;
         const int nlo = gidx_exact(c.too_lo);
         for (int j = nlo; j < win_lo; ++j) {
           uint64_t t = ld_tf(j);
@@ -371,6 +387,7 @@ struct Fh {
         double s = c.acc_rate / target_rate;
         s = s < 0.8 ? 0.8 : (s > 1.2 ? 1.2 : s);
         c.tscale *= s;
+        tscale_changed = true;
       }
     }
   }

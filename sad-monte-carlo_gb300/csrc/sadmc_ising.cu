@@ -31,12 +31,14 @@ __global__ void __launch_bounds__(128) ising_move_kernel(MoveLaunch m, IsingSys 
   int8_t* S = s.spins + (size_t)w * (size_t)L * (size_t)L;
   RecentScale rsb;
   rsb.init();
+  DrawCache<LPW, true> dc;
+  dc.init();
   for (uint64_t it = 0; it < m.n_moves; ++it) {
     const uint64_t t = fh.c.moves + 1;
     double rs, omrs;
     rsb.get(t, lane, rs, omrs);
     fh.begin_move(omrs);
-    Draws d = draws_ising(m.seed, (uint32_t)w, t, (uint32_t)L);
+    const Draws d = dc.get(m.seed, (uint32_t)w, t, (uint32_t)L, gmask, glane);
     const int i = (int)d.which, j = (int)d.j;
     int jp = j + 1 == L ? 0 : j + 1, jm = j == 0 ? L - 1 : j - 1;
     int ip = i + 1 == L ? 0 : i + 1, im = i == 0 ? L - 1 : i - 1;

@@ -196,14 +196,15 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
 
   RecentScale rsb;
   rsb.init();
+  DrawCache<LPW, false> dc;
+  dc.init();
   DS sc = ds_from_double(fh.c.tscale);
-  double tscale_seen = fh.c.tscale;
   for (uint64_t it = 0; it < m.n_moves; ++it) {
     const uint64_t t = fh.c.moves + 1;
     double rs, omrs;
     rsb.get(t, lane, rs, omrs);
     fh.begin_move(omrs);
-    Draws d = draws_continuous(m.seed, (uint32_t)w, t, (uint32_t)lj.n, 0u);
+    const Draws d = dc.get(m.seed, (uint32_t)w, t, (uint32_t)lj.n, gmask, glane);
     DS tx, ty, tz;
     double e2 = 0.0;
     bool possible = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, fh.c.E, s.radius2, tx, ty, tz, e2);
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
       fh.c.E = e2;
     }
     fh.finish_move(acc);
-    if (fh.c.tscale != tscale_seen) { tscale_seen = fh.c.tscale; sc = ds_from_double(tscale_seen); }
+    if (fh.tscale_changed) { fh.tscale_changed = false; sc = ds_from_double(fh.c.tscale); }
     if (m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
       const double e64 = lj.energy64();
       const double dr = fabs(e64 - fh.c.E);

@@ -134,5 +134,32 @@ __device__ __forceinline__ Draws draws_ising(uint64_t seed, uint32_t walker, uin
   return d;
 }
 
+// Lane glane of a walker's group holds the draws of move base + glane; a move reads its
+// draws with six group shuffles, so Philox and Box-Muller run once per LPW moves.
+template <int LPW, bool ISING>
+struct DrawCache {
+  uint64_t base;
+  Draws mine;
+  __device__ void init() { base = ~0ull; }
+  __device__ Draws get(uint64_t seed, uint32_t walker, uint64_t t, uint32_t n, unsigned gmask,
+                       int glane) {
+    if (base == ~0ull || t < base || t - base >= (uint64_t)LPW) {
+      base = t;
+      mine = ISING ? draws_ising(seed, walker, t + (uint64_t)glane, n)
+                   : draws_continuous(seed, walker, t + (uint64_t)glane, n, 0u);
+    }
+    if (LPW == 1) return mine;
+    const int src = (int)(t - base);
+    Draws d;
+    d.which = __shfl_sync(gmask, mine.which, src, LPW);
+    d.j = ISING ? __shfl_sync(gmask, mine.j, src, LPW) : 0u;
+    d.g0 = ISING ? 0.0f : __shfl_sync(gmask, mine.g0, src, LPW);
+    d.g1 = ISING ? 0.0f : __shfl_sync(gmask, mine.g1, src, LPW);
+    d.g2 = ISING ? 0.0f : __shfl_sync(gmask, mine.g2, src, LPW);
+    d.u53 = __shfl_sync(gmask, mine.u53, src, LPW);
+    return d;
+  }
+};
+
 }  // namespace dev
 }  // namespace sadmc

@@ -97,6 +97,9 @@ def lib():
         "sadmc_set_trace": (I32, [P, U64]), "sadmc_read_trace": (I32, [P, I32, P, P, P]),
         "sadmc_lanes_per_walker": (I32, [P]), "sadmc_autotune": (I32, [P, U64, P, P]),
         "sadmc_heat_capacity": (I32, [P, I32, P, P, I32, P]),
+        "sadmc_checkpoint": (I32, [P, ctypes.c_char_p]),
+        "sadmc_resume": (I32, [ctypes.c_char_p, P]),
+        "sadmc_get_config": (I32, [P, P, P]),
         "sadmc_draws": (I32, [I32, ctypes.c_uint32, U64, ctypes.c_uint32, U64, I32, ctypes.c_uint32,
                               P, P, P]),
     }
@@ -289,6 +292,23 @@ class Batch:
         cnt = ctypes.c_uint64(0)
         _check(lib().sadmc_read_trace(self.h, w, _p(e1), _p(e2), ctypes.byref(cnt)))
         return e1[:cnt.value], e2[:cnt.value]
+
+    def checkpoint(self, path):
+        """Atomic binary checkpoint of the whole batch (write to path.tmp, rename)."""
+        _check(lib().sadmc_checkpoint(self.h, os.fsencode(path)))
+
+    @classmethod
+    def resume(cls, path):
+        """A batch restored from a checkpoint; its runs continue bit for bit."""
+        b = cls.__new__(cls)
+        b.h = ctypes.c_void_p()
+        _check(lib().sadmc_resume(os.fsencode(path), ctypes.byref(b.h)))
+        b.cfg = Config()
+        _check(lib().sadmc_get_config(b.h, ctypes.byref(b.cfg), None))
+        b._geom = (Geometry * b.cfg.n_walkers)()
+        _check(lib().sadmc_get_config(b.h, None, b._geom))
+        b.n = np.array([g.n for g in b._geom])
+        return b
 
     def lanes_per_walker(self):
         return lib().sadmc_lanes_per_walker(self.h)
