@@ -4,6 +4,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <sstream>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -90,6 +94,12 @@ struct sadmc_handle {
   int pend_walker = -1;
   sadmc_proposal pend{};
   std::vector<WalkerCore> h_cores;
+  int wpb = 4;                                  // warps per block
+  std::map<uint64_t, cudaGraphExec_t> graphs;   // captured run(moves) sequences
+  void drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
 
   FhParams fh_params() const {
     FhParams P{};
@@ -162,9 +172,83 @@ struct sadmc_handle {
     m.trace_t0 = trace_t0;
     m.resum_interval = resum();
     m.drift_tol = drift_tol();
+    m.warps_per_block = wpb;
     return m;
   }
 };
+
+namespace {
+
+struct DevBuf {
+  void* ptr;
+  size_t bytes;
+};
+
+std::vector<DevBuf> state_buffers(sadmc_handle* h) {
+  const size_t W = h->W, nb = h->nb, np = h->np;
+  std::vector<DevBuf> v = {{h->d_cores, sizeof(WalkerCore) * W}, {h->plane_mem, W * nb * 8 * 8}};
+  switch (h->cfg.system) {
+    case SADMC_ISING: v.push_back({h->d_spins, W * (size_t)h->L * h->L}); break;
+    case SADMC_LJ: v.push_back({h->d_pos, W * 6 * np * sizeof(float)}); break;
+    default:
+      v.push_back({h->d_pos64, W * 3 * np * sizeof(double)});
+      v.push_back({h->d_pos32, W * 4 * np * sizeof(float)});
+      v.push_back({h->d_ncell, W * 3 * sizeof(int)});
+      v.push_back({h->d_cell_of, W * np * sizeof(int)});
+      v.push_back({h->d_cnt, W * (size_t)h->cell_cap * sizeof(int)});
+      v.push_back({h->d_atoms, W * (size_t)h->cell_cap * h->bucket * sizeof(int)});
+      break;
+  }
+  return v;
+}
+
+const char kMagic[8] = {'S', 'A', 'D', 'M', 'C', 'G', 'B', '1'};
+
+}  // namespace
+
+namespace {
+
+const uint64_t kChunk = 8192;  // moves per launch (keeps each launch to tens of ms)
+
+cudaError_t launch_chunks(sadmc_handle* h, uint64_t moves, cudaStream_t st) {
+  MoveLaunch m = h->base_launch();
+  cudaStream_t keep = h->stream;
+  h->stream = st;
+  cudaError_t e = cudaSuccess;
+  for (uint64_t left = moves; left > 0 && e == cudaSuccess;) {
+    m.n_moves = std::min(left, kChunk);
+    e = h->launch_move(m);
+    left -= m.n_moves;
+  }
+  h->stream = keep;
+  return e;
+}
+
+std::string tune_cache_path() {
+  if (const char* p = std::getenv("SADMC_TUNE_CACHE")) return p;
+  const char* home = std::getenv("HOME");
+  return std::string(home ? home : "/tmp") + "/.cache/sadmc_gb300_tune.txt";
+}
+
+std::string tune_key(const sadmc_handle* h) {
+  std::ostringstream k;
+  k << "sys" << h->cfg.system << "_np" << (h->cfg.system == SADMC_ISING ? h->L : h->np) << "_W"
+    << h->W << "_m" << h->cfg.method;
+  return k.str();
+}
+
+std::vector<int> lpw_candidates(const sadmc_handle* h) {
+  switch (h->cfg.system) {
+    case SADMC_ISING: return {1, 32};
+    case SADMC_LJ:
+      if (h->np == 32) return {4, 8, 16, 32};
+      if (h->np == 64) return {8, 16, 32};
+      return {32};
+    default: return {4, 8, 16, 32};
+  }
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -235,6 +319,22 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
     h->lpw = c.lanes_per_walker ? c.lanes_per_walker : (h->np <= 64 ? 8 : 32);
     if (!valid_lpw_lj(h->lpw, h->np)) { delete h; return fail(SADMC_ERR_INVALID, "unsupported lanes_per_walker"); }
   }
+  if (c.lanes_per_walker == 0) {  // a recorded autotuning result for this shape wins
+    std::ifstream in(tune_cache_path());
+    const std::string key = tune_key(h);
+    for (std::string line; std::getline(in, line);) {
+      std::istringstream ls(line);
+      std::string k;
+      int lpw = 0, wpb = 0;
+      if (ls >> k >> lpw >> wpb && k == key) {
+        const auto cand = lpw_candidates(h);
+        if (std::find(cand.begin(), cand.end(), lpw) != cand.end() && wpb >= 1 && wpb <= 4) {
+          h->lpw = lpw;
+          h->wpb = wpb;
+        }
+      }
+    }
+  }
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete h; return fail(SADMC_ERR_CUDA, cudaGetErrorString(e)); }
   const size_t plane = (size_t)h->W * (size_t)h->nb;
@@ -279,6 +379,7 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
 int32_t sadmc_destroy(sadmc_handle* h) {
   if (!h) return SADMC_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  h->drop_graphs();
   cudaFree(h->d_cores);
   cudaFree(h->d_tmp);
   cudaFree(h->plane_mem);
@@ -478,22 +579,37 @@ int32_t sadmc_initialize(sadmc_handle* h) {
   return SADMC_OK;
 }
 
+// The chunk launches of run(moves) are captured once per distinct `moves` into a CUDA
+// graph and replayed (the kernels read all walker state from device memory, so a replay
+// continues the chain); tracing runs launch directly.
 int32_t sadmc_run_async(sadmc_handle* h, uint64_t moves, void* stream) {
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
   if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  if (moves == 0) return SADMC_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
-  cudaStream_t keep = h->stream;
-  h->stream = st;
-  MoveLaunch m = h->base_launch();
-  const uint64_t chunk = 8192;
-  uint64_t left = moves;
-  while (left > 0) {
-    m.n_moves = std::min(left, chunk);
-    cudaError_t e = h->launch_move(m);
-    if (e != cudaSuccess) { h->stream = keep; return fail(SADMC_ERR_CUDA, cudaGetErrorString(e)); }
-    left -= m.n_moves;
+  if (h->d_trace || std::getenv("SADMC_NO_GRAPHS")) {
+    CUDA_TRY(launch_chunks(h, moves, st));
+  } else {
+    auto it = h->graphs.find(moves);
+    if (it == h->graphs.end()) {
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = launch_chunks(h, moves, st);
+      cudaError_t e2 = cudaStreamEndCapture(st, &g);
+      if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(SADMC_ERR_CUDA, std::string("graph capture: ") +
+                                        cudaGetErrorString(e != cudaSuccess ? e : e2));
+      }
+      e = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess)
+        return fail(SADMC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+      it = h->graphs.emplace(moves, ge).first;
+    }
+    CUDA_TRY(cudaGraphLaunch(it->second, st));
   }
-  h->stream = keep;
   h->moves_done += moves;
   return SADMC_OK;
 }
@@ -689,6 +805,7 @@ int32_t sadmc_status(sadmc_handle* h, uint32_t* flags) {
 
 int32_t sadmc_set_trace(sadmc_handle* h, uint64_t capacity) {
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  h->drop_graphs();
   cudaFree(h->d_trace);
   h->d_trace = nullptr;
   h->trace_cap = 0;
@@ -722,42 +839,85 @@ int32_t sadmc_read_trace(sadmc_handle* h, int32_t walker, double* e1, double* e2
 
 int32_t sadmc_lanes_per_walker(sadmc_handle* h) { return h ? h->lpw : 0; }
 
+// Autotuner: each (lanes per walker, warps per block) candidate runs `moves` moves on a
+// snapshot of the batch, timed with CUDA events; the snapshot is restored after every
+// candidate, the fastest is kept and recorded in the tuning cache
+// ($SADMC_TUNE_CACHE or ~/.cache/sadmc_gb300_tune.txt, one "key lpw wpb ms" per line).
 int32_t sadmc_autotune(sadmc_handle* h, uint64_t moves, int32_t* best_lpw, double* best_ms) {
-  (void)moves;
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
-  if (best_lpw) *best_lpw = h->lpw;
-  if (best_ms) *best_ms = 0.0;
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  if (moves == 0) moves = 1024;
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const auto bufs = state_buffers(h);
+  std::vector<void*> snap(bufs.size(), nullptr);
+  for (size_t i = 0; i < bufs.size(); ++i) {
+    if (cudaMalloc(&snap[i], bufs[i].bytes) != cudaSuccess) {
+      for (void* p : snap) cudaFree(p);
+      return fail(SADMC_ERR_NOMEM, "autotune snapshot allocation failed");
+    }
+    CUDA_TRY(cudaMemcpyAsync(snap[i], bufs[i].ptr, bufs[i].bytes, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  auto restore = [&]() -> cudaError_t {
+    for (size_t i = 0; i < bufs.size(); ++i) {
+      cudaError_t e = cudaMemcpyAsync(bufs[i].ptr, snap[i], bufs[i].bytes, cudaMemcpyDeviceToDevice, h->stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaStreamSynchronize(h->stream);
+  };
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int keep_lpw = h->lpw, keep_wpb = h->wpb;
+  int bl = keep_lpw, bw = keep_wpb;
+  float bms = 1e30f;
+  cudaError_t err = cudaSuccess;
+  for (int lpw : lpw_candidates(h)) {
+    for (int wpb : {1, 2, 4}) {
+      h->lpw = lpw;
+      h->wpb = wpb;
+      err = launch_chunks(h, std::min<uint64_t>(moves, 256), h->stream);  // warm-up
+      if (err == cudaSuccess) err = restore();
+      if (err == cudaSuccess) err = cudaEventRecord(e0, h->stream);
+      if (err == cudaSuccess) err = launch_chunks(h, moves, h->stream);
+      if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+      if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+      float ms = 0;
+      if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+      if (err == cudaSuccess) err = restore();
+      if (err != cudaSuccess) break;
+      if (ms < bms) { bms = ms; bl = lpw; bw = wpb; }
+    }
+    if (err != cudaSuccess) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (void* p : snap) cudaFree(p);
+  if (err != cudaSuccess) {
+    h->lpw = keep_lpw;
+    h->wpb = keep_wpb;
+    return fail(SADMC_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(err));
+  }
+  h->lpw = bl;
+  h->wpb = bw;
+  h->drop_graphs();
+  // record (best effort; an unwritable cache directory just skips it)
+  const std::string path = tune_cache_path(), key = tune_key(h);
+  std::vector<std::string> lines;
+  {
+    std::ifstream in(path);
+    for (std::string line; std::getline(in, line);)
+      if (line.rfind(key + " ", 0) != 0) lines.push_back(line);
+  }
+  std::ostringstream rec;
+  rec << key << " " << bl << " " << bw << " " << bms;
+  lines.push_back(rec.str());
+  std::ofstream out(path);
+  for (const auto& l : lines) out << l << "\n";
+  if (best_lpw) *best_lpw = bl;
+  if (best_ms) *best_ms = bms;
   return SADMC_OK;
 }
 
-namespace {
-
-struct DevBuf {
-  void* ptr;
-  size_t bytes;
-};
-
-std::vector<DevBuf> state_buffers(sadmc_handle* h) {
-  const size_t W = h->W, nb = h->nb, np = h->np;
-  std::vector<DevBuf> v = {{h->d_cores, sizeof(WalkerCore) * W}, {h->plane_mem, W * nb * 8 * 8}};
-  switch (h->cfg.system) {
-    case SADMC_ISING: v.push_back({h->d_spins, W * (size_t)h->L * h->L}); break;
-    case SADMC_LJ: v.push_back({h->d_pos, W * 6 * np * sizeof(float)}); break;
-    default:
-      v.push_back({h->d_pos64, W * 3 * np * sizeof(double)});
-      v.push_back({h->d_pos32, W * 4 * np * sizeof(float)});
-      v.push_back({h->d_ncell, W * 3 * sizeof(int)});
-      v.push_back({h->d_cell_of, W * np * sizeof(int)});
-      v.push_back({h->d_cnt, W * (size_t)h->cell_cap * sizeof(int)});
-      v.push_back({h->d_atoms, W * (size_t)h->cell_cap * h->bucket * sizeof(int)});
-      break;
-  }
-  return v;
-}
-
-const char kMagic[8] = {'S', 'A', 'D', 'M', 'C', 'G', 'B', '1'};
-
-}  // namespace
 
 int32_t sadmc_checkpoint(sadmc_handle* h, const char* path) {
   if (!h || !path) return fail(SADMC_ERR_INVALID, "null argument");

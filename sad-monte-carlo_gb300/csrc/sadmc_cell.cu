@@ -386,7 +386,8 @@ __global__ void cell_energy_kernel(const WalkerCore* cores, CellSys s, int n_wal
 #define SADMC_CELL_CASE(L, K)                                                           \
   if (lpw == L && s.kind == K) {                                                        \
     const int warps = (m.n_walkers + (32 / L) - 1) / (32 / L);                          \
-    dev::cell_move_kernel<L, K><<<(warps * 32 + 127) / 128, 128, 0, st>>>(m, s);        \
+    const int wpb = m.warps_per_block >= 1 && m.warps_per_block <= 4 ? m.warps_per_block : 4; \
+    dev::cell_move_kernel<L, K><<<(warps + wpb - 1) / wpb, 32 * wpb, 0, st>>>(m, s);   \
     return cudaGetLastError();                                                          \
   }
 

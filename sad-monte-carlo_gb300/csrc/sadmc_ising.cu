@@ -86,9 +86,10 @@ __global__ void ising_energy_kernel(IsingSys s, int n_walkers, double* out) {
 cudaError_t launch_ising_move(const MoveLaunch& m, const IsingSys& s, int lpw, cudaStream_t st) {
   const int wpw = 32 / lpw;
   const int warps = (m.n_walkers + wpw - 1) / wpw;
-  const int blocks = (warps * 32 + 127) / 128;
-  if (lpw == 1) dev::ising_move_kernel<1><<<blocks, 128, 0, st>>>(m, s);
-  else if (lpw == 32) dev::ising_move_kernel<32><<<blocks, 128, 0, st>>>(m, s);
+  const int wpb = m.warps_per_block >= 1 && m.warps_per_block <= 4 ? m.warps_per_block : 4;
+  const int blocks = (warps + wpb - 1) / wpb;
+  if (lpw == 1) dev::ising_move_kernel<1><<<blocks, 32 * wpb, 0, st>>>(m, s);
+  else if (lpw == 32) dev::ising_move_kernel<32><<<blocks, 32 * wpb, 0, st>>>(m, s);
   else return cudaErrorInvalidConfiguration;
   return cudaGetLastError();
 }

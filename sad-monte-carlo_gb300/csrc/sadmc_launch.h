@@ -23,6 +23,7 @@ struct MoveLaunch {
   int descent;             // 1: run the initial descent (energy.rs:840-851) instead
   uint64_t descent_limit;  // maximum descent proposals per walker
   double descent_max;      // max_allowed_energy the descent aims below
+  int warps_per_block;     // 1, 2 or 4 (kernels are bounded to 128 threads)
 };
 
 // LJ cluster in a spherical wall.  pos: [walker][6][np] binary32 planes

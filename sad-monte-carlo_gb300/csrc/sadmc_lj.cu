@@ -281,9 +281,9 @@ __global__ void lj_plan_kernel(WalkerCore* cores, LjSys s, int w, int which, flo
 
 #define SADMC_LJ_CASE(L, A)                                                            \
   if (lpw == L && s.np == L * A) {                                                     \
-    const int wpb = 128 / 32;                                                          \
+    const int wpb = m.warps_per_block >= 1 && m.warps_per_block <= 4 ? m.warps_per_block : 4; \
     const int warps = (m.n_walkers + (32 / L) - 1) / (32 / L);                         \
-    dev::lj_move_kernel<L, A><<<(warps + wpb - 1) / wpb, 128, 0, st>>>(m, s);          \
+    dev::lj_move_kernel<L, A><<<(warps + wpb - 1) / wpb, 32 * wpb, 0, st>>>(m, s);     \
     return cudaGetLastError();                                                         \
   }
 

@@ -73,7 +73,7 @@ def test_wca_uneven_trace_replay(gpu, oracle, lpw):
     confs = [wca_config(n, rho, 10 + k) for k, (n, rho) in enumerate(specs)]
     W = len(specs)
     cfg = gpu.make_config(gpu.WCA, W, max(n for n, _ in specs), method=1, t0=500.0,
-                          energy_bin=w_bin, e_lo=-2 * w_bin, e_hi=4000.0,
+                          energy_bin=w_bin, e_lo=-2 * w_bin, e_hi=2100.0, max_allowed=2000.0,
                           translation_scale=0.1, seed=seed, lanes_per_walker=lpw,
                           resum_interval=1000)
     b = gpu.Batch(cfg, [(n, 0.0, box) for (n, _), (_, box) in zip(specs, confs)])
@@ -85,7 +85,7 @@ def test_wca_uneven_trace_replay(gpu, oracle, lpw):
     for w, ((n, rho), (pos, box)) in enumerate(zip(specs, confs)):
         e1, e2 = b.trace(w, moves)
         ow = oracle.Walker(oracle.make_config(oracle.WCA, n, box=box, method=1, t0=500.0,
-                                              energy_bin=w_bin,
+                                              energy_bin=w_bin, max_allowed=2000.0,
                                               translation_scale=0.1, seed=seed, walker=w,
                                               e0=float(E0[w])), pos)
         disc, mismatch = ow.run_override(e1, e2)
