@@ -397,8 +397,8 @@ struct EnergyMC {
       double e2 = *e2o;
       if (e2_override) {
         double ge2 = e2_override[moves - 1 - override_base];
-        // |e2_gpu - e2| relative to the sum of |pair terms| of the proposal (binary32
-        // terms carry ~1e-6 relative error each)
+        // |e2_gpu - e2| relative to the gross magnitude of the proposal's pair terms
+        // (sum of 4 s^6 + 4 s^3), the scale of binary32 rounding in 4 (s^6 - s^3)
         if (ge2 != ge2) ++override_mismatch;  // GPU said impossible, oracle possible
         else max_e2_discrepancy = std::max(max_e2_discrepancy,
                                            std::fabs(ge2 - e2) / (1e-3 + sys.last_abs));

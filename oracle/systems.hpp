@@ -80,11 +80,18 @@ inline double lj_potential(double r2) {  // lj.rs:78-81
   return 4.0 * (powi6(s) - powi3(s));
 }
 
+// 4 s^6 + 4 s^3: the magnitude of the two parts of a pair term that cancel in
+// 4 (s^6 - s^3) near r = sigma, which sets the scale of a binary32 evaluation's error.
+inline double lj_gross(double r2) {
+  double s = 1.0 / r2;
+  return 4.0 * (powi6(s) + powi3(s));
+}
+
 struct Lj {
   double E = 0, error = 0;
   std::vector<V3> pos;
   double max_radius_squared = 0;
-  double last_abs = 0;  // sum of |pair terms| of the last plan (scale of binary32 error)
+  double last_abs = 0;  // sum of lj_gross over the pair terms of the last plan
   bool have_change = false;
   size_t ch_which = 0;
   V3 ch_to{};
@@ -107,9 +114,9 @@ struct Lj {
     last_abs = 0.0;
     for (size_t k = 0; k < pos.size(); ++k) {
       if (k == which) continue;
-      double vn = lj_potential(norm2(sub(pos[k], r))), vo = lj_potential(norm2(sub(pos[k], from)));
-      e += vn - vo;
-      last_abs += std::fabs(vn) + std::fabs(vo);
+      const double rn = norm2(sub(pos[k], r)), ro = norm2(sub(pos[k], from));
+      e += lj_potential(rn) - lj_potential(ro);
+      last_abs += lj_gross(rn) + lj_gross(ro);
     }
     have_change = true;
     ch_which = which;
@@ -346,24 +353,30 @@ struct Wca {
   std::optional<double> move_atom(size_t which, const V3& r) {  // wca.rs:119-140
     double e = E, dabse = 0.0;
     V3 from = cell.pos[which];
+    double gross = 0.0;
+    const double rc2 = wca_r_cutoff() * wca_r_cutoff();
     cell.for_each_candidate(r, which, [&](const V3& r1) {
-      double de = wca_potential(norm2(sub(r1, r)));
+      const double r2 = norm2(sub(r1, r));
+      double de = wca_potential(r2);
       e += de;
       dabse += de;
+      if (r2 < rc2) gross += lj_gross(r2) + 1.0;
       return true;
     });
     cell.for_each_candidate(from, which, [&](const V3& r1) {
-      double de = wca_potential(norm2(sub(r1, from)));
+      const double r2 = norm2(sub(r1, from));
+      double de = wca_potential(r2);
       e -= de;
       dabse += de;
+      if (r2 < rc2) gross += lj_gross(r2) + 1.0;
       return true;
     });
+    last_abs = gross;
     have_change = true;
     ch_which = which;
     ch_to = r;
     ch_e = e;
     ch_dabse = dabse;
-    last_abs = dabse;
     return e;
   }
   std::optional<double> plan_move(const Draws& d, double scale) {  // wca.rs:342-353

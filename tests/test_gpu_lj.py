@@ -12,10 +12,11 @@ from helpers import assert_bins_equal, assert_scalars_equal, lj_configs
 
 pytestmark = pytest.mark.gpu
 
-# Binary32 pair terms on positions rounded to binary32 carry ~1e-6 relative error each.
-# Injected proposals: |e2_gpu - e2_fp64| <= DE_ABS + DE_REL * |e2 - E|.  Trace replay: the
-# oracle reports max |e2_gpu - e2_fp64| / (1e-3 + sum of |pair terms| of the proposal),
-# bounded by REPLAY_REL.
+# Binary32 pair terms on positions rounded to binary32: 4 (s^6 - s^3) cancels near
+# r = sigma, so the rounding error scales with the gross magnitude 4 s^6 + 4 s^3 of each
+# term.  Injected proposals: |e2_gpu - e2_fp64| <= DE_ABS + DE_REL * |e2 - E|.  Trace
+# replay: the oracle reports max |e2_gpu - e2_fp64| / (1e-3 + sum of 4 s^6 + 4 s^3 over
+# the proposal's pair terms), bounded by REPLAY_REL.
 DE_ABS, DE_REL = 2e-4, 2e-5
 REPLAY_REL = 2e-5
 

@@ -76,7 +76,6 @@ def test_bin_range_is_flagged_not_faulted(gpu):
     would grow its vectors)."""
     L, W = 8, 4
     cfg = gpu.make_config(gpu.ISING, W, L, e_lo=-16, e_hi=16, seed=1)  # far narrower than [-128, 128]
-    spins = [np.ones(L * L) * (1 if w % 2 else -1) for w in range(W)]
     spins = [ising_spins(L, 5 + w) for w in range(W)]
     b = gpu.Batch(cfg, [(L, 0.0, (0, 0, 0))] * W)
     b.upload(spins)
@@ -86,5 +85,6 @@ def test_bin_range_is_flagged_not_faulted(gpu):
     assert (st & gpu.ST_BIN_RANGE).any()
     assert not (st & ~np.uint32(gpu.ST_BIN_RANGE)).any()
     E = b.energies()
-    assert np.all(E >= -16) and np.all(E <= 16)
+    # the planes hold the configured range plus two guard bins on each side
+    assert np.all(E >= -16 - 2 * 4) and np.all(E <= 16 + 2 * 4)
     np.testing.assert_array_equal(E, b.compute_energies())
