@@ -13,7 +13,9 @@
 //  * the SAD refill loops (energy.rs:542-583) visit only bins whose centre can meet the
 //    loop condition, each still tested with the reference's FP64 expression;
 //  * have_visited_since_maxentropy fills (energy.rs:950-965) are O(1) generation stamps;
-//  * gamma (SAD, SAMC) is evaluated for LPW consecutive moves at once, one per lane.
+//  * gamma (SAD, SAMC) is evaluated for 4*LPW consecutive moves at once;
+//  * the proposed bin's fields are fetched in one memory round trip and adopted when the
+//    move is accepted; the current bin lives in registers.
 #pragma once
 #include <cstdint>
 
@@ -57,11 +59,14 @@ struct Fh {
   // cached current bin (global index cur)
   int cur;
   double k_lnw, k_sE, k_sE2;
-  uint64_t k_hist, k_tf;
+  uint64_t k_hist, k_tf, k_stamp;
+  // the proposed bin's fields, fetched together in decide() (one memory round trip)
+  double p_lnw, p_sE, p_sE2;
+  uint64_t p_hist, p_tf, p_stamp;
   double cur_max;      // upper edge of the allocated range
   int win_lo, win_hi;  // SAD window as bin indices
-  // gamma batch: lane glane holds gamma(gb_base + glane)
-  double gb_val;
+  // gamma batch (see gamma())
+  double gb_val[4];
   uint64_t gb_base;
   bool gb_valid;
   // per-move scratch
@@ -103,7 +108,21 @@ struct Fh {
   __device__ void load_cur(int g) {
     g = g < 0 ? 0 : (g >= nbins ? nbins - 1 : g);
     cur = g;
-    k_lnw = lnw[g]; k_hist = hist[g]; k_tf = tf[g]; k_sE = sE[g]; k_sE2 = sE2[g];
+    k_lnw = lnw[g]; k_hist = hist[g]; k_tf = tf[g]; k_sE = sE[g]; k_sE2 = sE2[g]; k_stamp = stamp[g];
+  }
+  __device__ void fetch_pending(int g) {
+    if (g == cur) {
+      p_lnw = k_lnw; p_hist = k_hist; p_tf = k_tf; p_sE = k_sE; p_sE2 = k_sE2; p_stamp = k_stamp;
+    } else {
+      p_lnw = lnw[g]; p_hist = hist[g]; p_tf = tf[g]; p_sE = sE[g]; p_sE2 = sE2[g]; p_stamp = stamp[g];
+    }
+  }
+  // adopt the prefetched fields of bin g (== i2) as the current bin
+  __device__ void adopt_pending(int g) {
+    if (g == cur) return;
+    flush_cur();
+    cur = g;
+    k_lnw = p_lnw; k_hist = p_hist; k_tf = p_tf; k_sE = p_sE; k_sE2 = p_sE2; k_stamp = p_stamp;
   }
   __device__ void move_cur(int g) {
     if (g != cur) { flush_cur(); load_cur(g); }
@@ -168,19 +187,25 @@ struct Fh {
       default: return 0.0;
     }
   }
+  // gamma(gb_base + glane + LPW*q) sits in gb_val[q]; four independent divide chains per
+  // lane hide the FP64 divide latency and cover 4*LPW moves per evaluation.
   __device__ double gamma() {
     if (c.kind != M_SAD && c.kind != M_SAMC) return gamma_at(c.moves);
-    if (!gb_valid || c.moves < gb_base || c.moves - gb_base >= (uint64_t)LPW) {
+    if (!gb_valid || c.moves < gb_base || c.moves - gb_base >= (uint64_t)(4 * LPW)) {
       gb_base = c.moves;
-      gb_val = gamma_at(c.moves + (uint64_t)glane);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) gb_val[q] = gamma_at(c.moves + (uint64_t)(glane + LPW * q));
       gb_valid = true;
     }
-    if (LPW == 1) return gb_val;
-    return __shfl_sync(gmask, gb_val, (int)(c.moves - gb_base), LPW);
+    const int off = (int)(c.moves - gb_base);
+    const int q = off / LPW;
+    double v = q == 0 ? gb_val[0] : q == 1 ? gb_val[1] : q == 2 ? gb_val[2] : gb_val[3];
+    if (LPW == 1) return v;
+    return __shfl_sync(gmask, v, off % LPW, LPW);
   }
 
   // ---- have_visited_since_maxentropy as generation stamps ------------------------------
-  __device__ bool visited(int g) const { return stamp[g] == c.fill_gen ? true : (c.fill_val != 0); }
+  __device__ bool visited_cur() const { return k_stamp == c.fill_gen ? true : (c.fill_val != 0); }
   __device__ void fill_visited(bool v) { c.fill_gen += 1; c.fill_val = v ? 1 : 0; }
 
   // ---- prepare_for_state (energy.rs:400-434); false: outside the preallocated planes ---
@@ -189,6 +214,7 @@ struct Fh {
       if (c.b_lo == 0) return false;
       c.b_lo -= 1;
       if (wr) stamp[c.b_lo] = c.fill_gen;  // inserted as visited, round_trips already 1
+      if (c.b_lo == cur) k_stamp = c.fill_gen;
       c.cur_min -= width;
       grew_front = true;
     }
@@ -197,6 +223,7 @@ struct Fh {
       if (c.b_hi >= nbins - 1) return false;
       c.b_hi += 1;
       if (wr) stamp[c.b_hi] = c.fill_gen;
+      if (c.b_hi == cur) k_stamp = c.fill_gen;
       cur_max = c.cur_min + width * (double)(c.b_hi - c.b_lo + 1);
     }
     return true;
@@ -245,8 +272,9 @@ struct Fh {
       c.status |= ST_BIN_RANGE;
       return false;
     }
-    double lnw2_raw = ld_lnw(i2);
-    hist2 = ld_hist(i2);
+    fetch_pending(i2);
+    const double lnw2_raw = p_lnw;
+    hist2 = p_hist;
     bool rejected;
     switch (c.kind) {
       case M_SAD: {
@@ -289,7 +317,7 @@ struct Fh {
   __device__ void finish_move(bool accepted) {
     if (c.kind == M_DESCENT) return;
     int old_cur = cur;
-    if (accepted) move_cur(i2);
+    if (accepted) adopt_pending(i2);
     const double E = c.E;
     if (k_hist == 0) {  // energy.rs:938-940
       k_tf = c.moves;
@@ -307,7 +335,8 @@ struct Fh {
     } else if (li == c.max_S_local) {
       int i1 = grew_front ? gidx_exact(e1) : old_cur;
       if (i1 - c.b_lo != li) fill_visited(false);
-    } else if (!visited(cur)) {
+    } else if (!visited_cur()) {
+      k_stamp = c.fill_gen;
       if (wr) { stamp[cur] = c.fill_gen; rt[cur] = rt[cur] + 1; }
     }
   }

@@ -75,7 +75,7 @@ def test_wca_uneven_trace_replay(gpu, oracle, lpw):
     cfg = gpu.make_config(gpu.WCA, W, max(n for n, _ in specs), method=1, t0=500.0,
                           energy_bin=w_bin, e_lo=-2 * w_bin, e_hi=2100.0, max_allowed=2000.0,
                           translation_scale=0.1, seed=seed, lanes_per_walker=lpw,
-                          resum_interval=1000)
+                          resum_interval=1500)  # no re-sum on the last move
     b = gpu.Batch(cfg, [(n, 0.0, box) for (n, _), (_, box) in zip(specs, confs)])
     b.upload([p for p, _ in confs])
     b.initialize()

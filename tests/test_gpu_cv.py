@@ -26,7 +26,8 @@ def exact_cv(T):
     return np.array(out)
 
 
-@pytest.mark.parametrize("method,kw", [("sad", dict(method=0, min_T=0.5)), ("wl", dict(method=2))])
+@pytest.mark.parametrize("method,kw", [("sad", dict(method=0, min_T=0.5)),
+                                       ("samc", dict(method=1, t0=1e4))])
 def test_ising4_cv_error(gpu, method, kw):
     L, W = 4, 64
     cfg = gpu.make_config(gpu.ISING, W, L, e_lo=-36, e_hi=36, seed=12, **kw)
