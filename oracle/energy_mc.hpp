@@ -102,6 +102,7 @@ struct EnergyMC {
   double max_e2_discrepancy = 0.0;
   uint64_t override_base = 0;
   uint64_t override_mismatch = 0;
+  double worst[4] = {0, 0, 0, 0};  // move, e2 given, e2 own, gross magnitude at the worst move
 
   // EnergyMC::from_params, energy.rs:830-898 (descent loop at 840-851 uses the
   // descent stream with scale 0.05; at most `descent_limit` proposals).
@@ -400,8 +401,13 @@ struct EnergyMC {
         // |e2_gpu - e2| relative to the gross magnitude of the proposal's pair terms
         // (sum of 4 s^6 + 4 s^3), the scale of binary32 rounding in 4 (s^6 - s^3)
         if (ge2 != ge2) ++override_mismatch;  // GPU said impossible, oracle possible
-        else max_e2_discrepancy = std::max(max_e2_discrepancy,
-                                           std::fabs(ge2 - e2) / (1e-3 + sys.last_abs));
+        else {
+          const double dd = std::fabs(ge2 - e2) / (1e-3 + sys.last_abs);
+          if (dd > max_e2_discrepancy) {
+            max_e2_discrepancy = dd;
+            worst[0] = (double)moves; worst[1] = ge2; worst[2] = e2; worst[3] = sys.last_abs;
+          }
+        }
         e2 = ge2;
       }
       bool oob = false;

@@ -62,6 +62,7 @@ def lib():
             "orc_run": (None, [P, U64]),
             "orc_run_override": (D, [P, U64, P, P, P]),
             "orc_energy": (D, [P]), "orc_compute_energy": (D, [P]),
+            "orc_override_worst": (None, [P, P]),
             "orc_verify_energy": (ctypes.c_int, [P]),
             "orc_get_state": (None, [P, P]),
             "orc_plan_move": (ctypes.c_int, [P, U32, U32, D, D, D, D, P]),
@@ -147,6 +148,12 @@ class Walker:
         mm = ctypes.c_uint64(0)
         d = lib().orc_run_override(self.h, len(e2), _p(e1), _p(e2), ctypes.byref(mm))
         return d, mm.value
+
+    def override_worst(self):
+        """(move, e2 given, e2 own, gross pair-term magnitude) of the largest replay gap."""
+        o = np.zeros(4)
+        lib().orc_override_worst(self.h, _p(o))
+        return o
 
     def energy(self):
         return lib().orc_energy(self.h)

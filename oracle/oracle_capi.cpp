@@ -179,6 +179,10 @@ double orc_run_override(void* hv, uint64_t nmoves, const double* e1, const doubl
   });
 }
 
+void orc_override_worst(void* hv, double* out4) {
+  ((AnyMC*)hv)->visit([&](auto& mc) { for (int k = 0; k < 4; ++k) out4[k] = mc.worst[k]; return 0; });
+}
+
 double orc_energy(void* hv) { return ((AnyMC*)hv)->visit([](auto& mc) { return mc.sys.energy(); }); }
 double orc_compute_energy(void* hv) {
   return ((AnyMC*)hv)->visit([](auto& mc) { return mc.sys.compute_energy(); });

@@ -191,20 +191,20 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
     }
     const int new_c = cw.cell_index(nx, ny, nz);
     bool possible;
-    double e2;
+    float de;
     if (KIND == SYS_SW) {
       // e = E - (contacts at the new position) + (contacts at the old position); the
-      // FP64 sequence of unit steps of optsquare.rs:75-92 is exact on integers
+      // FP64 sequence of unit steps of optsquare.rs:75-92 is exact on integers, and so
+      // is the binary32 difference of the two counts
       const int newc = group_sum<LPW>(cn, gmask);
       const int oldc = group_sum<LPW>(co, gmask);
       possible = !__any_sync(gmask, overlap);
-      e2 = fh.c.E - (double)newc + (double)oldc;
+      de = (float)(oldc - newc);
     } else {
-      const float de = group_sum<LPW>(en - eo, gmask);
+      de = group_sum<LPW>(en - eo, gmask);
       possible = true;
-      e2 = fh.c.E + (double)de;
     }
-    possible = possible && !bad && finite64(e2);
+    possible = possible && !bad && fabsf(de) <= 3.0e38f;
     const int new_count = cw.cnt[new_c];
     if (possible && new_c != old_c && new_count >= cw.bucket) {
       possible = false;
@@ -213,10 +213,10 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
     if (m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
       TraceRec r;
       r.e1 = fh.c.E;
-      r.e2 = possible ? e2 : __longlong_as_double(0x7ff8000000000000ll);
+      r.e2 = possible ? fh.c.E + (double)de : __longlong_as_double(0x7ff8000000000000ll);
       m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = r;
     }
-    const bool acc = fh.decide(possible, e2, d.u53, rs);
+    const bool acc = fh.decide_de(possible, de, d.u53, rs);
     if (acc) {
       // ConfirmSystem::confirm -> Cell::move_atom (optcell.rs:162-175)
       if (new_c != old_c) {
@@ -243,7 +243,6 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
         cw.p32[a] = make_float4(t32x, t32y, t32z, 0.0f);
       }
       __syncwarp(gmask);
-      fh.c.E = e2;
     }
     fh.finish_move(acc);
     if (KIND == SYS_WCA && m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
@@ -275,7 +274,7 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
       const double dr = fabs(e64 - fh.c.E);
       if (dr > fh.c.drift) fh.c.drift = dr;
       if (dr > m.drift_tol) fh.c.status |= ST_DRIFT;
-      fh.c.E = e64;
+      fh.set_E(e64);
       fh.grew_front = false;
       if (!fh.prepare(e64)) fh.c.status |= ST_BIN_RANGE;
       else {

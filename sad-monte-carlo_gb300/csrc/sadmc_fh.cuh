@@ -31,15 +31,36 @@ __device__ __forceinline__ double u53_to_double(uint64_t v) {
 // rejected = (u > exp(d)) with u = u53 * 2^-53 and d <= 0 (energy.rs:465, 489, 498, 508).
 // Decided in FP32 when the FP32 estimate is outside its error margin; otherwise the
 // reference's FP64 comparison is evaluated.
+__device__ __forceinline__ float f32_trunc(double x);
 __device__ __forceinline__ bool metropolis_reject(double d, uint64_t u53) {
-  float df = (float)d;
+  float df = f32_trunc(d);
   if (df < -80.0f) return u53 != 0;  // exp(d) < 2e-35 < 2^-53: only u == 0 is accepted
   float e32 = __expf(df);
-  float m = 4.0e-6f + fabsf(df) * 3.0e-7f;
+  float m = 4.0e-6f + fabsf(df) * 4.0e-7f;
   float uf = (float)(u53 >> 29) * (1.0f / 16777216.0f);  // u in [uf, uf + 2^-24)
   if (uf > e32 * (1.0f + m)) return true;
   if (uf + (1.0f / 16777216.0f) < e32 * (1.0f - m)) return false;
   return u53_to_double(u53) > exp(d);
+}
+
+
+// binary32 value of a finite double by truncating its mantissa (relative error < 2^-23),
+// with integer instructions only; |x| < 2^-126 gives +-0, |x| >= 2^128 gives +-inf.
+__device__ __forceinline__ float f32_trunc(double x) {
+  const long long b = __double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+  if (e < -126) return __uint_as_float(sign);
+  if (e > 127) return __uint_as_float(sign | 0x7f800000u);
+  const unsigned m = (unsigned)((b >> 29) & 0x7fffffll);
+  return __uint_as_float(sign | ((unsigned)(e + 127) << 23) | m);
+}
+// x > y for doubles; non-negative values (sign bits clear) compare as their bit patterns.
+__device__ __forceinline__ bool dgt(double x, double y) {
+  const long long a = __double_as_longlong(x), b = __double_as_longlong(y);
+  if ((a | b) >= 0) return a > b;
+  return x > y;
 }
 
 template <int LPW>
@@ -75,6 +96,8 @@ struct Fh {
   uint64_t hist2;
   bool grew_front;
   bool tscale_changed;  // set when the SAD discovery adapted translation_scale
+  // binary32 copies for the FP32-first comparisons of decide_de (refreshed on change)
+  float Ef, cminf, cmaxf, maxf, minf, inv_wf;
   bool inverted;        // too_lo > too_hi (never true for SAD; kept exact)
 
   // ---- index helpers ---------------------------------------------------------------
@@ -226,6 +249,8 @@ struct Fh {
       if (c.b_hi == cur) k_stamp = c.fill_gen;
       cur_max = c.cur_min + width * (double)(c.b_hi - c.b_lo + 1);
     }
+    cminf = f32_trunc(c.cur_min);
+    cmaxf = f32_trunc(cur_max);
     return true;
   }
   // After the front grew the reference recomputes every local index with the new
@@ -247,6 +272,11 @@ struct Fh {
     if (below(e, g)) return ld_lnw(win_lo) + (e - c.too_lo) / c.min_T;
     if (above(e, g)) return ld_lnw(win_hi);
     return ld_lnw(g);
+  }
+
+  __device__ void set_E(double e) {
+    c.E = e;
+    Ef = f32_trunc(e);
   }
 
   // ---- one move ----------------------------------------------------------------------
@@ -312,6 +342,110 @@ struct Fh {
     return !rejected;
   }
 
+
+  // The decision of decide() for e2 = E + (double)de with de in binary32.  Each
+  // comparison of the reference on e2 is first taken on the binary32 estimate
+  // e2f = Ef + de, whose error is below tol (|E - Ef| < |E| 2^-23, one binary32 rounding,
+  // one binary64 rounding); inside the bound, or wherever the exact value enters
+  // arithmetic (SAD extrapolation, window edges, discoveries, the accepted energy), the
+  // FP64 e2 is formed and the reference's comparison is evaluated on it.
+  __device__ bool decide_de(bool possible, float de, uint64_t u53, double rs) {
+    if (!possible || !(fabsf(de) <= 3.0e38f)) return false;
+    const float e2f = Ef + de;
+    const float tol = (fabsf(Ef) + fabsf(e2f)) * 2.5e-7f + 1e-30f;
+    double e2 = 0.0;
+    bool have = false;
+    auto exact = [&]() -> double {
+      if (!have) { e2 = c.E + (double)de; have = true; }
+      return e2;
+    };
+    // e2 > T (T's binary32 copy Tf within |T| 2^-23)
+    auto gt = [&](float Tf, double T) -> bool {
+      const float m = tol + fabsf(Tf) * 2.5e-7f;
+      const float d = e2f - Tf;
+      if (d > m) return true;
+      if (d < -m) return false;
+      return exact() > T;
+    };
+    auto lt = [&](float Tf, double T) -> bool {
+      const float m = tol + fabsf(Tf) * 2.5e-7f;
+      const float d = e2f - Tf;
+      if (d < -m) return true;
+      if (d > m) return false;
+      return exact() < T;
+    };
+    // e2 > E (resp. e2 < E): the sign of de unless de is within rounding of E
+    const float tiny = fabsf(Ef) * 1e-15f + 1e-37f;
+    auto gtE = [&]() -> bool { return de > tiny ? true : (de <= 0.0f ? false : exact() > c.E); };
+    auto ltE = [&]() -> bool { return de < -tiny ? true : (de >= 0.0f ? false : exact() < c.E); };
+    bool oob = false;
+    if (has_max_allowed) oob = gt(maxf, max_allowed) && gtE();
+    if (has_min_allowed) oob = oob || (lt(minf, min_allowed) && ltE());
+    if (oob) return false;
+    if (c.kind == M_DESCENT) return ltE();
+    // prepare_for_state: only when e2 may lie outside [cur_min, cur_max)
+    if (lt(cminf, c.cur_min) || !lt(cmaxf, cur_max)) {
+      if (!prepare(exact())) { c.status |= ST_BIN_RANGE; return false; }
+      if (grew_front) reindex_after_growth();
+    }
+    // state_to_index
+    if (have) {
+      i2 = gidx(e2);
+    } else {
+      const float q = (e2f - cminf) * inv_wf;
+      const int qi = __float2int_rd(q);
+      const float fr = q - (float)qi;
+      const float m = (tol + fabsf(cminf) * 2.5e-7f) * inv_wf + fabsf(q) * 2.5e-7f + 1e-6f;
+      i2 = (fr > m && fr < 1.0f - m) ? qi + c.b_lo : gidx(exact());
+    }
+    if (i2 < c.b_lo || i2 > c.b_hi) {
+      c.status |= ST_BIN_RANGE;
+      return false;
+    }
+    fetch_pending(i2);
+    const double lnw2_raw = p_lnw;
+    hist2 = p_hist;
+    bool rejected;
+    switch (c.kind) {
+      case M_SAD: {
+        const double lnw1 = sad_lnw(c.E, cur);
+        if (i2 <= win_lo || i2 >= win_hi) exact();  // extrapolation / edge comparisons
+        const double lnw2 = sad_lnw(e2, i2);
+        rejected = dgt(lnw2, lnw1) && metropolis_reject(lnw1 - lnw2, u53);
+        if (!rejected && hist2 == 0) {  // energy.rs:466-483
+          exact();
+          if (e2 < c.too_hi && e2 > c.too_lo) {
+            c.latest_param = (c.too_hi - c.too_lo) / c.min_T;
+            c.num_states += 1;
+            c.tL = c.moves;
+            gb_valid = false;
+          }
+        }
+        break;
+      }
+      case M_SAMC: {
+        rejected = dgt(lnw2_raw, k_lnw) && metropolis_reject(k_lnw - lnw2_raw, u53);
+        break;
+      }
+      case M_WL:
+      case M_INV_T_WL: {
+        rejected = dgt(lnw2_raw, k_lnw) && metropolis_reject(k_lnw - lnw2_raw, u53);
+        if (!rejected && hist2 == 0 && c.lowest_hist > 0) c.wl_num_states += 1.0;
+        break;
+      }
+      default: {  // canonical (energy.rs:504-510)
+        rejected = gtE() ? metropolis_reject((c.E - exact()) / c.temperature, u53) : false;
+        break;
+      }
+    }
+    if (!rejected) {
+      c.accepted += 1;
+      c.acc_rate += rs;
+      set_E(exact());
+    }
+    return !rejected;
+  }
+
   // Histogram, energy sums, update_weights and max-entropy bookkeeping
   // (energy.rs:934-965).  Call after the system confirmed (c.E updated) or not.
   __device__ void finish_move(bool accepted) {
@@ -328,7 +462,7 @@ struct Fh {
     k_sE2 += E * E;
     update_weights(E);
     const int li = cur - c.b_lo;
-    if (k_lnw > c.max_S) {
+    if (dgt(k_lnw, c.max_S)) {
       c.max_S = k_lnw;
       c.max_S_local = li;
       fill_visited(true);

@@ -45,17 +45,16 @@ __global__ void __launch_bounds__(128) ising_move_kernel(MoveLaunch m, IsingSys 
     const int site = i + j * L;
     const int nt = S[i + jp * L] + S[i + jm * L] + S[ip + j * L] + S[im + j * L];
     const int sij = S[site];
-    const double e2 = fh.c.E - (double)(nt * sij * 2);
+    const float de = (float)(-(nt * sij * 2));  // exact: |de| <= 8
     if (m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
       TraceRec r;
       r.e1 = fh.c.E;
-      r.e2 = e2;
+      r.e2 = fh.c.E + (double)de;
       m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = r;
     }
-    const bool acc = fh.decide(true, e2, d.u53, rs);
+    const bool acc = fh.decide_de(true, de, d.u53, rs);
     if (acc) {
       if (wr) S[site] = (int8_t)(-sij);  // all lanes of the group store the same value
-      fh.c.E = e2;
       if (LPW > 1) __syncwarp(gmask);
     }
     fh.finish_move(acc);

@@ -72,9 +72,9 @@ struct LjWalker {
   }
 
   // plan_move of lj.rs:365-374 and move_atom of lj.rs:86-105 for a given displacement.
-  // Returns possible; e2 = E + dE (dE summed in binary32).
-  __device__ bool plan(int which, float g0, float g1, float g2, float sh, float sl, double E,
-                       double radius2, DS& tx, DS& ty, DS& tz, double& e2) const {
+  // Returns possible; de = the energy change summed in binary32 over the group.
+  __device__ bool plan(int which, float g0, float g1, float g2, float sh, float sl,
+                       double radius2, DS& tx, DS& ty, DS& tz, float& de_out) const {
     DS fx, fy, fz;
     fetch(which, fx, fy, fz);
     tx = ds_add(fx, ds_scale(g0, sh, sl));
@@ -108,8 +108,7 @@ struct LjWalker {
         de += vn - vo;
       }
     }
-    de = group_sum<LPW>(de, gmask);
-    e2 = E + (double)de;
+    de_out = group_sum<LPW>(de, gmask);
     return true;
   }
 
@@ -170,8 +169,9 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
         ++steps;
         Draws d = draws_continuous(m.seed, (uint32_t)w, steps, (uint32_t)lj.n, 1u);
         DS tx, ty, tz;
-        double e2;
-        bool ok = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, fh.c.E, s.radius2, tx, ty, tz, e2);
+        float de;
+        bool ok = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, s.radius2, tx, ty, tz, de);
+        const double e2 = fh.c.E + (double)de;
         if (ok && finite64(e2)) {
           if (e2 < fh.c.E) { lj.put((int)d.which, tx, ty, tz); fh.c.E = e2; }
           if (fh.c.E < m.descent_max) {
@@ -206,20 +206,16 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
     fh.begin_move(omrs);
     const Draws d = dc.get(m.seed, (uint32_t)w, t, (uint32_t)lj.n, gmask, glane);
     DS tx, ty, tz;
-    double e2 = 0.0;
-    bool possible = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, fh.c.E, s.radius2, tx, ty, tz, e2);
-    possible = possible && finite64(e2);
+    float de = 0.0f;
+    const bool possible = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, s.radius2, tx, ty, tz, de);
     if (m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
       TraceRec r;
       r.e1 = fh.c.E;
-      r.e2 = possible ? e2 : __longlong_as_double(0x7ff8000000000000ll);
+      r.e2 = possible ? fh.c.E + (double)de : __longlong_as_double(0x7ff8000000000000ll);
       m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = r;
     }
-    const bool acc = fh.decide(possible, e2, d.u53, rs);
-    if (acc) {
-      lj.put((int)d.which, tx, ty, tz);
-      fh.c.E = e2;
-    }
+    const bool acc = fh.decide_de(possible, de, d.u53, rs);
+    if (acc) lj.put((int)d.which, tx, ty, tz);
     fh.finish_move(acc);
     if (fh.tscale_changed) { fh.tscale_changed = false; sc = ds_from_double(fh.c.tscale); }
     if (m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
@@ -227,7 +223,7 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
       const double dr = fabs(e64 - fh.c.E);
       if (dr > fh.c.drift) fh.c.drift = dr;
       if (dr > m.drift_tol) fh.c.status |= ST_DRIFT;
-      fh.c.E = e64;
+      fh.set_E(e64);
       fh.grew_front = false;
       if (!fh.prepare(e64)) fh.c.status |= ST_BIN_RANGE;
       else {
@@ -266,9 +262,9 @@ __global__ void lj_plan_kernel(WalkerCore* cores, LjSys s, int w, int which, flo
   lj.load(pw, s.np);
   const DS sc = ds_from_double(scale);
   DS tx, ty, tz;
-  double e2 = 0.0;
-  const double E = cores[w].E;
-  bool ok = lj.plan(which, g0, g1, g2, sc.h, sc.l, E, s.radius2, tx, ty, tz, e2);
+  float de = 0.0f;
+  bool ok = lj.plan(which, g0, g1, g2, sc.h, sc.l, s.radius2, tx, ty, tz, de);
+  const double e2 = cores[w].E + (double)de;
   if (lane == 0) { out[0] = ok ? e2 : 0.0; out[1] = ok ? 1.0 : 0.0; }
   if (ok && confirm) {
     lj.put(which, tx, ty, tz);

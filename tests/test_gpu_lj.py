@@ -49,7 +49,7 @@ def test_lj_trace_replay(gpu, oracle, n, lpw):
                                               e0=float(E0[w])), confs[w])
         disc, mismatch = ow.run_override(e1, e2)
         assert mismatch == 0, f"walker {w}: possibility differs on {mismatch} moves"
-        assert disc < REPLAY_REL, f"walker {w}: max relative |de| {disc}"
+        assert disc < REPLAY_REL, f"walker {w}: max relative |de| {disc} at {ow.override_worst()}"
         label = f"n{n} lpw{lpw} walker {w}"
         assert_bins_equal(b.bins(w), ow.bins(), label=label)
         assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
