@@ -187,6 +187,36 @@ int32_t sadmc_resume(const char* path, sadmc_handle** out);
 /* The configuration and per-walker geometry of a handle (geom: n_walkers entries). */
 int32_t sadmc_get_config(sadmc_handle* h, sadmc_config* cfg, sadmc_geometry* geom);
 
+/* Learned surrogate for delayed-acceptance LJ moves (no counterpart in the reference):
+ * a 32-RBF descriptor per atom -> 64 -> 64 -> 1 SiLU MLP, bf16 tensor-core forward with
+ * FP32 accumulation, FP32 backward, Adam.  SADMC_SG_NPARAM FP32 parameters in the order
+ * W1[32][64], b1[64], W2[64][64], b2[64], w3[64], b3. */
+#define SADMC_SG_NPARAM 6337
+/* Allocate the surrogate of an LJ handle: random weights from `seed`, a ring buffer of
+ * `ring_capacity` training configurations. */
+int32_t sadmc_surrogate_init(sadmc_handle* h, uint64_t seed, int32_t ring_capacity);
+int32_t sadmc_surrogate_get_params(sadmc_handle* h, float* params);
+int32_t sadmc_surrogate_set_params(sadmc_handle* h, const float* params);
+/* Append every walker's current configuration and exact energy to the training ring. */
+int32_t sadmc_surrogate_collect(sadmc_handle* h, int32_t* ring_count);
+/* `steps` Adam steps on minibatches of `batch` ring configurations drawn with `seed`;
+ * *loss receives the last minibatch loss (mean squared configuration-energy error). */
+int32_t sadmc_surrogate_train(sadmc_handle* h, int32_t steps, int32_t batch, float lr,
+                              uint64_t seed, double* loss);
+/* Loss and gradients on caller configurations (positions [configs][N][3], host arrays),
+ * without updating the weights (for gradient checks). */
+int32_t sadmc_surrogate_loss_grads(sadmc_handle* h, const float* pos, const float* target,
+                                   int32_t configs, double* loss, float* grads);
+/* `moves` delayed-acceptance moves of every walker (SAD, SAMC or WL; LJ): the surrogate
+ * screens each proposal, the exact pair energy decides (Christen & Fox 2005).  Descriptors
+ * are rebuilt from scratch every refresh_interval moves (0: never).  stats (optional) gets
+ * per walker the running totals (stage-1 rejections, exact evaluations). */
+int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, uint64_t* stats);
+
+/* Surrogate energies of caller configurations (host arrays). */
+int32_t sadmc_surrogate_predict(sadmc_handle* h, const float* pos, int32_t configs,
+                                float* energies);
+
 /* The counter-based draws the kernels consume for moves t0 .. t0+count-1 of one walker
  * (Philox4x32-10 keyed by (walker, seed); stream_pair 0 moves, 1 descent): idx2 gets
  * (atom or i, j) pairs, g3 the three normals, u the Metropolis uniform.  Host arrays.

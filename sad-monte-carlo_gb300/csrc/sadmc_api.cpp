@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "sadmc_launch.h"
+#include "sadmc_surrogate.h"
 #include "sadmc_types.h"
 
 using namespace sadmc;
@@ -95,6 +96,52 @@ struct sadmc_handle {
   sadmc_proposal pend{};
   std::vector<WalkerCore> h_cores;
   int wpb = 4;                                  // warps per block
+  // learned surrogate (LJ)
+  float* sg_master = nullptr;                   // FP32 parameters
+  float* sg_grad = nullptr;
+  float* sg_m = nullptr;
+  float* sg_v = nullptr;
+  __nv_bfloat16* sg_w1t = nullptr;              // bf16 copies for the tensor cores
+  __nv_bfloat16* sg_w2t = nullptr;
+  float* sg_ring_pos = nullptr;                 // [cap][N][3] binary32
+  float* sg_ring_e = nullptr;
+  int sg_cap = 0, sg_head = 0, sg_count = 0, sg_step = 0;
+  void* sg_scratch = nullptr;                   // per-row activations of a training step
+  size_t sg_scratch_rows = 0;
+  float* sg_batch_pos = nullptr;                // gathered minibatch
+  float* sg_batch_e = nullptr;
+  int* sg_idx = nullptr;
+  int sg_batch_cap = 0;
+  double* sg_loss = nullptr;
+  uint64_t* sg_stats = nullptr;                 // [W][2] delayed-acceptance counters
+  SgWeights sg_weights() const { return SgWeights::from(sg_master, sg_w1t, sg_w2t); }
+  void free_surrogate() {
+    cudaFree(sg_master); cudaFree(sg_grad); cudaFree(sg_m); cudaFree(sg_v); cudaFree(sg_w1t);
+    cudaFree(sg_w2t); cudaFree(sg_ring_pos); cudaFree(sg_ring_e); cudaFree(sg_scratch);
+    cudaFree(sg_batch_pos); cudaFree(sg_batch_e); cudaFree(sg_idx); cudaFree(sg_loss); cudaFree(sg_stats);
+    sg_stats = nullptr;
+    sg_master = sg_grad = sg_m = sg_v = sg_ring_pos = sg_ring_e = sg_batch_pos = sg_batch_e = nullptr;
+    sg_w1t = sg_w2t = nullptr; sg_scratch = nullptr; sg_idx = nullptr; sg_loss = nullptr;
+  }
+  // scratch for `rows` rows and a gathered batch of `configs` configurations
+  cudaError_t sg_reserve(size_t rows, int configs) {
+    cudaError_t e = cudaSuccess;
+    if (rows > sg_scratch_rows) {
+      cudaFree(sg_scratch);
+      sg_scratch = nullptr;
+      e = cudaMalloc(&sg_scratch, SgScratch::bytes(rows));
+      sg_scratch_rows = e == cudaSuccess ? rows : 0;
+    }
+    if (e == cudaSuccess && configs > sg_batch_cap) {
+      cudaFree(sg_batch_pos); cudaFree(sg_batch_e); cudaFree(sg_idx);
+      sg_batch_pos = nullptr; sg_batch_e = nullptr; sg_idx = nullptr;
+      e = cudaMalloc(&sg_batch_pos, sizeof(float) * 3 * (size_t)configs * geom[0].n);
+      if (e == cudaSuccess) e = cudaMalloc(&sg_batch_e, sizeof(float) * configs);
+      if (e == cudaSuccess) e = cudaMalloc(&sg_idx, sizeof(int) * configs);
+      sg_batch_cap = e == cudaSuccess ? configs : 0;
+    }
+    return e;
+  }
   std::map<uint64_t, cudaGraphExec_t> graphs;   // captured run(moves) sequences
   void drop_graphs() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -380,6 +427,7 @@ int32_t sadmc_destroy(sadmc_handle* h) {
   if (!h) return SADMC_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->drop_graphs();
+  h->free_surrogate();
   cudaFree(h->d_cores);
   cudaFree(h->d_tmp);
   cudaFree(h->plane_mem);
@@ -990,6 +1038,177 @@ int32_t sadmc_get_config(sadmc_handle* h, sadmc_config* cfg, sadmc_geometry* geo
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
   if (cfg) *cfg = h->cfg;
   if (geom) std::memcpy(geom, h->geom.data(), sizeof(sadmc_geometry) * h->W);
+  return SADMC_OK;
+}
+
+
+int32_t sadmc_surrogate_init(sadmc_handle* h, uint64_t seed, int32_t ring_capacity) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (h->cfg.system != SADMC_LJ) return fail(SADMC_ERR_INVALID, "the surrogate is for LJ clusters");
+  for (int w = 1; w < h->W; ++w)
+    if (h->geom[w].n != h->geom[0].n) return fail(SADMC_ERR_INVALID, "surrogate needs walkers of equal N");
+  if (ring_capacity <= 0) return fail(SADMC_ERR_INVALID, "ring_capacity must be positive");
+  h->free_surrogate();
+  const int n = h->geom[0].n;
+  cudaError_t e = cudaMalloc(&h->sg_master, sizeof(float) * SG_NPARAM);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_grad, sizeof(float) * SG_NPARAM);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_m, sizeof(float) * SG_NPARAM);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_v, sizeof(float) * SG_NPARAM);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_w1t, sizeof(__nv_bfloat16) * SG_RBF * SG_H1);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_w2t, sizeof(__nv_bfloat16) * SG_H1 * SG_H2);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_ring_pos, sizeof(float) * 3 * (size_t)n * ring_capacity);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_ring_e, sizeof(float) * ring_capacity);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_loss, sizeof(double));
+  if (e != cudaSuccess) { h->free_surrogate(); return fail(SADMC_ERR_NOMEM, "surrogate allocation failed"); }
+  // N(0, 1/fan_in) weights, zero biases (a splitmix/Box-Muller host generator)
+  std::vector<float> p(SG_NPARAM, 0.0f);
+  uint64_t s = seed * 0x9E3779B97F4A7C15ull + 1;
+  auto next = [&]() {
+    s += 0x9E3779B97F4A7C15ull;
+    uint64_t z = s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  };
+  auto normal = [&]() { return std::sqrt(-2.0 * std::log(next())) * std::cos(6.283185307179586 * next()); };
+  for (int k = 0; k < SG_RBF * SG_H1; ++k) p[SG_OFF_W1 + k] = (float)(normal() / std::sqrt((double)SG_RBF));
+  for (int k = 0; k < SG_H1 * SG_H2; ++k) p[SG_OFF_W2 + k] = (float)(normal() / std::sqrt((double)SG_H1));
+  for (int k = 0; k < SG_H2; ++k) p[SG_OFF_W3 + k] = (float)(normal() / std::sqrt((double)SG_H2));
+  h->sg_cap = ring_capacity;
+  h->sg_head = h->sg_count = h->sg_step = 0;
+  return sadmc_surrogate_set_params(h, p.data());
+}
+
+int32_t sadmc_surrogate_set_params(sadmc_handle* h, const float* params) {
+  if (!h || !params) return fail(SADMC_ERR_INVALID, "null argument");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  CUDA_TRY(cudaMemcpy(h->sg_master, params, sizeof(float) * SG_NPARAM, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemset(h->sg_m, 0, sizeof(float) * SG_NPARAM));
+  CUDA_TRY(cudaMemset(h->sg_v, 0, sizeof(float) * SG_NPARAM));
+  h->sg_step = 0;
+  CUDA_TRY(sg_refresh(h->sg_master, h->sg_weights(), h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return SADMC_OK;
+}
+
+int32_t sadmc_surrogate_get_params(sadmc_handle* h, float* params) {
+  if (!h || !params) return fail(SADMC_ERR_INVALID, "null argument");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(cudaMemcpy(params, h->sg_master, sizeof(float) * SG_NPARAM, cudaMemcpyDeviceToHost));
+  return SADMC_OK;
+}
+
+int32_t sadmc_surrogate_collect(sadmc_handle* h, int32_t* ring_count) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  int32_t r = h->pull_cores();
+  if (r) return r;
+  std::vector<double> E(h->W);
+  for (int w = 0; w < h->W; ++w) E[w] = h->h_cores[w].E;
+  CUDA_TRY(cudaMemcpyAsync(h->d_tmp, E.data(), sizeof(double) * h->W, cudaMemcpyHostToDevice, h->stream));
+  const int take = std::min(h->W, h->sg_cap);
+  CUDA_TRY(sg_collect(h->d_pos, h->np, h->geom[0].n, h->d_tmp, take, h->sg_ring_pos, h->sg_ring_e,
+                      h->sg_cap, h->sg_head, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->sg_head = (h->sg_head + take) % h->sg_cap;
+  h->sg_count = std::min(h->sg_cap, h->sg_count + take);
+  if (ring_count) *ring_count = h->sg_count;
+  return SADMC_OK;
+}
+
+int32_t sadmc_surrogate_train(sadmc_handle* h, int32_t steps, int32_t batch, float lr,
+                              uint64_t seed, double* loss) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  if (h->sg_count == 0) return fail(SADMC_ERR_STATE, "the training ring is empty");
+  if (steps <= 0 || batch <= 0) return fail(SADMC_ERR_INVALID, "steps and batch must be positive");
+  const int n = h->geom[0].n;
+  CUDA_TRY(h->sg_reserve((size_t)batch * n, batch));
+  const SgScratch sc = SgScratch::carve(h->sg_scratch, (size_t)batch * n);
+  std::vector<int> idx(batch);
+  uint64_t s = seed ^ 0xD1B54A32D192ED03ull;
+  for (int it = 0; it < steps; ++it) {
+    for (int b = 0; b < batch; ++b) {
+      s = s * 6364136223846793005ull + 1442695040888963407ull;
+      idx[b] = (int)((s >> 33) % (uint64_t)h->sg_count);
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->sg_idx, idx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(sg_gather(h->sg_ring_pos, h->sg_ring_e, n, h->sg_idx, batch, h->sg_batch_pos, h->sg_batch_e, h->stream));
+    h->sg_step += 1;
+    CUDA_TRY(sg_train_step(h->sg_batch_pos, h->sg_batch_e, batch, n, h->sg_weights(), h->sg_master,
+                           h->sg_grad, h->sg_m, h->sg_v, h->sg_step, lr, sc, h->sg_loss, h->stream));
+  }
+  double l = 0;
+  CUDA_TRY(cudaMemcpyAsync(&l, h->sg_loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (loss) *loss = l;
+  return SADMC_OK;
+}
+
+int32_t sadmc_surrogate_loss_grads(sadmc_handle* h, const float* pos, const float* target,
+                                   int32_t configs, double* loss, float* grads) {
+  if (!h || !pos || !target || configs <= 0) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  const int n = h->geom[0].n;
+  CUDA_TRY(h->sg_reserve((size_t)configs * n, configs));
+  const SgScratch sc = SgScratch::carve(h->sg_scratch, (size_t)configs * n);
+  CUDA_TRY(cudaMemcpyAsync(h->sg_batch_pos, pos, sizeof(float) * 3 * (size_t)configs * n, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->sg_batch_e, target, sizeof(float) * configs, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(sg_train_step(h->sg_batch_pos, h->sg_batch_e, configs, n, h->sg_weights(), h->sg_master,
+                         h->sg_grad, h->sg_m, h->sg_v, 0, 0.0f, sc, h->sg_loss, h->stream));
+  double l = 0;
+  CUDA_TRY(cudaMemcpyAsync(&l, h->sg_loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (grads) CUDA_TRY(cudaMemcpyAsync(grads, h->sg_grad, sizeof(float) * SG_NPARAM, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (loss) *loss = l;
+  return SADMC_OK;
+}
+
+int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, uint64_t* stats) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  if (h->cfg.method == SADMC_CANONICAL) return fail(SADMC_ERR_INVALID, "delayed acceptance needs a flat-histogram method");
+  if (h->np > 64) return fail(SADMC_ERR_INVALID, "delayed acceptance supports up to 64 atoms");
+  if (!h->sg_stats) {
+    CUDA_TRY(cudaMalloc(&h->sg_stats, sizeof(uint64_t) * 2 * h->W));
+    CUDA_TRY(cudaMemset(h->sg_stats, 0, sizeof(uint64_t) * 2 * h->W));
+  }
+  MoveLaunch m = h->base_launch();
+  m.trace = nullptr;
+  for (uint64_t left = moves; left > 0;) {
+    m.n_moves = std::min<uint64_t>(left, 8192);
+    CUDA_TRY(launch_lj_da(m, LjSys{h->d_pos, h->np, h->radius2()}, h->sg_weights(), refresh_interval,
+                          h->sg_stats, h->stream));
+    left -= m.n_moves;
+  }
+  h->moves_done += moves;
+  if (stats) CUDA_TRY(cudaMemcpyAsync(stats, h->sg_stats, sizeof(uint64_t) * 2 * h->W, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return SADMC_OK;
+}
+
+int32_t sadmc_surrogate_predict(sadmc_handle* h, const float* pos, int32_t configs, float* energies) {
+  if (!h || !pos || !energies || configs <= 0) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  const int n = h->geom[0].n;
+  const size_t rows = (size_t)configs * n;
+  CUDA_TRY(h->sg_reserve(rows, configs));
+  const SgScratch sc = SgScratch::carve(h->sg_scratch, rows);
+  CUDA_TRY(cudaMemcpyAsync(h->sg_batch_pos, pos, sizeof(float) * 3 * rows, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(sg_descriptors(h->sg_batch_pos, n, (int)rows, sc.gq, nullptr, h->stream));
+  CUDA_TRY(sg_forward(sc.gq, (int)rows, h->sg_weights(), sc.e, nullptr, nullptr, h->stream));
+  std::vector<float> e(rows);
+  CUDA_TRY(cudaMemcpyAsync(e.data(), sc.e, sizeof(float) * rows, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  for (int c = 0; c < configs; ++c) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += e[(size_t)c * n + i];
+    energies[c] = (float)s;
+  }
   return SADMC_OK;
 }
 

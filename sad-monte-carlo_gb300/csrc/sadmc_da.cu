@@ -1,0 +1,233 @@
+// Delayed-acceptance moves for LJ clusters (Christen & Fox, "Markov chain Monte Carlo
+// using an approximation", J. Comput. Graph. Stat. 14, 2005), screened by the learned
+// surrogate of sadmc_surrogate.cu.  One walker per warp.
+//
+// Stage 1: the proposal of lj.rs:365-374 is screened with the surrogate energy
+//   E~ = E + sum_i [e_s(G'_i) - e_s(G_i)], accepted with min(1, exp(ln w(E) - ln w(E~))).
+//   The descriptors change incrementally: atom i != a gains phi(|r_i - to|) - phi(|r_i - from|),
+//   the moved atom's row is rebuilt from the new distances; the MLP runs on all rows on the
+//   tensor cores.
+// Stage 2: the exact binary32 pair energy e2 (as in lj_move_kernel) decides with
+//   min(1, exp(ln w(E~) - ln w(e2))) through the shared flat-histogram bookkeeping, so the
+//   exact energy makes every final decision and, for a fixed ln w, detailed balance holds.
+// A stage-1 rejection is a rejected move (it is histogrammed like any other).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "sadmc_common.cuh"
+#include "sadmc_fh.cuh"
+#include "sadmc_launch.h"
+#include "sadmc_lj_walker.cuh"
+#include "sadmc_mma.cuh"
+#include "sadmc_rng.cuh"
+#include "sadmc_surrogate.h"
+
+namespace sadmc {
+namespace dev {
+
+template <int APL>
+__global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeights wts,
+                                                    int refresh_interval, uint64_t* stats) {
+  constexpr int NR = 32 * APL;  // descriptor rows (atoms, padded)
+  __shared__ float sG[NR][SG_RBF];                  // current descriptors (FP32)
+  __shared__ float sGf[NR][SG_RBF];                 // proposed descriptors (FP32)
+  __shared__ __nv_bfloat16 sGb[NR][SG_RBF];         // proposed descriptors (bf16, MLP input)
+  __shared__ float sT[32][SG_RBF + 1];              // contributions to the moved atom's row
+  __shared__ float sE[NR], sEn[NR];                 // per-atom surrogate energies
+  __shared__ uint32_t sW1[SG_H1 * SG_RBF / 2], sW2[SG_H2 * SG_H1 / 2];
+  __shared__ float sb1[SG_H1], sb2[SG_H2], sw3[SG_H2];
+  const int lane = threadIdx.x;
+  for (int k = lane; k < SG_H1 * SG_RBF / 2; k += 32) sW1[k] = reinterpret_cast<const uint32_t*>(wts.w1t)[k];
+  for (int k = lane; k < SG_H2 * SG_H1 / 2; k += 32) sW2[k] = reinterpret_cast<const uint32_t*>(wts.w2t)[k];
+  for (int k = lane; k < SG_H1; k += 32) { sb1[k] = wts.b1[k]; sb2[k] = wts.b2[k]; sw3[k] = wts.w3[k]; }
+  const float b3 = wts.b3[0];
+  const int w = blockIdx.x;
+  if (w >= m.n_walkers) return;
+  __syncwarp();
+  Fh<32> fh;
+  fh.load(m.cores, m.P, m.B, w, 0xffffffffu, lane, true);
+  LjWalker<32, APL> lj;
+  lj.glane = lane;
+  lj.gmask = 0xffffffffu;
+  lj.n = fh.c.n;
+  const int n = lj.n;
+  float* pw = s.pos + (size_t)w * 6 * (size_t)s.np;
+  lj.load(pw, s.np);
+  const float inv2w2 = 1.0f / (2.0f * 0.1f * 0.1f);
+
+  // surrogate energies of all rows from sGb -> dst
+  auto forward_rows = [&](float* dst) {
+    for (int r0 = 0; r0 < n; r0 += 16) {
+      float ea, eb;
+      mlp16(reinterpret_cast<const uint32_t*>(&sGb[r0][0]), sW1, sW2, sb1, sb2, sw3, b3, ea, eb);
+      const int g = lane >> 2;
+      if ((lane & 3) == 0) {
+        if (r0 + g < NR) dst[r0 + g] = ea;
+        if (r0 + g + 8 < NR) dst[r0 + g + 8] = eb;
+      }
+    }
+    __syncwarp();
+  };
+  // full descriptors of the current configuration, their bf16 copy and energies
+  auto refresh = [&]() {
+    for (int q = 0; q < APL; ++q) {
+      float gacc[SG_RBF];
+#pragma unroll
+      for (int k = 0; k < SG_RBF; ++k) gacc[k] = 0.f;
+      const int i = lane + 32 * q;
+      const float xi = lj.x[q].h, yi = lj.y[q].h, zi = lj.z[q].h;
+      for (int j = 0; j < n; ++j) {
+        DS a, b, c;
+        lj.fetch(j, a, b, c);
+        if (i < n && j != i) {
+          const float dx = a.h - xi, dy = b.h - yi, dz = c.h - zi;
+          const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+#pragma unroll
+          for (int k = 0; k < SG_RBF; ++k) {
+            const float d = r - rbf_centre(k);
+            gacc[k] += __expf(-d * d * inv2w2);
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < SG_RBF; ++k) {
+        sG[i][k] = i < n ? gacc[k] : 0.f;
+        sGb[i][k] = __float2bfloat16_rn(i < n ? gacc[k] : 0.f);
+      }
+    }
+    __syncwarp();
+    forward_rows(sE);
+  };
+  refresh();
+
+  RecentScale rsb;
+  rsb.init();
+  DrawCache<32, false> dc;
+  dc.init();
+  DS sc = ds_from_double(fh.c.tscale);
+  uint64_t screened_out = 0, exact_evals = 0;
+  for (uint64_t it = 0; it < m.n_moves; ++it) {
+    const uint64_t t = fh.c.moves + 1;
+    double rs, omrs;
+    rsb.get(t, lane, rs, omrs);
+    fh.begin_move(omrs);
+    const Draws d = dc.get(m.seed, (uint32_t)w, t, (uint32_t)n, 0xffffffffu, lane);
+    // second-stage uniform: its own Philox stream (counter word 2 = 4)
+    const Philox4 U = philox4x32_10(Philox4{(uint32_t)t, (uint32_t)(t >> 32), 4u, (uint32_t)(m.seed >> 32)},
+                                    (uint32_t)w, (uint32_t)m.seed);
+    const uint64_t u2 = u53_bits(U.x, U.y);
+    const int a = (int)d.which;
+    DS fx, fy, fz;
+    lj.fetch(a, fx, fy, fz);
+    const DS tx = ds_add(fx, ds_scale(d.g0, sc.h, sc.l));
+    const DS ty = ds_add(fy, ds_scale(d.g1, sc.h, sc.l));
+    const DS tz = ds_add(fz, ds_scale(d.g2, sc.h, sc.l));
+    // ---- stage 1: surrogate screen ----
+    float part = 0.f;
+    for (int q = 0; q < APL; ++q) {
+      const int i = lane + 32 * q;
+      float contrib[SG_RBF];
+      if (i < n && i != a) {
+        const float xi = lj.x[q].h, yi = lj.y[q].h, zi = lj.z[q].h;
+        float dx = xi - fx.h, dy = yi - fy.h, dz = zi - fz.h;
+        const float ro = sqrtf(dx * dx + dy * dy + dz * dz);
+        dx = xi - tx.h; dy = yi - ty.h; dz = zi - tz.h;
+        const float rn = sqrtf(dx * dx + dy * dy + dz * dz);
+#pragma unroll
+        for (int k = 0; k < SG_RBF; ++k) {
+          const float cn = rbf_centre(k);
+          const float pn = __expf(-(rn - cn) * (rn - cn) * inv2w2);
+          const float po = __expf(-(ro - cn) * (ro - cn) * inv2w2);
+          const float gnew = sG[i][k] + pn - po;
+          sGf[i][k] = gnew;
+          sGb[i][k] = __float2bfloat16_rn(gnew);
+          contrib[k] = pn;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < SG_RBF; ++k) contrib[k] = 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < SG_RBF; ++k) sT[lane][k] = q == 0 ? contrib[k] : sT[lane][k] + contrib[k];
+    }
+    __syncwarp();
+    {  // moved atom's row: column sums of sT
+      float ga = 0.f;
+      for (int r = 0; r < 32; ++r) ga += sT[r][lane];
+      sGf[a][lane] = ga;
+      sGb[a][lane] = __float2bfloat16_rn(ga);
+    }
+    __syncwarp();
+    forward_rows(sEn);
+    for (int q = 0; q < APL; ++q) {
+      const int i = lane + 32 * q;
+      if (i < n) part += sEn[i] - sE[i];
+    }
+    const float des = group_sum<32>(part, 0xffffffffu);
+    const double e_til = fh.c.E + (double)des;
+    const double lnw_cur = fh.lnw_current();
+    const double lnw_til = fh.lnw_at(e_til);
+    const bool uphill1 = dgt(lnw_til, lnw_cur);
+    const bool rej1 = uphill1 && metropolis_reject(lnw_cur - lnw_til, d.u53);
+    // a certain stage-1 acceptance consumed no randomness: stage 2 may use the move's own
+    // uniform (with a constant surrogate the chain is then the plain chain, bit for bit)
+    const uint64_t u_second = uphill1 ? u2 : d.u53;
+    bool acc = false;
+    if (rej1) {
+      ++screened_out;
+    } else {
+      // ---- stage 2: exact energy ----
+      ++exact_evals;
+      DS ux, uy, uz;
+      float de = 0.f;
+      const bool possible = lj.plan(a, d.g0, d.g1, d.g2, sc.h, sc.l, s.radius2, ux, uy, uz, de);
+      acc = fh.decide_de(possible, de, u_second, rs, true, lnw_til);
+      if (acc) {
+        lj.put(a, tx, ty, tz);
+        for (int q = 0; q < APL; ++q) {
+          const int i = lane + 32 * q;
+#pragma unroll
+          for (int k = 0; k < SG_RBF; ++k) sG[i][k] = sGf[i][k];
+          sE[i] = sEn[i];
+        }
+        // the moved atom's row was written by lane k into column k
+        for (int k = 0; k < SG_RBF; ++k) sG[a][k] = sGf[a][k];
+        __syncwarp();
+      }
+    }
+    fh.finish_move(acc);
+    if (fh.tscale_changed) { fh.tscale_changed = false; sc = ds_from_double(fh.c.tscale); }
+    if (m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
+      const double e64 = lj.energy64();
+      const double dr = fabs(e64 - fh.c.E);
+      if (dr > fh.c.drift) fh.c.drift = dr;
+      if (dr > m.drift_tol) fh.c.status |= ST_DRIFT;
+      fh.set_E(e64);
+      fh.grew_front = false;
+      if (!fh.prepare(e64)) fh.c.status |= ST_BIN_RANGE;
+      else {
+        if (fh.grew_front) fh.reindex_after_growth();
+        fh.move_cur(fh.gidx(e64));
+      }
+    }
+    if (refresh_interval > 0 && (t % (uint64_t)refresh_interval) == 0) refresh();
+  }
+  lj.store(pw, s.np, true);
+  fh.store(m.cores, w);
+  if (stats && lane == 0) {
+    stats[2 * w] += screened_out;
+    stats[2 * w + 1] += exact_evals;
+  }
+}
+
+}  // namespace dev
+
+cudaError_t launch_lj_da(const MoveLaunch& m, const LjSys& s, const SgWeights& w,
+                         int refresh_interval, uint64_t* stats, cudaStream_t st) {
+  if (s.np == 32) dev::lj_da_kernel<1><<<m.n_walkers, 32, 0, st>>>(m, s, w, refresh_interval, stats);
+  else if (s.np == 64) dev::lj_da_kernel<2><<<m.n_walkers, 32, 0, st>>>(m, s, w, refresh_interval, stats);
+  else return cudaErrorInvalidConfiguration;
+  return cudaGetLastError();
+}
+
+}  // namespace sadmc

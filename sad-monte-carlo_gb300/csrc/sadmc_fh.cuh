@@ -279,6 +279,25 @@ struct Fh {
     Ef = f32_trunc(e);
   }
 
+  // ln w the Metropolis test would use at energy e (no bin growth; energies outside the
+  // allocated bins read 0, the value a newly allocated bin starts with, or the SAD
+  // extrapolation).  Used for the surrogate stage of delayed-acceptance moves.
+  __device__ double lnw_at(double e) const {
+    int g;
+    if (e < c.cur_min) g = c.b_lo - 1;
+    else if (e >= cur_max) g = c.b_hi + 1;
+    else g = gidx_exact(e);
+    if (c.kind == M_SAD) {
+      if (e < c.too_lo) return ld_lnw(win_lo) + (e - c.too_lo) / c.min_T;
+      if (e > c.too_hi) return ld_lnw(win_hi);
+    }
+    if (g < c.b_lo || g > c.b_hi) return 0.0;
+    return ld_lnw(g);
+  }
+  __device__ double lnw_current() const {
+    return c.kind == M_SAD ? sad_lnw(c.E, cur) : k_lnw;
+  }
+
   // ---- one move ----------------------------------------------------------------------
   __device__ void begin_move(double one_minus_rs) {
     c.moves += 1;                  // energy.rs:905
@@ -349,7 +368,11 @@ struct Fh {
   // one binary64 rounding); inside the bound, or wherever the exact value enters
   // arithmetic (SAD extrapolation, window edges, discoveries, the accepted energy), the
   // FP64 e2 is formed and the reference's comparison is evaluated on it.
-  __device__ bool decide_de(bool possible, float de, uint64_t u53, double rs) {
+  // has_first: the Metropolis test uses lnw_first in place of ln w(E) -- the second stage
+  // of a delayed-acceptance move, which accepts with min(1, exp(ln w(E~) - ln w(e2))) for
+  // the surrogate-predicted energy E~.
+  __device__ bool decide_de(bool possible, float de, uint64_t u53, double rs,
+                            bool has_first = false, double lnw_first = 0.0) {
     if (!possible || !(fabsf(de) <= 3.0e38f)) return false;
     const float e2f = Ef + de;
     const float tol = (fabsf(Ef) + fabsf(e2f)) * 2.5e-7f + 1e-30f;
@@ -408,7 +431,7 @@ struct Fh {
     bool rejected;
     switch (c.kind) {
       case M_SAD: {
-        const double lnw1 = sad_lnw(c.E, cur);
+        const double lnw1 = has_first ? lnw_first : sad_lnw(c.E, cur);
         if (i2 <= win_lo || i2 >= win_hi) exact();  // extrapolation / edge comparisons
         const double lnw2 = sad_lnw(e2, i2);
         rejected = dgt(lnw2, lnw1) && metropolis_reject(lnw1 - lnw2, u53);
@@ -424,12 +447,14 @@ struct Fh {
         break;
       }
       case M_SAMC: {
-        rejected = dgt(lnw2_raw, k_lnw) && metropolis_reject(k_lnw - lnw2_raw, u53);
+        const double lnw1 = has_first ? lnw_first : k_lnw;
+        rejected = dgt(lnw2_raw, lnw1) && metropolis_reject(lnw1 - lnw2_raw, u53);
         break;
       }
       case M_WL:
       case M_INV_T_WL: {
-        rejected = dgt(lnw2_raw, k_lnw) && metropolis_reject(k_lnw - lnw2_raw, u53);
+        const double lnw1 = has_first ? lnw_first : k_lnw;
+        rejected = dgt(lnw2_raw, lnw1) && metropolis_reject(lnw1 - lnw2_raw, u53);
         if (!rejected && hist2 == 0 && c.lowest_hist > 0) c.wl_num_states += 1.0;
         break;
       }

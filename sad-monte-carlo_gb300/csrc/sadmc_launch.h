@@ -43,6 +43,12 @@ cudaError_t launch_lj_plan(WalkerCore* cores, const LjSys& s, int walker, int wh
                            float g1, float g2, double scale, int confirm, double* out,
                            cudaStream_t st);
 
+// Delayed-acceptance LJ moves screened by the surrogate (sadmc_da.cu); stats gets per
+// walker (stage-1 rejections, exact evaluations) added.  One warp per walker.
+struct SgWeights;
+cudaError_t launch_lj_da(const MoveLaunch& m, const LjSys& s, const SgWeights& w,
+                         int refresh_interval, uint64_t* stats, cudaStream_t st);
+
 // 2D Ising.  spins: [walker][L*L] int8, index i + j*L.
 struct IsingSys {
   int8_t* spins;

@@ -1,0 +1,93 @@
+// Device helpers of the surrogate MLP: RBF centres, SiLU, bf16 packing and the
+// mma.sync m16n8k16 bf16 tensor-core instruction (FP32 accumulation).
+#pragma once
+#include <cuda_bf16.h>
+#include <cstdint>
+
+namespace sadmc {
+namespace dev {
+
+__device__ __forceinline__ float rbf_centre(int k) { return 0.8f + (2.2f / 31.0f) * (float)k; }
+
+__device__ __forceinline__ float silu32(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float dsilu32(float z) {
+  const float s = 1.0f / (1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// D = A * B + C, m16n8k16, bf16 x bf16 -> f32
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+}  // namespace dev
+}  // namespace sadmc
+
+namespace sadmc {
+namespace dev {
+
+// Surrogate energies of 16 rows (one warp): A fragments of G from a row-major bf16 tile
+// in shared memory (32 bf16 = 16 words per row), weights in shared memory as in the
+// forward kernel.  Rows g and g+8 of the tile end in ea / eb (in the quad's lane t == 0
+// and the others alike).
+__device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1,
+                                      const uint32_t* sW2, const float* sb1, const float* sb2,
+                                      const float* sw3, float b3, float& ea, float& eb) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t aG[2][4];
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt) {
+    aG[kt][0] = gtile[g * 16 + 8 * kt + t];
+    aG[kt][1] = gtile[(g + 8) * 16 + 8 * kt + t];
+    aG[kt][2] = gtile[g * 16 + 8 * kt + 4 + t];
+    aG[kt][3] = gtile[(g + 8) * 16 + 8 * kt + 4 + t];
+  }
+  float h1[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    const int n = 8 * j + g;
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt) mma16816(c, aG[kt], sW1[n * 16 + 8 * kt + t], sW1[n * 16 + 8 * kt + 4 + t]);
+    const float bb0 = sb1[8 * j + 2 * t], bb1 = sb1[8 * j + 2 * t + 1];
+    h1[j][0] = silu32(c[0] + bb0); h1[j][1] = silu32(c[1] + bb1);
+    h1[j][2] = silu32(c[2] + bb0); h1[j][3] = silu32(c[3] + bb1);
+  }
+  ea = 0.f;
+  eb = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    const int n = 8 * j + g;
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+      const uint32_t a[4] = {pack_bf16(h1[2 * kt][0], h1[2 * kt][1]), pack_bf16(h1[2 * kt][2], h1[2 * kt][3]),
+                             pack_bf16(h1[2 * kt + 1][0], h1[2 * kt + 1][1]),
+                             pack_bf16(h1[2 * kt + 1][2], h1[2 * kt + 1][3])};
+      mma16816(c, a, sW2[n * 32 + 8 * kt + t], sW2[n * 32 + 8 * kt + 4 + t]);
+    }
+    const float bb0 = sb2[8 * j + 2 * t], bb1 = sb2[8 * j + 2 * t + 1];
+    const float w0 = sw3[8 * j + 2 * t], w1 = sw3[8 * j + 2 * t + 1];
+    ea += silu32(c[0] + bb0) * w0 + silu32(c[1] + bb1) * w1;
+    eb += silu32(c[2] + bb0) * w0 + silu32(c[3] + bb1) * w1;
+  }
+  ea += __shfl_xor_sync(0xffffffffu, ea, 1);
+  ea += __shfl_xor_sync(0xffffffffu, ea, 2);
+  eb += __shfl_xor_sync(0xffffffffu, eb, 1);
+  eb += __shfl_xor_sync(0xffffffffu, eb, 2);
+  ea += b3;
+  eb += b3;
+}
+
+}  // namespace dev
+}  // namespace sadmc

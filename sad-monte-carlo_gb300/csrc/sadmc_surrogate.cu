@@ -15,33 +15,11 @@
 #include <cuda_runtime.h>
 
 #include "sadmc_common.cuh"
+#include "sadmc_mma.cuh"
 #include "sadmc_surrogate.h"
 
 namespace sadmc {
 namespace dev {
-
-__device__ __forceinline__ float rbf_centre(int k) { return 0.8f + (2.2f / 31.0f) * (float)k; }
-
-__device__ __forceinline__ float silu32(float z) { return z / (1.0f + __expf(-z)); }
-__device__ __forceinline__ float dsilu32(float z) {
-  const float s = 1.0f / (1.0f + __expf(-z));
-  return s * (1.0f + z * (1.0f - s));
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<uint32_t*>(&v);
-}
-__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-
-// D = A * B + C, m16n8k16, bf16 x bf16 -> f32
-__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
 
 // Descriptors of rows [row0, row0 + rows): row r = atom (r % n) of configuration (r / n);
 // positions [configs][n][3] binary32.  Writes bf16 G (the forward operand) and, if

@@ -100,6 +100,14 @@ def lib():
         "sadmc_checkpoint": (I32, [P, ctypes.c_char_p]),
         "sadmc_resume": (I32, [ctypes.c_char_p, P]),
         "sadmc_get_config": (I32, [P, P, P]),
+        "sadmc_surrogate_init": (I32, [P, U64, I32]),
+        "sadmc_surrogate_get_params": (I32, [P, P]),
+        "sadmc_surrogate_set_params": (I32, [P, P]),
+        "sadmc_surrogate_collect": (I32, [P, P]),
+        "sadmc_surrogate_train": (I32, [P, I32, I32, ctypes.c_float, U64, P]),
+        "sadmc_surrogate_loss_grads": (I32, [P, P, P, I32, P, P]),
+        "sadmc_surrogate_predict": (I32, [P, P, I32, P]),
+        "sadmc_run_da": (I32, [P, U64, I32, P]),
         "sadmc_draws": (I32, [I32, ctypes.c_uint32, U64, ctypes.c_uint32, U64, I32, ctypes.c_uint32,
                               P, P, P]),
     }
@@ -310,6 +318,52 @@ class Batch:
         b.n = np.array([g.n for g in b._geom])
         return b
 
+    # ---- learned surrogate (LJ) -------------------------------------------------------
+    SG_NPARAM = 6337
+
+    def surrogate_init(self, seed=0, ring_capacity=100000):
+        _check(lib().sadmc_surrogate_init(self.h, seed, ring_capacity))
+
+    def surrogate_params(self):
+        out = np.zeros(self.SG_NPARAM, np.float32)
+        _check(lib().sadmc_surrogate_get_params(self.h, _p(out)))
+        return out
+
+    def surrogate_set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        _check(lib().sadmc_surrogate_set_params(self.h, _p(p)))
+
+    def surrogate_collect(self):
+        n = ctypes.c_int32(0)
+        _check(lib().sadmc_surrogate_collect(self.h, ctypes.byref(n)))
+        return n.value
+
+    def surrogate_train(self, steps, batch=256, lr=1e-3, seed=0):
+        loss = ctypes.c_double(0)
+        _check(lib().sadmc_surrogate_train(self.h, steps, batch, lr, seed, ctypes.byref(loss)))
+        return loss.value
+
+    def surrogate_loss_grads(self, pos, target):
+        pos = np.ascontiguousarray(pos, np.float32)
+        target = np.ascontiguousarray(target, np.float32)
+        g = np.zeros(self.SG_NPARAM, np.float32)
+        loss = ctypes.c_double(0)
+        _check(lib().sadmc_surrogate_loss_grads(self.h, _p(pos), _p(target), len(target),
+                                                ctypes.byref(loss), _p(g)))
+        return loss.value, g
+
+    def run_da(self, moves, refresh_interval=2048):
+        """Delayed-acceptance moves; returns per-walker (stage-1 rejections, exact evaluations)."""
+        st = np.zeros(2 * self.W, np.uint64)
+        _check(lib().sadmc_run_da(self.h, int(moves), refresh_interval, _p(st)))
+        return st.reshape(-1, 2)
+
+    def surrogate_predict(self, pos):
+        pos = np.ascontiguousarray(pos, np.float32)
+        out = np.zeros(pos.shape[0], np.float32)
+        _check(lib().sadmc_surrogate_predict(self.h, _p(pos), pos.shape[0], _p(out)))
+        return out
+
     def lanes_per_walker(self):
         return lib().sadmc_lanes_per_walker(self.h)
 
@@ -317,6 +371,23 @@ class Batch:
         lpw, ms = ctypes.c_int32(0), ctypes.c_double(0)
         _check(lib().sadmc_autotune(self.h, int(moves), ctypes.byref(lpw), ctypes.byref(ms)))
         return lpw.value, ms.value
+
+
+def unpack_params(flat):
+    """Flat surrogate parameters -> dict (W1 [32,64], b1, W2 [64,64], b2, w3, b3)."""
+    f = np.asarray(flat, np.float64)
+    o = 0
+    out = {}
+    for name, shape in [("W1", (32, 64)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)),
+                        ("w3", (64,)), ("b3", (1,))]:
+        size = int(np.prod(shape))
+        out[name] = f[o:o + size].reshape(shape)
+        o += size
+    return out
+
+
+def pack_params(d):
+    return np.concatenate([np.ravel(d[k]) for k in ("W1", "b1", "W2", "b2", "w3", "b3")]).astype(np.float32)
 
 
 def draws(system, n, seed, walker, t0, count, stream_pair=0):

@@ -133,3 +133,40 @@ def test_heat_capacity_matches_numpy(oracle):
         P = P / P.sum()
         U = (E * P).sum()
         assert c == pytest.approx(((E - U) ** 2 * P).sum() / t ** 2, rel=1e-10)
+
+
+def test_mlp_oracle_gradients_by_finite_differences():
+    """The FP64 surrogate oracle's analytic gradients (no bf16 emulation) against central
+    differences."""
+    import mlp_oracle as M
+    rng = np.random.default_rng(0)
+    n, C = 6, 3
+    pos = rng.uniform(-1.2, 1.2, (C, n, 3))
+    G = np.concatenate([M.descriptors(p) for p in pos])
+    target = rng.uniform(-10, 0, C)
+    p = M.init_params(1)
+    p["b1"] = rng.normal(0, 0.1, 64)
+    p["b3"] = np.array([0.3])
+    loss, g = M.loss_and_grads(G, n, target, p, emulate_bf16=False)
+    for name in p:
+        flat = p[name].ravel()
+        for k in rng.choice(flat.size, size=min(6, flat.size), replace=False):
+            old = flat[k]
+            flat[k] = old + 1e-6
+            lp, _ = M.loss_and_grads(G, n, target, p, emulate_bf16=False)
+            flat[k] = old - 1e-6
+            lm, _ = M.loss_and_grads(G, n, target, p, emulate_bf16=False)
+            flat[k] = old
+            fd = (lp - lm) / 2e-6
+            assert fd == pytest.approx(g[name].ravel()[k], rel=1e-5, abs=1e-8), (name, k)
+
+
+def test_bf16_rounding_is_nearest_even():
+    import mlp_oracle as M
+    x = np.array([1.0 + 2 ** -8, 1.0 + 2 ** -9, 1.0 + 3 * 2 ** -9, 1.0 + 3 * 2 ** -8, -3.14159])
+    r = M.bf16(x)
+    assert r[0] == 1.0                      # midpoint, ties to even (down)
+    assert r[1] == 1.0                      # below the midpoint
+    assert r[2] == 1.0 + 2 ** -7            # above the midpoint
+    assert r[3] == 1.0 + 2 ** -6            # midpoint, ties to even (up)
+    assert r[4] == -3.140625
