@@ -57,6 +57,56 @@ def lj_configs(n_walkers, seed):
     return out
 
 
+def da_compare(G, rank=0, walkers=8192, moves=2048):
+    """C4 shape: LJ38 (R=3.5), SAD; the surrogate is trained on configurations the walkers
+    visit, then plain and delayed-acceptance moves are timed on the same batch state."""
+    import ctypes
+    import torch
+    n, R = 38, 3.5
+    rng = np.random.default_rng(77 + rank)
+    confs = []
+    for _ in range(walkers):  # uniform in the sphere with sequential 0.8 rejection
+        pts = []
+        while len(pts) < n:
+            p = rng.uniform(-R, R, 3)
+            if p @ p >= R * R or (pts and np.min(np.sum((np.array(pts) - p) ** 2, axis=1)) < 0.64):
+                continue
+            pts.append(p)
+        confs.append(np.array(pts))
+    cfg = G.make_config(G.LJ, walkers, n, method=G.SAD, min_T=0.05, energy_bin=0.2,
+                        max_allowed=0.0, e_lo=-180.0, e_hi=1.0, target_rate=0.5,
+                        translation_scale=0.1, seed=21 + rank, lanes_per_walker=32)
+    b = G.Batch(cfg, [(n, R, (0, 0, 0))] * walkers)
+    b.upload(confs)
+    b.initialize()
+    b.surrogate_init(seed=3, ring_capacity=1 << 16)
+    for _ in range(8):
+        b.run(1024)
+        b.surrogate_collect()
+    t0 = time.perf_counter()
+    loss = b.surrogate_train(800, batch=512, lr=2e-3, seed=5)
+    train_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    m0, a0 = b.counters()
+    t0 = time.perf_counter()
+    b.run(moves)
+    plain_s = time.perf_counter() - t0
+    m1, a1 = b.counters()
+    t0 = time.perf_counter()
+    st = b.run_da(moves)
+    da_s = time.perf_counter() - t0
+    m2, a2 = b.counters()
+    b.close()
+    screened = float(st[:, 0].sum()) / float(st.sum())
+    return {"workload": f"C4 shape: LJ{n} (R={R}), SAD, {walkers} walkers, {moves} moves/walker each arm, "
+                        "one walker per warp in both arms",
+            "plain_moves_per_s": (m1 - m0) / plain_s, "plain_accepted_per_s": (a1 - a0) / plain_s,
+            "da_moves_per_s": (m2 - m1) / da_s, "da_accepted_per_s": (a2 - a1) / da_s,
+            "da_vs_plain": ((m2 - m1) / da_s) / ((m1 - m0) / plain_s),
+            "screened_fraction": screened, "surrogate_rmse": float(np.sqrt(loss)),
+            "train_s": train_s}
+
+
 def make_batch(G, n_walkers, seed=1, lpw=0):
     cfg = G.make_config(G.LJ, n_walkers, N_ATOMS, method=G.SAD, min_T=0.2, energy_bin=WIDTH,
                         max_allowed=0.0, e_lo=E_LO - 2 * WIDTH, e_hi=E_HI + 2 * WIDTH,
@@ -178,6 +228,7 @@ def run_gpu(args):
     import torch
     import sadmc_gb300 as G
     import build as B
+    import replicas as Rp
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -191,7 +242,7 @@ def run_gpu(args):
 
     # ---- device-resident throughput -------------------------------------------------
     confs = lj_configs(WALKERS, 1000 + rank)
-    b = make_batch(G, WALKERS, seed=1 + rank, lpw=args.lpw)
+    b = make_batch(G, WALKERS, seed=Rp.rank_seed(1, rank), lpw=args.lpw)
     b.upload(list(confs))
     b.initialize()
     stream = torch.cuda.Stream()
@@ -220,10 +271,7 @@ def run_gpu(args):
     moves = m1 - m0
     if moves != WALKERS * MOVES_PER_STEP * args.steps:
         raise RuntimeError(f"move count {moves} != expected")
-    t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(t.item())
+    ms = Rp.max_over_ranks(ms, device="cuda")
     value = moves * world / (ms * 1e-3)
     acc_rate = (a1 - a0) / moves
     status = b.status()
@@ -269,6 +317,10 @@ def run_gpu(args):
                "includes": "upload, initialize (FP64 energies, descent, bins), run, read planes"}
         be.close()
 
+    da = None
+    if not args.no_da and world == 1:
+        da = da_compare(G, rank)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -301,6 +353,7 @@ def run_gpu(args):
             "gpu_launches": args.steps * launches_per_step,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "delayed_acceptance": da,
         }
         print(json.dumps(line))
     if world > 1:
@@ -320,6 +373,7 @@ def main():
                     help="walkers (profiling a smaller case; the bench line uses 4096)")
     ap.add_argument("--moves", type=int, default=MOVES_PER_STEP, help="moves per walker per step")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-da", action="store_true", help="skip the delayed-acceptance comparison")
     args = ap.parse_args()
     WALKERS, MOVES_PER_STEP = args.walkers, args.moves
     if args.impl == "reference":
