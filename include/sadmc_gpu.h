@@ -155,6 +155,11 @@ int32_t sadmc_read_planes(sadmc_handle* h, double* lnw, uint64_t* histogram, int
 /* Wang-Landau per-stage histogram (Method::WL::hist), *n entries from *min_energy. */
 int32_t sadmc_read_wl_hist(sadmc_handle* h, int32_t walker, uint64_t* hist, int64_t* n,
                            double* min_energy);
+/* The binned "pressure" datum of the WCA fluid, collected every N^2 moves
+ * (Bins::extra["pressure"], a BinCounts; src/system/wca.rs:202-218 collected at
+ * src/mc/energy.rs:944-946): count and total per allocated bin, the same n entries as
+ * sadmc_read_bins.  SADMC_ERR_INVALID for the systems that collect no data. */
+int32_t sadmc_read_extra(sadmc_handle* h, int32_t walker, uint64_t* count, double* total);
 
 /* Scalar state of one walker, SADMC_N_SCALARS doubles in this order: moves, accepted,
  * acceptance_rate, translation_scale, method, too_lo, too_hi, tL, tF, num_states,

@@ -65,7 +65,15 @@ struct Bins {  // energy.rs:145-163
   double min = 0, width = 1;
   std::vector<uint64_t> histogram, t_found;
   std::vector<double> lnw, energy_total, energy_squared_total;
+  // the one `extra` datum of the systems here: WCA "pressure" (BinCounts, energy.rs:136-142)
+  std::vector<uint64_t> extra_count;
+  std::vector<double> extra_total;
 };
+
+// System::data_to_collect (src/system/mod.rs:88-90): only the WCA fluid collects data
+// (wca.rs:202-218), every N^2 moves.
+template <class S>
+inline bool collect_extra(const S&, uint64_t, double*) { return false; }
 
 // SadVersion::compute_gamma, energy.rs:22-38
 inline double sad_compute_gamma(double latest_parameter, double t, double tF, double num_states) {
@@ -185,6 +193,10 @@ struct EnergyMC {
       bins.lnw.insert(bins.lnw.begin(), 0.0);
       bins.energy_total.insert(bins.energy_total.begin(), 0.0);
       bins.energy_squared_total.insert(bins.energy_squared_total.begin(), 0.0);
+      if (!bins.extra_count.empty()) {
+        bins.extra_count.insert(bins.extra_count.begin(), 0);
+        bins.extra_total.insert(bins.extra_total.begin(), 0.0);
+      }
       have_visited_since_maxentropy.insert(have_visited_since_maxentropy.begin(), 1);
       round_trips.insert(round_trips.begin(), 1);
       bins.min -= bins.width;
@@ -195,6 +207,10 @@ struct EnergyMC {
       bins.t_found.push_back(0);
       bins.energy_total.push_back(0.0);
       bins.energy_squared_total.push_back(0.0);
+      if (!bins.extra_count.empty()) {
+        bins.extra_count.push_back(0);
+        bins.extra_total.push_back(0.0);
+      }
       have_visited_since_maxentropy.push_back(1);
       round_trips.push_back(1);
     }
@@ -429,6 +445,15 @@ struct EnergyMC {
     bins.histogram[i] += 1;
     bins.energy_total[i] += energy;
     bins.energy_squared_total[i] += energy * energy;
+    double datum;
+    if (collect_extra(sys, moves, &datum)) {  // energy.rs:944-946, accumulate_extra 374-386
+      if (bins.extra_count.empty()) {
+        bins.extra_count.assign(bins.lnw.size(), 0);
+        bins.extra_total.assign(bins.lnw.size(), 0.0);
+      }
+      bins.extra_count[i] += 1;
+      bins.extra_total[i] += datum;
+    }
     update_weights(energy);
     if (bins.lnw[i] > max_S) {
       max_S = bins.lnw[i];

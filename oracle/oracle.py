@@ -63,6 +63,7 @@ def lib():
             "orc_run_override": (D, [P, U64, P, P, P]),
             "orc_energy": (D, [P]), "orc_compute_energy": (D, [P]),
             "orc_override_worst": (None, [P, P]),
+            "orc_extra": (I64, [P, P, P]),
             "orc_verify_energy": (ctypes.c_int, [P]),
             "orc_get_state": (None, [P, P]),
             "orc_plan_move": (ctypes.c_int, [P, U32, U32, D, D, D, D, P]),
@@ -148,6 +149,14 @@ class Walker:
         mm = ctypes.c_uint64(0)
         d = lib().orc_run_override(self.h, len(e2), _p(e1), _p(e2), ctypes.byref(mm))
         return d, mm.value
+
+    def extra(self):
+        """The WCA pressure BinCounts: (count, total) per bin (empty arrays if none)."""
+        n = lib().orc_extra(self.h, None, None)
+        c = np.zeros(max(n, 1), np.uint64)
+        t = np.zeros(max(n, 1))
+        lib().orc_extra(self.h, _p(c), _p(t))
+        return c[:n], t[:n]
 
     def override_worst(self):
         """(move, e2 given, e2 own, gross pair-term magnitude) of the largest replay gap."""

@@ -179,6 +179,18 @@ double orc_run_override(void* hv, uint64_t nmoves, const double* e1, const doubl
   });
 }
 
+// The "pressure" BinCounts of the bins (empty unless the system collects it).
+int64_t orc_extra(void* hv, uint64_t* count, double* total) {
+  return ((AnyMC*)hv)->visit([&](auto& mc) {
+    const size_t n = mc.bins.extra_count.size();
+    for (size_t k = 0; k < n; ++k) {
+      if (count) count[k] = mc.bins.extra_count[k];
+      if (total) total[k] = mc.bins.extra_total[k];
+    }
+    return (int64_t)n;
+  });
+}
+
 void orc_override_worst(void* hv, double* out4) {
   ((AnyMC*)hv)->visit([&](auto& mc) { for (int k = 0; k < 4; ++k) out4[k] = mc.worst[k]; return 0; });
 }

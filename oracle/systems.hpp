@@ -398,6 +398,19 @@ struct Wca {
   }
 };
 
+// System::data_to_collect (src/system/mod.rs:88-90); the primary template (no datum)
+// lives with the bins in energy_mc.hpp.
+template <class S>
+inline bool collect_extra(const S&, uint64_t, double*);
+// wca.rs:202-218: the pressure datum every N^2 moves
+template <>
+inline bool collect_extra<Wca>(const Wca& s, uint64_t iter, double* out) {
+  const uint64_t n = (uint64_t)s.num_atoms();
+  if (n == 0 || iter % (n * n) != 0) return false;
+  *out = s.pressure();
+  return true;
+}
+
 // ---------------------------------------------------------------------------------
 // Square well with a hard core (the "hard sphere with contact-count bins" system):
 // src/system/optsquare.rs:24-322

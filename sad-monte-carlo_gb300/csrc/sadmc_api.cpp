@@ -68,6 +68,7 @@ struct sadmc_handle {
   WalkerCore* d_cores = nullptr;
   BinPlanes planes{};
   void* plane_mem = nullptr;
+  int n_planes = 8;  // 10 with the WCA pressure planes
   float* d_pos = nullptr;      // LJ: [W][6][np]
   int8_t* d_spins = nullptr;   // Ising: [W][L*L]
   // periodic cell systems (square well, WCA)
@@ -233,7 +234,7 @@ struct DevBuf {
 
 std::vector<DevBuf> state_buffers(sadmc_handle* h) {
   const size_t W = h->W, nb = h->nb, np = h->np;
-  std::vector<DevBuf> v = {{h->d_cores, sizeof(WalkerCore) * W}, {h->plane_mem, W * nb * 8 * 8}};
+  std::vector<DevBuf> v = {{h->d_cores, sizeof(WalkerCore) * W}, {h->plane_mem, W * nb * 8 * (size_t)h->n_planes}};
   switch (h->cfg.system) {
     case SADMC_ISING: v.push_back({h->d_spins, W * (size_t)h->L * h->L}); break;
     case SADMC_LJ: v.push_back({h->d_pos, W * 6 * np * sizeof(float)}); break;
@@ -385,8 +386,9 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete h; return fail(SADMC_ERR_CUDA, cudaGetErrorString(e)); }
   const size_t plane = (size_t)h->W * (size_t)h->nb;
+  h->n_planes = c.system == SADMC_WCA ? 10 : 8;
   bool ok = dalloc(&h->d_cores, h->W) == cudaSuccess && dalloc(&h->d_tmp, h->W + 2) == cudaSuccess &&
-            cudaMalloc(&h->plane_mem, plane * 8 * 8) == cudaSuccess;
+            cudaMalloc(&h->plane_mem, plane * 8 * (size_t)h->n_planes) == cudaSuccess;
   if (ok) {
     char* b = (char*)h->plane_mem;
     h->planes.lnw = (double*)(b + 0 * plane * 8);
@@ -397,6 +399,10 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
     h->planes.round_trips = (uint64_t*)(b + 5 * plane * 8);
     h->planes.visit_stamp = (uint64_t*)(b + 6 * plane * 8);
     h->planes.wl_hist = (uint64_t*)(b + 7 * plane * 8);
+    if (h->n_planes == 10) {
+      h->planes.ex_count = (uint64_t*)(b + 8 * plane * 8);
+      h->planes.ex_total = (double*)(b + 9 * plane * 8);
+    }
     if (c.system == SADMC_ISING) ok = dalloc(&h->d_spins, (size_t)h->W * h->L * h->L) == cudaSuccess;
     else if (c.system == SADMC_LJ) ok = dalloc(&h->d_pos, (size_t)h->W * 6 * h->np) == cudaSuccess;
     else {
@@ -775,6 +781,23 @@ int32_t sadmc_read_bins(sadmc_handle* h, int32_t walker, double* lnw, uint64_t* 
   if (visited)
     for (size_t i = 0; i < n; ++i) visited[i] = st[i] == k.fill_gen ? 1 : (uint8_t)(k.fill_val != 0);
   // the cached current bin lives in the planes after each launch (flushed on store)
+  return SADMC_OK;
+}
+
+int32_t sadmc_read_extra(sadmc_handle* h, int32_t walker, uint64_t* count, double* total) {
+  if (!h || walker < 0 || walker >= h->W) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  if (!h->planes.ex_count) return fail(SADMC_ERR_INVALID, "this system collects no data");
+  WalkerCore k;
+  CUDA_TRY(cudaMemcpyAsync(&k, h->d_cores + walker, sizeof(k), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const size_t n = (size_t)(k.b_hi - k.b_lo + 1);
+  const size_t off = (size_t)walker * h->nb + k.b_lo;
+  if (count)
+    CUDA_TRY(cudaMemcpyAsync(count, h->planes.ex_count + off, n * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (total)
+    CUDA_TRY(cudaMemcpyAsync(total, h->planes.ex_total + off, n * 8, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
   return SADMC_OK;
 }
 

@@ -74,7 +74,42 @@ struct CellWalker {
   int nc[3];
   int np, bucket;
   __device__ int cell_index(int x, int y, int z) const { return (x * nc[1] + y) * nc[2] + z; }
+  // FP64 sum of f(|r_i - r_j|^2) over the candidates j != i of atom i in its 27
+  // subcells, with the reference's periodic image offsets (the
+  // maybe_interacting_atoms_excluding loops of wca.rs:202-218 and 222-230).
+  template <class F>
+  __device__ double pair_sum64(int i, F f) const {
+    const double ix = p[i], iy = p[np + i], iz = p[2 * np + i];
+    const int ci = cell_of[i];
+    const int cx = ci / (nc[1] * nc[2]), cy = (ci / nc[2]) % nc[1], cz = ci % nc[2];
+    double e = 0.0;
+    for (int k0 = 0; k0 < 27; ++k0) {
+      const int dx = k0 / 9 - 1, dy = (k0 / 3) % 3 - 1, dz = k0 % 3 - 1;
+      int ux = cx + dx, uy = cy + dy, uz = cz + dz, ox = 0, oy = 0, oz = 0;
+      if (ux < 0) { ux += nc[0]; ox = 1; } else if (ux >= nc[0]) { ux -= nc[0]; ox = -1; }
+      if (uy < 0) { uy += nc[1]; oy = 1; } else if (uy >= nc[1]) { uy -= nc[1]; oy = -1; }
+      if (uz < 0) { uz += nc[2]; oz = 1; } else if (uz >= nc[2]) { uz -= nc[2]; oz = -1; }
+      const int c = cell_index(ux, uy, uz);
+      const int mm = cnt[c];
+      for (int q = 0; q < mm; ++q) {
+        const int j = atoms[(size_t)c * bucket + q];
+        if (j == i) continue;
+        const double bx = (p[j] - (double)ox * L[0]) - ix;
+        const double by = (p[np + j] - (double)oy * L[1]) - iy;
+        const double bz = (p[2 * np + j] - (double)oz * L[2]) - iz;
+        e += f(bx * bx + by * by + bz * bz);
+      }
+    }
+    return e;
+  }
 };
+
+// potential_pressure (wca.rs:79-92): -r dV/dr / 2 for r < 2^(1/6), sigma = epsilon = 1.
+__device__ __forceinline__ double wca_pressure64(double r2, double rc2) {
+  if (!(r2 < rc2)) return 0.0;
+  double s = 1.0 / r2;
+  return 4.0 * 3.0 * (2.0 * powi6(s) - powi3(s));
+}
 
 template <int LPW, int KIND>
 struct CellOps {
@@ -245,31 +280,24 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
       __syncwarp(gmask);
     }
     fh.finish_move(acc);
+    if (KIND == SYS_WCA && m.B.ex_count && (t % ((uint64_t)n * (uint64_t)n)) == 0) {
+      // the "pressure" datum every N^2 moves into the current bin (wca.rs:202-218,
+      // collected and binned as in energy.rs:944-946 and 374-386)
+      double pv = 0.0;
+      for (int i = glane; i < n; i += LPW)
+        pv += cw.pair_sum64(i, [&](double r2) { return wca_pressure64(r2, wsqr); });
+      pv = group_sum<LPW>(pv, gmask);
+      if (wr && glane == 0) {
+        const size_t k = (size_t)w * fh.nbins + fh.cur;
+        m.B.ex_count[k] += 1;
+        m.B.ex_total[k] += pv / (3.0 * (cw.L[0] * cw.L[1] * cw.L[2]));
+      }
+    }
     if (KIND == SYS_WCA && m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
       // FP64 re-sum (wca.rs:222-230)
       double e = 0.0;
-      for (int i = glane; i < n; i += LPW) {
-        const double ix = cw.p[i], iy = cw.p[s.np + i], iz = cw.p[2 * s.np + i];
-        const int ci = cw.cell_of[i];
-        const int cx = ci / (cw.nc[1] * cw.nc[2]), cy = (ci / cw.nc[2]) % cw.nc[1], cz = ci % cw.nc[2];
-        for (int k0 = 0; k0 < 27; ++k0) {
-          const int dx = k0 / 9 - 1, dy = (k0 / 3) % 3 - 1, dz = k0 % 3 - 1;
-          int ux = cx + dx, uy = cy + dy, uz = cz + dz, ox = 0, oy = 0, oz = 0;
-          if (ux < 0) { ux += cw.nc[0]; ox = 1; } else if (ux >= cw.nc[0]) { ux -= cw.nc[0]; ox = -1; }
-          if (uy < 0) { uy += cw.nc[1]; oy = 1; } else if (uy >= cw.nc[1]) { uy -= cw.nc[1]; oy = -1; }
-          if (uz < 0) { uz += cw.nc[2]; oz = 1; } else if (uz >= cw.nc[2]) { uz -= cw.nc[2]; oz = -1; }
-          const int c = cw.cell_index(ux, uy, uz);
-          const int mm = cw.cnt[c];
-          for (int q = 0; q < mm; ++q) {
-            const int j = cw.atoms[(size_t)c * cw.bucket + q];
-            if (j == i) continue;
-            const double bx = (cw.p[j] - (double)ox * cw.L[0]) - ix;
-            const double by = (cw.p[s.np + j] - (double)oy * cw.L[1]) - iy;
-            const double bz = (cw.p[2 * s.np + j] - (double)oz * cw.L[2]) - iz;
-            e += wca_v64(bx * bx + by * by + bz * bz, wsqr);
-          }
-        }
-      }
+      for (int i = glane; i < n; i += LPW)
+        e += cw.pair_sum64(i, [&](double r2) { return wca_v64(r2, wsqr); });
       const double e64 = group_sum<LPW>(e, gmask) * 0.5;
       const double dr = fabs(e64 - fh.c.E);
       if (dr > fh.c.drift) fh.c.drift = dr;

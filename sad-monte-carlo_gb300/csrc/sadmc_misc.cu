@@ -21,6 +21,7 @@ __global__ void init_planes_kernel(const WalkerCore* cores, BinPlanes B, int nbi
     B.round_trips[k] = 1;
     B.visit_stamp[k] = 0;
     B.wl_hist[k] = 0;
+    if (B.ex_count) { B.ex_count[k] = 0; B.ex_total[k] = 0.0; }
     if (g == c.b_lo) {
       B.hist[k] = 1;
       B.sumE[k] = c.E;

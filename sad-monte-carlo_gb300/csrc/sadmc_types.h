@@ -73,6 +73,10 @@ struct BinPlanes {
   uint64_t* round_trips;
   uint64_t* visit_stamp;  // generation at which a bin was last set visited
   uint64_t* wl_hist;
+  // the binned "pressure" datum of the WCA fluid (BinCounts count/total); null for the
+  // systems that collect no data
+  uint64_t* ex_count;
+  double* ex_total;
 };
 
 // Per-move record for parity replay (trace mode only).

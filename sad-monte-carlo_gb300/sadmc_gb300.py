@@ -91,6 +91,7 @@ def lib():
         "sadmc_nbins": (I32, [P, I32, P, P, P]),
         "sadmc_read_bins": (I32, [P, I32, P, P, P, P, P, P, P]),
         "sadmc_read_wl_hist": (I32, [P, I32, P, P, P]),
+        "sadmc_read_extra": (I32, [P, I32, P, P]),
         "sadmc_plane_bins": (I32, [P, P]), "sadmc_read_planes": (I32, [P, P, P, P, P]),
         "sadmc_read_scalars": (I32, [P, I32, P]),
         "sadmc_counters": (I32, [P, P, P]), "sadmc_status": (I32, [P, P]),
@@ -276,6 +277,13 @@ class Batch:
         out = np.zeros(max(n.value, 1), np.uint64)
         _check(lib().sadmc_read_wl_hist(self.h, w, _p(out), ctypes.byref(n), ctypes.byref(me)))
         return out[:n.value], me.value
+
+    def extra(self, w):
+        """The WCA "pressure" BinCounts of walker w: (count, total) over its bins."""
+        n = len(self.bins(w)["lnw"])
+        c, t = np.zeros(n, np.uint64), np.zeros(n)
+        _check(lib().sadmc_read_extra(self.h, w, _p(c), _p(t)))
+        return c, t
 
     def scalars(self, w):
         o = np.zeros(len(SCALARS))

@@ -66,6 +66,47 @@ def wca_config(n, rho, seed):
     return np.mod(pos, L), (L, L, L)
 
 
+@pytest.mark.parametrize("lpw", [4, 16])
+def test_wca_pressure_channel(gpu, oracle, lpw):
+    """The binned "pressure" datum (wca.rs:202-218, every N^2 moves): counts bit-exact,
+    totals to FP64 summation order, on small fluids that collect several samples."""
+    specs = [(32, 0.6), (27, 0.7), (40, 0.8), (48, 0.8)]
+    moves, seed, w_bin = 8000, 9, 0.5
+    confs = [wca_config(n, rho, 30 + k) for k, (n, rho) in enumerate(specs)]
+    cfg = gpu.make_config(gpu.WCA, len(specs), max(n for n, _ in specs), method=1, t0=500.0,
+                          energy_bin=w_bin, e_lo=-2 * w_bin, e_hi=2100.0, max_allowed=2000.0,
+                          translation_scale=0.1, seed=seed, lanes_per_walker=lpw,
+                          resum_interval=1500)
+    b = gpu.Batch(cfg, [(n, 0.0, box) for (n, _), (_, box) in zip(specs, confs)])
+    b.upload([p for p, _ in confs])
+    b.initialize()
+    E0 = b.energies()
+    b.set_trace(moves)
+    b.run(moves)
+    for w, ((n, rho), (pos, box)) in enumerate(zip(specs, confs)):
+        e1, e2 = b.trace(w, moves)
+        ow = oracle.Walker(oracle.make_config(oracle.WCA, n, box=box, method=1, t0=500.0,
+                                              energy_bin=w_bin, max_allowed=2000.0,
+                                              translation_scale=0.1, seed=seed, walker=w,
+                                              e0=float(E0[w])), pos)
+        disc, mismatch = ow.run_override(e1, e2)
+        assert mismatch == 0 and disc < 2e-5, (w, mismatch, disc)
+        gc, gt = b.extra(w)
+        oc, ot = ow.extra()
+        assert int(gc.sum()) == moves // (n * n), (w, gc.sum())
+        np.testing.assert_array_equal(gc, oc, err_msg=f"walker {w}")
+        np.testing.assert_allclose(gt, ot, rtol=1e-12, atol=0, err_msg=f"walker {w}")
+    # the square well collects no data
+    (pos, box), = sw_walkers(oracle, 108, [0.3], 7)
+    sw = gpu.Batch(gpu.make_config(gpu.SW, 1, 108, e_lo=-650.0, e_hi=2.0, well_width=1.3),
+                   [(108, 0.0, box)])
+    sw.upload([pos])
+    sw.initialize()
+    sw.run(10)
+    with pytest.raises(gpu.SadmcError, match="collects no data"):
+        sw.extra(0)
+
+
 @pytest.mark.parametrize("lpw", [8, 32])
 def test_wca_uneven_trace_replay(gpu, oracle, lpw):
     specs = [(64, 0.6), (64, 0.9), (128, 0.7), (128, 0.8), (96, 0.75), (64, 0.85)]

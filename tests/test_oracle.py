@@ -76,6 +76,37 @@ def test_wca_energy_is_right(oracle, n, rho):
     assert oracle.selftest_moves(w, 1000, 1.0) == 0
 
 
+def test_wca_pressure_datum(oracle):
+    """wca.rs:202-218: every N^2 moves the bin of the current energy receives
+    sum_pairs 12 (2 s^6 - s^3) / (3 V) (s = 1/r^2, r < 2^(1/6)), computed here with numpy
+    minimum images on the final state after exactly N^2 moves."""
+    n, rho = 32, 0.6
+    L = (n / rho) ** (1 / 3)
+    m = 4
+    g = np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)
+    g = g[np.random.default_rng(5).permutation(len(g))[:n]]
+    pos = np.mod((g + 0.5) * (L / m), L)
+    w = oracle.Walker(oracle.make_config(oracle.WCA, n, box=(L, L, L), method=1, t0=500.0,
+                                         energy_bin=0.5, max_allowed=2000.0), pos)
+    w.run(n * n - 1)
+    c, t = w.extra()
+    assert len(c) == 0  # nothing collected before move N^2 (the BinCounts is created lazily)
+    w.run(1)
+    c, t = w.extra()
+    assert int(c.sum()) == 1 and len(c) == len(w.bins()["lnw"])
+    x = w.state()
+    d = x[:, None, :] - x[None, :, :]
+    d -= L * np.round(d / L)
+    r2 = (d ** 2).sum(-1)
+    np.fill_diagonal(r2, np.inf)
+    s = np.where(r2 < 2 ** (1 / 3), 1.0 / r2, 0.0)
+    p = (12.0 * (2 * s ** 6 - s ** 3)).sum() / (3 * L ** 3)
+    assert p > 0
+    np.testing.assert_allclose(t.sum(), p, rtol=1e-12)
+    b = w.bins()
+    assert int(np.nonzero(c)[0][0]) == int((w.energy() - b["min"]) / b["width"])
+
+
 def test_max_balls_within(oracle):
     # optsquare.rs:290-322 counts lattice points of its own construction
     assert oracle.max_balls_within(1.3) == 6
