@@ -56,3 +56,43 @@ def lj_configs(oracle, n, radius, seeds):
         assert ok
         out.append(pos)
     return out
+
+
+class OracleView:
+    """An oracle walker seen through the accessors of export.BatchWalker."""
+
+    def __init__(self, walker):
+        self.wk = walker
+        self.cfg = walker.cfg
+        self.system = walker.cfg.system
+        self.n = int(walker.cfg.n)
+        self.radius = float(walker.cfg.radius)
+        self.box = tuple(float(x) for x in walker.cfg.box)
+
+    def bins(self):
+        return self.wk.bins()
+
+    def scalars(self):
+        return self.wk.scalars()
+
+    def state(self):
+        return self.wk.state()
+
+    def wl_hist(self):
+        return self.wk.wl_hist()
+
+    def extra(self):
+        return self.wk.extra() if self.system == 2 else None
+
+
+def read_flow_yaml(path):
+    """Read a file written by export.write_yaml (its values are JSON apart from the
+    YAML spellings of non-finite floats)."""
+    import json
+    out = {}
+    with open(path) as f:
+        for line in f:
+            k, v = line.rstrip("\n").split(": ", 1)
+            v = v.replace("-.inf", "-Infinity").replace(".inf", "Infinity").replace(".nan", "NaN")
+            out[k] = json.loads(v)
+    return out
