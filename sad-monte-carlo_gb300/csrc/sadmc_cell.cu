@@ -90,7 +90,7 @@ struct CellWalker {
       if (uy < 0) { uy += nc[1]; oy = 1; } else if (uy >= nc[1]) { uy -= nc[1]; oy = -1; }
       if (uz < 0) { uz += nc[2]; oz = 1; } else if (uz >= nc[2]) { uz -= nc[2]; oz = -1; }
       const int c = cell_index(ux, uy, uz);
-      const int mm = cnt[c];
+      const int mm = min(cnt[c], bucket);  // counts never exceed the bucket
       for (int q = 0; q < mm; ++q) {
         const int j = atoms[(size_t)c * bucket + q];
         if (j == i) continue;
@@ -127,7 +127,7 @@ struct CellOps {
     if (uy < 0) { uy += cw.nc[1]; oy = 1; } else if (uy >= cw.nc[1]) { uy -= cw.nc[1]; oy = -1; }
     if (uz < 0) { uz += cw.nc[2]; oz = 1; } else if (uz >= cw.nc[2]) { uz -= cw.nc[2]; oz = -1; }
     const int c = cw.cell_index(ux, uy, uz);
-    const int m = cw.cnt[c];
+    const int m = min(cw.cnt[c], cw.bucket);
     const int* list = cw.atoms + (size_t)c * cw.bucket;
     const float sx = (float)ox * cw.L32[0], sy = (float)oy * cw.L32[1], sz = (float)oz * cw.L32[2];
     for (int k = 0; k < m; ++k) {
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
       // ConfirmSystem::confirm -> Cell::move_atom (optcell.rs:162-175)
       if (new_c != old_c) {
         int* lo = cw.atoms + (size_t)old_c * cw.bucket;
-        const int mo = cw.cnt[old_c];
+        const int mo = min(cw.cnt[old_c], cw.bucket);
         int pos = -1;
         for (int k = glane; k < mo; k += LPW)
           if (lo[k] == a) pos = k;

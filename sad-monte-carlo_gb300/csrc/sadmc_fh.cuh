@@ -153,6 +153,13 @@ struct Fh {
   __device__ void sync() {
     if (LPW > 1) __syncwarp(gmask);
   }
+  // Lane 0's value of a predicate for the whole lane group.  Every branch that leads to a
+  // group collective (__syncwarp, shuffles) takes its predicate through here, so the
+  // lanes of a group always reach the same collectives.
+  __device__ bool uni(bool x) const {
+    if (LPW == 1) return x;
+    return __shfl_sync(gmask, (int)x, 0, LPW) != 0;
+  }
   __device__ uint64_t group_min(uint64_t v) const {
 #pragma unroll
     for (int o = LPW / 2; o > 0; o >>= 1) {
@@ -186,6 +193,13 @@ struct Fh {
     gb_valid = false;
     grew_front = false;
     tscale_changed = false;
+    // binary32 shadows of decide_de (each within |x| 2^-23 of its FP64 value)
+    Ef = f32_trunc(c.E);
+    cminf = f32_trunc(c.cur_min);
+    cmaxf = f32_trunc(cur_max);
+    maxf = f32_trunc(max_allowed);
+    minf = f32_trunc(min_allowed);
+    inv_wf = (float)inv_width;
   }
   __device__ void store(WalkerCore* cores, int w) {
     if (c.kind != M_DESCENT) flush_cur();
@@ -306,63 +320,8 @@ struct Fh {
     grew_front = false;
   }
 
-  // Bounds test, prepare_for_state and reject_move (energy.rs:915-931); true = accept.
-  __device__ bool decide(bool possible, double e2, uint64_t u53, double rs) {
-    if (!possible) return false;
-    bool oob = false;
-    if (has_max_allowed) oob = e2 > max_allowed && e2 > c.E;
-    if (has_min_allowed) oob = oob || (e2 < min_allowed && e2 < c.E);
-    if (oob) return false;
-    if (c.kind == M_DESCENT) return e2 < c.E;  // energy.rs:840-851
-    if (!prepare(e2)) { c.status |= ST_BIN_RANGE; return false; }
-    if (grew_front) reindex_after_growth();
-    i2 = gidx(e2);
-    if (i2 < c.b_lo || i2 > c.b_hi) {  // only reachable through rounding at the range edge
-      c.status |= ST_BIN_RANGE;
-      return false;
-    }
-    fetch_pending(i2);
-    const double lnw2_raw = p_lnw;
-    hist2 = p_hist;
-    bool rejected;
-    switch (c.kind) {
-      case M_SAD: {
-        double lnw1 = sad_lnw(c.E, cur);
-        double lnw2 = sad_lnw(e2, i2);
-        rejected = lnw2 > lnw1 && metropolis_reject(lnw1 - lnw2, u53);
-        if (!rejected && hist2 == 0 && !below(e2, i2) && !above(e2, i2) && e2 < c.too_hi &&
-            e2 > c.too_lo) {  // energy.rs:466-483
-          c.latest_param = (c.too_hi - c.too_lo) / c.min_T;
-          c.num_states += 1;
-          c.tL = c.moves;
-          gb_valid = false;
-        }
-        break;
-      }
-      case M_SAMC: {
-        rejected = lnw2_raw > k_lnw && metropolis_reject(k_lnw - lnw2_raw, u53);
-        break;
-      }
-      case M_WL:
-      case M_INV_T_WL: {
-        rejected = lnw2_raw > k_lnw && metropolis_reject(k_lnw - lnw2_raw, u53);
-        if (!rejected && hist2 == 0 && c.lowest_hist > 0) c.wl_num_states += 1.0;
-        break;
-      }
-      default: {  // canonical (energy.rs:504-510)
-        rejected = c.E >= e2 ? false : metropolis_reject((c.E - e2) / c.temperature, u53);
-        break;
-      }
-    }
-    if (!rejected) {
-      c.accepted += 1;
-      c.acc_rate += rs;
-    }
-    return !rejected;
-  }
-
-
-  // The decision of decide() for e2 = E + (double)de with de in binary32.  Each
+  // Bounds test, prepare_for_state and reject_move (energy.rs:915-931) for
+  // e2 = E + (double)de with de in binary32; true = accept.  Each
   // comparison of the reference on e2 is first taken on the binary32 estimate
   // e2f = Ef + de, whose error is below tol (|E - Ef| < |E| 2^-23, one binary32 rounding,
   // one binary64 rounding); inside the bound, or wherever the exact value enters
@@ -371,13 +330,23 @@ struct Fh {
   // has_first: the Metropolis test uses lnw_first in place of ln w(E) -- the second stage
   // of a delayed-acceptance move, which accepts with min(1, exp(ln w(E~) - ln w(e2))) for
   // the surrogate-predicted energy E~.
+  // The group takes lane 0's decision (all lanes hold the same state, so they agree).
   __device__ bool decide_de(bool possible, float de, uint64_t u53, double rs,
                             bool has_first = false, double lnw_first = 0.0) {
-    if (!possible || !(fabsf(de) <= 3.0e38f)) return false;
-    const float e2f = Ef + de;
-    const float tol = (fabsf(Ef) + fabsf(e2f)) * 2.5e-7f + 1e-30f;
     double e2 = 0.0;
     bool have = false;
+    const bool accepted = uni(!rejects(possible, de, u53, has_first, lnw_first, e2, have));
+    if (accepted) {
+      if (c.kind != M_DESCENT) { c.accepted += 1; c.acc_rate += rs; }
+      set_E(have ? e2 : c.E + (double)de);
+    }
+    return accepted;
+  }
+  __device__ bool rejects(bool possible, float de, uint64_t u53, bool has_first,
+                          double lnw_first, double& e2, bool& have) {
+    if (!possible || !(fabsf(de) <= 3.0e38f)) return true;
+    const float e2f = Ef + de;
+    const float tol = (fabsf(Ef) + fabsf(e2f)) * 2.5e-7f + 1e-30f;
     auto exact = [&]() -> double {
       if (!have) { e2 = c.E + (double)de; have = true; }
       return e2;
@@ -404,11 +373,11 @@ struct Fh {
     bool oob = false;
     if (has_max_allowed) oob = gt(maxf, max_allowed) && gtE();
     if (has_min_allowed) oob = oob || (lt(minf, min_allowed) && ltE());
-    if (oob) return false;
-    if (c.kind == M_DESCENT) return ltE();
+    if (oob) return true;
+    if (c.kind == M_DESCENT) return !ltE();
     // prepare_for_state: only when e2 may lie outside [cur_min, cur_max)
     if (lt(cminf, c.cur_min) || !lt(cmaxf, cur_max)) {
-      if (!prepare(exact())) { c.status |= ST_BIN_RANGE; return false; }
+      if (!prepare(exact())) { c.status |= ST_BIN_RANGE; return true; }
       if (grew_front) reindex_after_growth();
     }
     // state_to_index
@@ -423,7 +392,7 @@ struct Fh {
     }
     if (i2 < c.b_lo || i2 > c.b_hi) {
       c.status |= ST_BIN_RANGE;
-      return false;
+      return true;
     }
     fetch_pending(i2);
     const double lnw2_raw = p_lnw;
@@ -463,12 +432,7 @@ struct Fh {
         break;
       }
     }
-    if (!rejected) {
-      c.accepted += 1;
-      c.acc_rate += rs;
-      set_E(exact());
-    }
-    return !rejected;
+    return rejected;
   }
 
   // Histogram, energy sums, update_weights and max-entropy bookkeeping
@@ -588,7 +552,7 @@ struct Fh {
 
   __device__ void wl_update() {  // energy.rs:638-752
     const bool inv_t = c.kind == M_INV_T_WL;
-    if (c.has_min_gamma && c.gamma < c.min_gamma) {  // production run
+    if (uni(c.has_min_gamma && c.gamma < c.min_gamma)) {  // production run
       int k = c.wl_lo + (cur - c.b_lo);
       if (k >= c.wl_lo && k <= c.wl_hi) { if (wr) wlh[k] = wlh[k] + 1; }
       else c.status |= ST_BIN_RANGE;
@@ -596,8 +560,8 @@ struct Fh {
     }
     const int len_b = c.b_hi - c.b_lo + 1;
     int len_w = c.wl_hi >= c.wl_lo ? c.wl_hi - c.wl_lo + 1 : 0;
-    if (len_w != len_b) {
-      if (len_w == 0 || (c.gamma != 1.0 && c.lowest_hist > 0)) {
+    if (uni(len_w != len_b)) {
+      if (uni(len_w == 0 || (c.gamma != 1.0 && c.lowest_hist > 0))) {
         c.gamma = 1.0;
         c.lowest_hist = 0;
         c.wl_highest_hist = 0;
@@ -638,7 +602,7 @@ struct Fh {
     bool cond = h == c.lowest_hist + 1 && len_w > 1 &&
                 (!has_min_allowed || min_allowed >= c.min_energy) &&
                 (!has_max_allowed || max_allowed <= max_energy);
-    if (cond) {
+    if (uni(cond)) {
       sync();
       uint64_t mn = ~0ull;
       for (int j = glane; j < len_w; j += LPW) {
@@ -650,7 +614,7 @@ struct Fh {
       mn = group_min(mn);
       cond = mn == c.lowest_hist + 1;
     }
-    if (cond) {
+    if (uni(cond)) {
       c.lowest_hist = h;
       if ((inv_t && c.lowest_hist > 0) ||
           (double)c.lowest_hist >= 0.8 * (double)c.total_hist / c.wl_num_states) {
