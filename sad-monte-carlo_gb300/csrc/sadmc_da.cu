@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
     const double lnw_cur = fh.lnw_current();
     const double lnw_til = fh.lnw_at(e_til);
     const bool uphill1 = dgt(lnw_til, lnw_cur);
-    const bool rej1 = uphill1 && metropolis_reject(lnw_cur - lnw_til, d.u53);
+    const bool rej1 = fh.uni(uphill1 && metropolis_reject(lnw_cur - lnw_til, d.u53));
     // a certain stage-1 acceptance consumed no randomness: stage 2 may use the move's own
     // uniform (with a constant surrogate the chain is then the plain chain, bit for bit)
     const uint64_t u_second = uphill1 ? u2 : d.u53;

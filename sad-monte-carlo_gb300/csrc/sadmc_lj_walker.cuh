@@ -85,13 +85,19 @@ struct LjWalker {
     }
     if (impossible) return false;
     float de = 0.0f;
+    // Differences of double-single positions: the high parts of two nearby atoms subtract
+    // exactly (Sterbenz), so close pairs keep their full relative precision in r^2.
 #pragma unroll
     for (int k = 0; k < APL; ++k) {
       const int j = glane + LPW * k;
       if (j < n && j != which) {
-        float dx = x[k].h - tx.h, dy = y[k].h - ty.h, dz = z[k].h - tz.h;
+        float dx = (x[k].h - tx.h) + (x[k].l - tx.l);
+        float dy = (y[k].h - ty.h) + (y[k].l - ty.l);
+        float dz = (z[k].h - tz.h) + (z[k].l - tz.l);
         float vn = lj_v32(dx * dx + dy * dy + dz * dz);
-        dx = x[k].h - fx.h; dy = y[k].h - fy.h; dz = z[k].h - fz.h;
+        dx = (x[k].h - fx.h) + (x[k].l - fx.l);
+        dy = (y[k].h - fy.h) + (y[k].l - fy.l);
+        dz = (z[k].h - fz.h) + (z[k].l - fz.l);
         float vo = lj_v32(dx * dx + dy * dy + dz * dz);
         de += vn - vo;
       }

@@ -90,7 +90,7 @@ def test_wca_pressure_channel(gpu, oracle, lpw):
                                               translation_scale=0.1, seed=seed, walker=w,
                                               e0=float(E0[w])), pos)
         disc, mismatch = ow.run_override(e1, e2)
-        assert mismatch == 0 and disc < 2e-5, (w, mismatch, disc)
+        assert mismatch == 0 and disc < 2e-5, (w, mismatch, disc, ow.override_worst())
         gc, gt = b.extra(w)
         oc, ot = ow.extra()
         assert int(gc.sum()) == moves // (n * n), (w, gc.sum())
@@ -136,5 +136,6 @@ def test_wca_uneven_trace_replay(gpu, oracle, lpw):
         assert_bins_equal(b.bins(w), ow.bins(), label=label)
         assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
         np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-12)
-    np.testing.assert_allclose(b.energies(), b.compute_energies(), atol=1e-3)
+    # incremental binary32 dE since the last FP64 re-sum (500 moves) vs the FP64 re-sum
+    np.testing.assert_allclose(b.energies(), b.compute_energies(), atol=1e-3, rtol=2e-6)
     assert not (b.status() & ~np.uint32(gpu.ST_DESCENT_FAILED)).any()
