@@ -118,8 +118,8 @@ void* orc_create(const orc_config* c, const double* state) {
     s.E = s.compute_energy();
     uint32_t L = (uint32_t)c->n;
     h->ising.reset(new EnergyMC<Ising>());
-    h->ising->init(std::move(s), p, [seed, walker, L](uint64_t t, uint32_t) {
-      return draws_ising(seed, walker, t, L);
+    h->ising->init(std::move(s), p, [seed, walker, L](uint64_t t, uint32_t stream) {
+      return draws_ising(seed, walker, t, L, stream);
     }, dl);
   } else {
     uint32_t n = (uint32_t)c->n;

@@ -148,10 +148,12 @@ inline Draws draws_continuous(uint64_t seed, uint32_t walker, uint64_t t, uint32
   return d;
 }
 
-inline Draws draws_ising(uint64_t seed, uint32_t walker, uint64_t t, uint32_t L) {
+// stream_pair 0: moves; 1: the initial descent (counter word 2 = 2 * stream_pair).
+inline Draws draws_ising(uint64_t seed, uint32_t walker, uint64_t t, uint32_t L,
+                         uint32_t stream_pair = 0) {
   uint32_t k0 = walker, k1 = (uint32_t)seed;
   uint32_t shi = (uint32_t)(seed >> 32);
-  U4 A = philox4x32_10(U4{(uint32_t)t, (uint32_t)(t >> 32), 0u, shi}, k0, k1);
+  U4 A = philox4x32_10(U4{(uint32_t)t, (uint32_t)(t >> 32), 2u * stream_pair, shi}, k0, k1);
   Draws d;
   d.which = mulhi_range(A.x, L);
   d.j = mulhi_range(A.y, L);

@@ -562,7 +562,7 @@ int32_t sadmc_initialize(sadmc_handle* h) {
   CUDA_TRY(cudaMemcpyAsync(E.data(), h->d_tmp, sizeof(double) * h->W, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   for (int w = 0; w < h->W; ++w) h->h_cores[w].E = E[w];
-  if (c.has_max_allowed && c.system == SADMC_LJ) {
+  if (c.has_max_allowed) {
     // from_params descent (energy.rs:840-851)
     r = h->push_cores();
     if (r) return r;
@@ -582,6 +582,17 @@ int32_t sadmc_initialize(sadmc_handle* h) {
         if (!(h->h_cores[w].E < c.max_allowed) && h->h_cores[w].pad2 < m.descent_limit) all = false;
       if (all) break;
       left -= m.n_moves;
+    }
+    if (c.system != SADMC_LJ) {
+      // the descent accumulated energy changes; start from the FP64 energy of the result
+      // (the LJ kernel re-sums itself)
+      CUDA_TRY(h->launch_energy(h->d_tmp));
+      CUDA_TRY(cudaMemcpyAsync(E.data(), h->d_tmp, sizeof(double) * h->W, cudaMemcpyDeviceToHost, h->stream));
+      CUDA_TRY(cudaStreamSynchronize(h->stream));
+      for (int w = 0; w < h->W; ++w) {
+        h->h_cores[w].E = E[w];
+        if (!(E[w] < c.max_allowed)) h->h_cores[w].status |= ST_DESCENT_FAILED;
+      }
     }
   }
   // EnergyMC fields (energy.rs:852-898) and Method::new (energy.rs:247-313)

@@ -74,16 +74,15 @@ struct CellWalker {
   int nc[3];
   int np, bucket;
   __device__ int cell_index(int x, int y, int z) const { return (x * nc[1] + y) * nc[2] + z; }
-  // FP64 sum of f(|r_i - r_j|^2) over the candidates j != i of atom i in its 27
-  // subcells, with the reference's periodic image offsets (the
-  // maybe_interacting_atoms_excluding loops of wca.rs:202-218 and 222-230).
+  // FP64 sum of f(|q - r_j|^2) over the candidates j != skip in the 27 subcells around
+  // subcell (cx, cy, cz), with the reference's periodic image offsets (the
+  // maybe_interacting_atoms_excluding loops of wca.rs:202-218 and 222-230); neighbour
+  // subcells k0 = k_first, k_first + k_step, ... (a lane's share).
   template <class F>
-  __device__ double pair_sum64(int i, F f) const {
-    const double ix = p[i], iy = p[np + i], iz = p[2 * np + i];
-    const int ci = cell_of[i];
-    const int cx = ci / (nc[1] * nc[2]), cy = (ci / nc[2]) % nc[1], cz = ci % nc[2];
+  __device__ double near_sum64(double qx, double qy, double qz, int cx, int cy, int cz, int skip,
+                               F f, int k_first, int k_step) const {
     double e = 0.0;
-    for (int k0 = 0; k0 < 27; ++k0) {
+    for (int k0 = k_first; k0 < 27; k0 += k_step) {
       const int dx = k0 / 9 - 1, dy = (k0 / 3) % 3 - 1, dz = k0 % 3 - 1;
       int ux = cx + dx, uy = cy + dy, uz = cz + dz, ox = 0, oy = 0, oz = 0;
       if (ux < 0) { ux += nc[0]; ox = 1; } else if (ux >= nc[0]) { ux -= nc[0]; ox = -1; }
@@ -93,14 +92,21 @@ struct CellWalker {
       const int mm = min(cnt[c], bucket);  // counts never exceed the bucket
       for (int q = 0; q < mm; ++q) {
         const int j = atoms[(size_t)c * bucket + q];
-        if (j == i) continue;
-        const double bx = (p[j] - (double)ox * L[0]) - ix;
-        const double by = (p[np + j] - (double)oy * L[1]) - iy;
-        const double bz = (p[2 * np + j] - (double)oz * L[2]) - iz;
+        if (j == skip) continue;
+        const double bx = (p[j] - (double)ox * L[0]) - qx;
+        const double by = (p[np + j] - (double)oy * L[1]) - qy;
+        const double bz = (p[2 * np + j] - (double)oz * L[2]) - qz;
         e += f(bx * bx + by * by + bz * bz);
       }
     }
     return e;
+  }
+  // The same sum for atom i over all 27 subcells around its own.
+  template <class F>
+  __device__ double pair_sum64(int i, F f) const {
+    const int ci = cell_of[i];
+    return near_sum64(p[i], p[np + i], p[2 * np + i], ci / (nc[1] * nc[2]), (ci / nc[2]) % nc[1],
+                      ci % nc[2], i, f, 0, 1);
   }
 };
 
@@ -188,6 +194,134 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
   const double rc = s.r_cut;
   const double wsqr = rc * rc;
   const float wsqr32 = (float)wsqr;
+
+  // plan_move: put_in_cell(from + g * scale) (optsquare.rs:273-284, wca.rs:342-353) and the
+  // energy change over the 27 subcells around the old and the new position.
+  struct Prop {
+    int a, old_c, new_c, new_count;
+    double fx, fy, fz, tx, ty, tz;
+    float t32x, t32y, t32z, de;
+    bool possible;
+  };
+  auto plan = [&](int a, float g0, float g1, float g2, double sc) {
+    Prop p;
+    p.a = a;
+    p.fx = cw.p[a]; p.fy = cw.p[s.np + a]; p.fz = cw.p[2 * s.np + a];
+    bool bad = false;
+    p.tx = wrap_axis(p.fx + (double)g0 * sc, cw.L[0], &bad);
+    p.ty = wrap_axis(p.fy + (double)g1 * sc, cw.L[1], &bad);
+    p.tz = wrap_axis(p.fz + (double)g2 * sc, cw.L[2], &bad);
+    const int nx = subcell_axis(p.tx, cw.L[0], cw.nc[0]);
+    const int ny = subcell_axis(p.ty, cw.L[1], cw.nc[1]);
+    const int nz = subcell_axis(p.tz, cw.L[2], cw.nc[2]);
+    p.old_c = cw.cell_of[a];
+    const int ocx = p.old_c / (cw.nc[1] * cw.nc[2]), ocy = (p.old_c / cw.nc[2]) % cw.nc[1],
+              ocz = p.old_c % cw.nc[2];
+    p.t32x = (float)p.tx; p.t32y = (float)p.ty; p.t32z = (float)p.tz;
+    const float4 f32 = cw.p32[a];
+    int cn = 0, co = 0;
+    bool overlap = false;
+    float en = 0.0f, eo = 0.0f;
+    for (int k = glane; k < 54; k += LPW) {
+      if (k < 27)
+        CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, p.tx, p.ty, p.tz, p.t32x, p.t32y, p.t32z, a,
+                                 wsqr, wsqr32, true, cn, overlap, en, wsqr32);
+      else
+        CellOps<LPW, KIND>::scan(cw, k - 27, ocx, ocy, ocz, p.fx, p.fy, p.fz, f32.x, f32.y, f32.z,
+                                 a, wsqr, wsqr32, false, co, overlap, eo, wsqr32);
+    }
+    p.new_c = cw.cell_index(nx, ny, nz);
+    if (KIND == SYS_SW) {
+      // e = E - (contacts at the new position) + (contacts at the old position); the
+      // FP64 sequence of unit steps of optsquare.rs:75-92 is exact on integers, and so
+      // is the binary32 difference of the two counts
+      const int newc = group_sum<LPW>(cn, gmask);
+      const int oldc = group_sum<LPW>(co, gmask);
+      p.possible = !__any_sync(gmask, overlap);
+      p.de = (float)(oldc - newc);
+    } else {
+      p.de = group_sum<LPW>(en - eo, gmask);
+      p.possible = true;
+    }
+    p.possible = p.possible && !bad && fabsf(p.de) <= 3.0e38f;
+    p.new_count = cw.cnt[p.new_c];
+    if (p.possible && p.new_c != p.old_c && p.new_count >= cw.bucket) {
+      p.possible = false;
+      fh.c.status |= ST_CELL_OVERFLOW;
+    }
+    return p;
+  };
+  // ConfirmSystem::confirm -> Cell::move_atom (optcell.rs:162-175)
+  auto apply = [&](const Prop& p) {
+    const int a = p.a;
+    if (p.new_c != p.old_c) {
+      int* lo = cw.atoms + (size_t)p.old_c * cw.bucket;
+      const int mo = min(cw.cnt[p.old_c], cw.bucket);
+      int pos = -1;
+      for (int k = glane; k < mo; k += LPW)
+        if (lo[k] == a) pos = k;
+      for (int o = LPW / 2; o > 0; o >>= 1) {
+        int x = __shfl_xor_sync(gmask, pos, o, LPW);
+        pos = x > pos ? x : pos;
+      }
+      __syncwarp(gmask);
+      if (wr && pos >= 0) {
+        lo[pos] = lo[mo - 1];
+        cw.cnt[p.old_c] = mo - 1;
+        cw.atoms[(size_t)p.new_c * cw.bucket + p.new_count] = a;
+        cw.cnt[p.new_c] = p.new_count + 1;
+        cw.cell_of[a] = p.new_c;
+      }
+    }
+    if (wr) {
+      cw.p[a] = p.tx; cw.p[s.np + a] = p.ty; cw.p[2 * s.np + a] = p.tz;
+      cw.p32[a] = make_float4(p.t32x, p.t32y, p.t32z, 0.0f);
+    }
+    __syncwarp(gmask);
+  };
+
+  if (m.descent) {
+    // from_params descent (energy.rs:840-851): proposals of rms 0.05 on the descent stream,
+    // confirmed when downhill; after every possible proposal the energy is tested against
+    // max_allowed_energy (so at least one proposal is made).  WCA energy changes are the
+    // FP64 one-atom sums here; square-well changes are exact integers.
+    bool done = fh.c.pad1 != 0;
+    uint64_t steps = fh.c.pad2;
+    for (uint64_t it = 0; it < m.n_moves; ++it) {
+      if (__all_sync(0xffffffffu, done)) break;
+      if (!done) {
+        ++steps;
+        const Draws d = draws_continuous(m.seed, (uint32_t)w, steps, (uint32_t)n, 1u);
+        const Prop p = plan((int)d.which, d.g0, d.g1, d.g2, 0.05);
+        if (p.possible) {
+          double de = (double)p.de;
+          if (KIND == SYS_WCA) {
+            const int ci = p.new_c;
+            const int nx = ci / (cw.nc[1] * cw.nc[2]), ny = (ci / cw.nc[2]) % cw.nc[1], nz = ci % cw.nc[2];
+            const int oc = p.old_c;
+            const int ox = oc / (cw.nc[1] * cw.nc[2]), oy = (oc / cw.nc[2]) % cw.nc[1], oz = oc % cw.nc[2];
+            auto v64 = [&](double r2) { return wca_v64(r2, wsqr); };
+            double part = cw.near_sum64(p.tx, p.ty, p.tz, nx, ny, nz, p.a, v64, glane, LPW) -
+                          cw.near_sum64(p.fx, p.fy, p.fz, ox, oy, oz, p.a, v64, glane, LPW);
+            de = group_sum<LPW>(part, gmask);
+          }
+          const double e2 = fh.c.E + de;
+          if (fh.uni(e2 < fh.c.E)) {
+            apply(p);
+            fh.c.E = e2;
+          }
+          if (fh.c.E < m.descent_max) done = true;
+        }
+        if (steps >= m.descent_limit) done = true;
+        done = fh.uni(done);
+      }
+    }
+    fh.c.pad2 = steps;
+    fh.c.pad1 = done ? 1 : 0;
+    if (wr && glane == 0) m.cores[w] = fh.c;  // the host re-sums E in FP64 afterwards
+    return;
+  }
+
   RecentScale rsb;
   rsb.init();
   DrawCache<LPW, false> dc;
@@ -198,87 +332,15 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
     rsb.get(t, lane, rs, omrs);
     fh.begin_move(omrs);
     const Draws d = dc.get(m.seed, (uint32_t)w, t, (uint32_t)n, gmask, glane);
-    const int a = (int)d.which;
-    const double sc = fh.c.tscale;
-    const double fx = cw.p[a], fy = cw.p[s.np + a], fz = cw.p[2 * s.np + a];
-    bool bad = false;
-    // plan_move: put_in_cell(from + g * scale) (optsquare.rs:273-284, wca.rs:342-353)
-    const double tx = wrap_axis(fx + (double)d.g0 * sc, cw.L[0], &bad);
-    const double ty = wrap_axis(fy + (double)d.g1 * sc, cw.L[1], &bad);
-    const double tz = wrap_axis(fz + (double)d.g2 * sc, cw.L[2], &bad);
-    const int nx = subcell_axis(tx, cw.L[0], cw.nc[0]);
-    const int ny = subcell_axis(ty, cw.L[1], cw.nc[1]);
-    const int nz = subcell_axis(tz, cw.L[2], cw.nc[2]);
-    const int old_c = cw.cell_of[a];
-    const int ocx = old_c / (cw.nc[1] * cw.nc[2]), ocy = (old_c / cw.nc[2]) % cw.nc[1], ocz = old_c % cw.nc[2];
-    const float t32x = (float)tx, t32y = (float)ty, t32z = (float)tz;
-    const float4 f32 = cw.p32[a];
-    int cn = 0, co = 0;
-    bool overlap = false;
-    float en = 0.0f, eo = 0.0f;
-    for (int k = glane; k < 54; k += LPW) {
-      if (k < 27)
-        CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, tx, ty, tz, t32x, t32y, t32z, a, wsqr, wsqr32,
-                                 true, cn, overlap, en, wsqr32);
-      else
-        CellOps<LPW, KIND>::scan(cw, k - 27, ocx, ocy, ocz, fx, fy, fz, f32.x, f32.y, f32.z, a,
-                                 wsqr, wsqr32, false, co, overlap, eo, wsqr32);
-    }
-    const int new_c = cw.cell_index(nx, ny, nz);
-    bool possible;
-    float de;
-    if (KIND == SYS_SW) {
-      // e = E - (contacts at the new position) + (contacts at the old position); the
-      // FP64 sequence of unit steps of optsquare.rs:75-92 is exact on integers, and so
-      // is the binary32 difference of the two counts
-      const int newc = group_sum<LPW>(cn, gmask);
-      const int oldc = group_sum<LPW>(co, gmask);
-      possible = !__any_sync(gmask, overlap);
-      de = (float)(oldc - newc);
-    } else {
-      de = group_sum<LPW>(en - eo, gmask);
-      possible = true;
-    }
-    possible = possible && !bad && fabsf(de) <= 3.0e38f;
-    const int new_count = cw.cnt[new_c];
-    if (possible && new_c != old_c && new_count >= cw.bucket) {
-      possible = false;
-      fh.c.status |= ST_CELL_OVERFLOW;
-    }
+    const Prop p = plan((int)d.which, d.g0, d.g1, d.g2, fh.c.tscale);
     if (m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
       TraceRec r;
       r.e1 = fh.c.E;
-      r.e2 = possible ? fh.c.E + (double)de : __longlong_as_double(0x7ff8000000000000ll);
+      r.e2 = p.possible ? fh.c.E + (double)p.de : __longlong_as_double(0x7ff8000000000000ll);
       m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = r;
     }
-    const bool acc = fh.decide_de(possible, de, d.u53, rs);
-    if (acc) {
-      // ConfirmSystem::confirm -> Cell::move_atom (optcell.rs:162-175)
-      if (new_c != old_c) {
-        int* lo = cw.atoms + (size_t)old_c * cw.bucket;
-        const int mo = min(cw.cnt[old_c], cw.bucket);
-        int pos = -1;
-        for (int k = glane; k < mo; k += LPW)
-          if (lo[k] == a) pos = k;
-        for (int o = LPW / 2; o > 0; o >>= 1) {
-          int x = __shfl_xor_sync(gmask, pos, o, LPW);
-          pos = x > pos ? x : pos;
-        }
-        __syncwarp(gmask);
-        if (wr && pos >= 0) {
-          lo[pos] = lo[mo - 1];
-          cw.cnt[old_c] = mo - 1;
-          cw.atoms[(size_t)new_c * cw.bucket + new_count] = a;
-          cw.cnt[new_c] = new_count + 1;
-          cw.cell_of[a] = new_c;
-        }
-      }
-      if (wr) {
-        cw.p[a] = tx; cw.p[s.np + a] = ty; cw.p[2 * s.np + a] = tz;
-        cw.p32[a] = make_float4(t32x, t32y, t32z, 0.0f);
-      }
-      __syncwarp(gmask);
-    }
+    const bool acc = fh.decide_de(p.possible, p.de, d.u53, rs);
+    if (acc) apply(p);
     fh.finish_move(acc);
     if (KIND == SYS_WCA && m.B.ex_count && (t % ((uint64_t)n * (uint64_t)n)) == 0) {
       // the "pressure" datum every N^2 moves into the current bin (wca.rs:202-218,

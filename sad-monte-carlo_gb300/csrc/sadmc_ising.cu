@@ -29,6 +29,38 @@ __global__ void __launch_bounds__(128) ising_move_kernel(MoveLaunch m, IsingSys 
   fh.load(m.cores, m.P, m.B, w, gmask, glane, wr);
   const int L = s.L;
   int8_t* S = s.spins + (size_t)w * (size_t)L * (size_t)L;
+  if (m.descent) {
+    // from_params descent (energy.rs:840-851): flips on the descent stream, confirmed when
+    // downhill, the energy tested against max_allowed_energy after each (so at least one
+    // proposal is made); energies are exact integers.
+    bool done = fh.c.pad1 != 0;
+    uint64_t steps = fh.c.pad2;
+    for (uint64_t it = 0; it < m.n_moves; ++it) {
+      if (__all_sync(0xffffffffu, done)) break;
+      if (!done) {
+        ++steps;
+        const Draws d = draws_ising(m.seed, (uint32_t)w, steps, (uint32_t)L, 1u);
+        const int i = (int)d.which, j = (int)d.j;
+        const int jp = j + 1 == L ? 0 : j + 1, jm = j == 0 ? L - 1 : j - 1;
+        const int ip = i + 1 == L ? 0 : i + 1, im = i == 0 ? L - 1 : i - 1;
+        const int nt = S[i + jp * L] + S[i + jm * L] + S[ip + j * L] + S[im + j * L];
+        const int sij = S[i + j * L];
+        const double e2 = fh.c.E - (double)(nt * sij * 2);
+        if (fh.uni(e2 < fh.c.E)) {
+          if (wr) S[i + j * L] = (int8_t)(-sij);
+          if (LPW > 1) __syncwarp(gmask);
+          fh.c.E = e2;
+        }
+        if (fh.c.E < m.descent_max) done = true;
+        if (steps >= m.descent_limit) done = true;
+        done = fh.uni(done);
+      }
+    }
+    fh.c.pad2 = steps;
+    fh.c.pad1 = done ? 1 : 0;
+    if (wr && glane == 0) m.cores[w] = fh.c;
+    return;
+  }
   RecentScale rsb;
   rsb.init();
   DrawCache<LPW, true> dc;
