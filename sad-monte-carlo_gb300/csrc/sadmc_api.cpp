@@ -211,6 +211,7 @@ struct sadmc_handle {
   MoveLaunch base_launch() const {
     MoveLaunch m{};
     m.cores = d_cores;
+    m.method = cfg.method;
     m.P = fh_params();
     m.B = planes;
     m.n_walkers = W;

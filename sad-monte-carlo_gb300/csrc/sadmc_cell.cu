@@ -326,6 +326,9 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
   rsb.init();
   DrawCache<LPW, false> dc;
   dc.init();
+  Every resum, datum;
+  resum.init(fh.c.moves, KIND == SYS_WCA && m.resum_interval > 0 ? (uint64_t)m.resum_interval : 0);
+  datum.init(fh.c.moves, KIND == SYS_WCA && m.B.ex_count ? (uint64_t)n * (uint64_t)n : 0);
   for (uint64_t it = 0; it < m.n_moves; ++it) {
     const uint64_t t = fh.c.moves + 1;
     double rs, omrs;
@@ -342,7 +345,7 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
     const bool acc = fh.decide_de(p.possible, p.de, d.u53, rs);
     if (acc) apply(p);
     fh.finish_move(acc);
-    if (KIND == SYS_WCA && m.B.ex_count && (t % ((uint64_t)n * (uint64_t)n)) == 0) {
+    if (datum.tick()) {
       // the "pressure" datum every N^2 moves into the current bin (wca.rs:202-218,
       // collected and binned as in energy.rs:944-946 and 374-386)
       double pv = 0.0;
@@ -355,7 +358,7 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
         m.B.ex_total[k] += pv / (3.0 * (cw.L[0] * cw.L[1] * cw.L[2]));
       }
     }
-    if (KIND == SYS_WCA && m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
+    if (resum.tick()) {
       // FP64 re-sum (wca.rs:222-230)
       double e = 0.0;
       for (int i = glane; i < n; i += LPW)

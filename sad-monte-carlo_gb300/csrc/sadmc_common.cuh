@@ -61,6 +61,22 @@ __device__ __forceinline__ int group_sum(int v, unsigned gmask) {
   return v;
 }
 
+// "t % period == 0" for the move counter t = moves + 1, moves + 2, ... of one launch, as a
+// countdown: one 64-bit remainder per launch instead of one per move.  period 0: never.
+struct Every {
+  uint32_t left, period;
+  __device__ void init(uint64_t moves, uint64_t period_) {
+    period = (uint32_t)period_;
+    left = period ? period - (uint32_t)(moves % period_) : 0u;
+  }
+  // call once per move, after the move counter advanced
+  __device__ bool tick() {
+    if (period == 0) return false;
+    if (--left == 0) { left = period; return true; }
+    return false;
+  }
+};
+
 // Rust's powi(6) / powi(3) as LLVM expands them (x2 = x*x; x6 = (x2*x2)*x2; x3 = x*x2).
 __device__ __forceinline__ double powi6(double x) { double x2 = x * x; return (x2 * x2) * x2; }
 __device__ __forceinline__ double powi3(double x) { return x * (x * x); }

@@ -106,6 +106,9 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
   dc.init();
   DS sc = ds_from_double(fh.c.tscale);
   uint64_t screened_out = 0, exact_evals = 0;
+  Every resum, refresh_every;
+  resum.init(fh.c.moves, m.resum_interval > 0 ? (uint64_t)m.resum_interval : 0);
+  refresh_every.init(fh.c.moves, refresh_interval > 0 ? (uint64_t)refresh_interval : 0);
   for (uint64_t it = 0; it < m.n_moves; ++it) {
     const uint64_t t = fh.c.moves + 1;
     double rs, omrs;
@@ -197,7 +200,7 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
     }
     fh.finish_move(acc);
     if (fh.tscale_changed) { fh.tscale_changed = false; sc = ds_from_double(fh.c.tscale); }
-    if (m.resum_interval > 0 && (t % (uint64_t)m.resum_interval) == 0) {
+    if (resum.tick()) {
       const double e64 = lj.energy64();
       const double dr = fabs(e64 - fh.c.E);
       if (dr > fh.c.drift) fh.c.drift = dr;
@@ -210,7 +213,7 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
         fh.move_cur(fh.gidx(e64));
       }
     }
-    if (refresh_interval > 0 && (t % (uint64_t)refresh_interval) == 0) refresh();
+    if (refresh_every.tick()) refresh();
   }
   lj.store(pw, s.np, true);
   fh.store(m.cores, w);

@@ -63,7 +63,11 @@ __device__ __forceinline__ bool dgt(double x, double y) {
   return x > y;
 }
 
-template <int LPW>
+// FAM: the method a kernel is specialised for (M_SAD, ...), or FAM_ANY for the kind held
+// in each walker's state (WL and 1/t-WL, whose walkers switch to SAMC at run time).
+constexpr int FAM_ANY = -1;
+
+template <int LPW, int FAM = FAM_ANY>
 struct Fh {
   WalkerCore c;
   // launch constants
@@ -156,6 +160,8 @@ struct Fh {
   // Lane 0's value of a predicate for the whole lane group.  Every branch that leads to a
   // group collective (__syncwarp, shuffles) takes its predicate through here, so the
   // lanes of a group always reach the same collectives.
+  // the method: a compile-time constant in a specialised kernel (dead paths vanish)
+  __device__ int kind() const { return FAM >= 0 ? FAM : (int)c.kind; }
   __device__ bool uni(bool x) const {
     if (LPW == 1) return x;
     return __shfl_sync(gmask, (int)x, 0, LPW) != 0;
@@ -185,7 +191,7 @@ struct Fh {
     cur_max = c.cur_min + width * (double)(c.b_hi - c.b_lo + 1);
     if (c.kind != M_DESCENT) {
       load_cur(gidx_exact(c.E));
-      if (c.kind == M_SAD) { win_lo = gidx_exact(c.too_lo); win_hi = gidx_exact(c.too_hi); }
+      if (kind() == M_SAD) { win_lo = gidx_exact(c.too_lo); win_hi = gidx_exact(c.too_hi); }
     } else {
       cur = -1;
     }
@@ -208,7 +214,7 @@ struct Fh {
 
   // ---- gamma (energy.rs:799-825; SadVersion::compute_gamma energy.rs:22-38) -----------
   __device__ double gamma_at(uint64_t t) const {
-    switch (c.kind) {
+    switch (kind()) {
       case M_SAD: {
         double p = c.latest_param, tF = (double)c.tF, ns = (double)c.num_states;
         if (p * tF * ns == 0.0) return 0.0;
@@ -227,7 +233,7 @@ struct Fh {
   // gamma(gb_base + glane + LPW*q) sits in gb_val[q]; four independent divide chains per
   // lane hide the FP64 divide latency and cover 4*LPW moves per evaluation.
   __device__ double gamma() {
-    if (c.kind != M_SAD && c.kind != M_SAMC) return gamma_at(c.moves);
+    if (kind() != M_SAD && kind() != M_SAMC) return gamma_at(c.moves);
     if (!gb_valid || c.moves < gb_base || c.moves - gb_base >= (uint64_t)(4 * LPW)) {
       gb_base = c.moves;
 #pragma unroll
@@ -271,7 +277,7 @@ struct Fh {
   // bins.min; refresh the cached indices the same way.
   __device__ void reindex_after_growth() {
     move_cur(gidx_exact(c.E));
-    if (c.kind == M_SAD) { win_lo = gidx_exact(c.too_lo); win_hi = gidx_exact(c.too_hi); }
+    if (kind() == M_SAD) { win_lo = gidx_exact(c.too_lo); win_hi = gidx_exact(c.too_hi); }
   }
 
   // e < too_lo and e > too_hi from the bin index g of e: the index is monotone in e, so
@@ -301,7 +307,7 @@ struct Fh {
     if (e < c.cur_min) g = c.b_lo - 1;
     else if (e >= cur_max) g = c.b_hi + 1;
     else g = gidx_exact(e);
-    if (c.kind == M_SAD) {
+    if (kind() == M_SAD) {
       if (e < c.too_lo) return ld_lnw(win_lo) + (e - c.too_lo) / c.min_T;
       if (e > c.too_hi) return ld_lnw(win_hi);
     }
@@ -309,7 +315,7 @@ struct Fh {
     return ld_lnw(g);
   }
   __device__ double lnw_current() const {
-    return c.kind == M_SAD ? sad_lnw(c.E, cur) : k_lnw;
+    return kind() == M_SAD ? sad_lnw(c.E, cur) : k_lnw;
   }
 
   // ---- one move ----------------------------------------------------------------------
@@ -398,7 +404,7 @@ struct Fh {
     const double lnw2_raw = p_lnw;
     hist2 = p_hist;
     bool rejected;
-    switch (c.kind) {
+    switch (kind()) {
       case M_SAD: {
         const double lnw1 = has_first ? lnw_first : sad_lnw(c.E, cur);
         if (i2 <= win_lo || i2 >= win_hi) exact();  // extrapolation / edge comparisons
@@ -444,7 +450,7 @@ struct Fh {
     const double E = c.E;
     if (k_hist == 0) {  // energy.rs:938-940
       k_tf = c.moves;
-      if (c.kind == M_SAD && cur >= win_lo && cur <= win_hi && c.moves > c.win_tmax) c.win_tmax = c.moves;
+      if (kind() == M_SAD && cur >= win_lo && cur <= win_hi && c.moves > c.win_tmax) c.win_tmax = c.moves;
     }
     k_hist += 1;
     k_sE += E;
@@ -470,8 +476,8 @@ struct Fh {
     if (g != g) c.status |= ST_NAN_GAMMA;
     double old = k_lnw;
     k_lnw += g;
-    if (c.kind == M_SAD) sad_update(energy, old);
-    else if (c.kind == M_WL || c.kind == M_INV_T_WL) wl_update();
+    if (kind() == M_SAD) sad_update(energy, old);
+    else if (kind() == M_WL || kind() == M_INV_T_WL) wl_update();
   }
 
   __device__ void sad_update(double energy, double old_lnw) {  // energy.rs:523-636
@@ -551,7 +557,7 @@ struct Fh {
   }
 
   __device__ void wl_update() {  // energy.rs:638-752
-    const bool inv_t = c.kind == M_INV_T_WL;
+    const bool inv_t = kind() == M_INV_T_WL;
     if (uni(c.has_min_gamma && c.gamma < c.min_gamma)) {  // production run
       int k = c.wl_lo + (cur - c.b_lo);
       if (k >= c.wl_lo && k <= c.wl_hi) { if (wr) wlh[k] = wlh[k] + 1; }

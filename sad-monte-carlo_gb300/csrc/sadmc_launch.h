@@ -24,6 +24,7 @@ struct MoveLaunch {
   uint64_t descent_limit;  // maximum descent proposals per walker
   double descent_max;      // max_allowed_energy the descent aims below
   int warps_per_block;     // 1, 2 or 4 (kernels are bounded to 128 threads)
+  int method;              // the configured method (selects a specialised kernel)
 };
 
 // LJ cluster in a spherical wall.  pos: [walker][6][np] binary32 planes
