@@ -212,6 +212,21 @@ int32_t sadmc_surrogate_train(sadmc_handle* h, int32_t steps, int32_t batch, flo
  * without updating the weights (for gradient checks). */
 int32_t sadmc_surrogate_loss_grads(sadmc_handle* h, const float* pos, const float* target,
                                    int32_t configs, double* loss, float* grads);
+/* No counterpart in the reference.  sadmc_surrogate_loss_grads for callers that cannot
+ * call cudaMalloc: a host program whose device memory is all owned by its own pool
+ * allocator (a training framework), or code on a latency-critical stream where an
+ * allocation's implicit device synchronisation would stall the other streams.  Device
+ * pointers in and out, stream-ordered on `stream` (null: the handle's stream), returns
+ * without synchronising.  Allocates nothing: the scratch is a file-scope static device
+ * array of SADMC_SG_NOALLOC_MAX_ROWS rows (configs x atoms); larger requests fail with
+ * SADMC_ERR_INVALID.  *loss is zeroed before it accumulates; grads (SADMC_SG_NPARAM)
+ * are overwritten.  The first call on a device resolves the scratch's address (set-up)
+ * and should come before any stream capture.  Calls overlapping in time on one device
+ * share the scratch and race: serialise them. */
+#define SADMC_SG_NOALLOC_MAX_ROWS 4096
+int32_t sadmc_surrogate_loss_grads_noalloc(sadmc_handle* h, const float* pos,
+                                           const float* target, int32_t configs,
+                                           double* loss, float* grads, void* stream);
 /* `moves` delayed-acceptance moves of every walker (SAD, SAMC or WL; LJ): the surrogate
  * screens each proposal, the exact pair energy decides (Christen & Fox 2005).  Descriptors
  * are rebuilt from scratch every refresh_interval moves (0: never).  stats (optional) gets

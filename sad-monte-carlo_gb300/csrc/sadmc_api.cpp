@@ -1202,6 +1202,26 @@ int32_t sadmc_surrogate_loss_grads(sadmc_handle* h, const float* pos, const floa
   return SADMC_OK;
 }
 
+int32_t sadmc_surrogate_loss_grads_noalloc(sadmc_handle* h, const float* pos, const float* target,
+                                           int32_t configs, double* loss, float* grads,
+                                           void* stream) {
+  if (!h || !pos || !target || !loss || !grads || configs <= 0)
+    return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  const size_t rows = (size_t)configs * (size_t)h->geom[0].n;
+  if (rows > SG_STATIC_ROWS)
+    return fail(SADMC_ERR_INVALID, "configs x atoms exceeds the static scratch of " +
+                                       std::to_string(SG_STATIC_ROWS) + " rows");
+  void* base = nullptr;
+  CUDA_TRY(sg_static_scratch(&base));
+  const SgScratch sc = SgScratch::carve(base, rows);
+  const cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  // step 0: loss (zeroed first) and gradients only, no optimizer state touched
+  CUDA_TRY(sg_train_step(pos, target, configs, h->geom[0].n, h->sg_weights(), h->sg_master,
+                         grads, nullptr, nullptr, 0, 0.0f, sc, loss, st));
+  return SADMC_OK;
+}
+
 int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, uint64_t* stats) {
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
   if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");

@@ -14,6 +14,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "sadmc_common.cuh"
 #include "sadmc_mma.cuh"
 #include "sadmc_surrogate.h"
@@ -276,6 +278,31 @@ cudaError_t sg_forward(const __nv_bfloat16* gq, int rows, const SgWeights& w, fl
   const int tiles = (rows + 15) / 16;
   dev::forward_kernel<<<(tiles + 3) / 4, 128, 0, st>>>(gq, rows, w, e, z1, z2);
   return cudaGetLastError();
+}
+
+namespace {
+// Scratch of sadmc_surrogate_loss_grads_noalloc: SgScratch for SG_STATIC_ROWS rows
+// (about 4.3 MB), one copy per device, never allocated or freed at run time.
+static __device__ __align__(256) unsigned char g_sg_static_scratch[SgScratch::bytes(SG_STATIC_ROWS)];
+constexpr int kStaticDevices = 64;
+std::mutex g_static_mu;
+void* g_static_addr[kStaticDevices] = {};
+}  // namespace
+
+cudaError_t sg_static_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kStaticDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_sg_static_scratch);  // with `dev` current
+    if (e != cudaSuccess) return e;
+    g_static_addr[dev] = p;
+  }
+  *out = g_static_addr[dev];
+  return cudaSuccess;
 }
 
 cudaError_t sg_train_step(const float* pos, const float* target, int configs, int n,

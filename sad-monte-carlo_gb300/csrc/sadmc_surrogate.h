@@ -39,7 +39,7 @@ struct SgScratch {
   float* d1;             // [rows][64]
   float* d2;             // [rows][64]
   // bytes of scratch for `rows` rows
-  static size_t bytes(size_t rows) {
+  static constexpr size_t bytes(size_t rows) {
     return rows * (SG_RBF * 2 + 4 + 4 + 4 * 4 * 64) + 6 * 256;
   }
   static SgScratch carve(void* base, size_t rows) {
@@ -56,6 +56,14 @@ struct SgScratch {
     return s;
   }
 };
+
+// Rows (configurations x atoms) of the file-scope static scratch that serves callers
+// which cannot allocate device memory (sadmc_surrogate_loss_grads_noalloc).
+constexpr size_t SG_STATIC_ROWS = 4096;
+// Device address of that static scratch on the current device.  The first call on a
+// device resolves the symbol (cudaGetSymbolAddress, with the device current) and caches
+// it; later calls on that device only read the cache.
+cudaError_t sg_static_scratch(void** out);
 
 cudaError_t sg_descriptors(const float* pos, int n, int rows, __nv_bfloat16* gq, float* gf,
                            cudaStream_t st);

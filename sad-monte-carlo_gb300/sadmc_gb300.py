@@ -107,6 +107,7 @@ def lib():
         "sadmc_surrogate_collect": (I32, [P, P]),
         "sadmc_surrogate_train": (I32, [P, I32, I32, ctypes.c_float, U64, P]),
         "sadmc_surrogate_loss_grads": (I32, [P, P, P, I32, P, P]),
+        "sadmc_surrogate_loss_grads_noalloc": (I32, [P, P, P, I32, P, P, P]),
         "sadmc_surrogate_predict": (I32, [P, P, I32, P]),
         "sadmc_run_da": (I32, [P, U64, I32, P]),
         "sadmc_draws": (I32, [I32, ctypes.c_uint32, U64, ctypes.c_uint32, U64, I32, ctypes.c_uint32,
@@ -359,6 +360,15 @@ class Batch:
         _check(lib().sadmc_surrogate_loss_grads(self.h, _p(pos), _p(target), len(target),
                                                 ctypes.byref(loss), _p(g)))
         return loss.value, g
+
+    def surrogate_loss_grads_noalloc(self, pos_ptr, target_ptr, configs, loss_ptr, grads_ptr,
+                                     stream_ptr=None):
+        """sadmc_surrogate_loss_grads_noalloc on device pointers (ints): stream-ordered,
+        allocates nothing, returns without synchronising."""
+        _check(lib().sadmc_surrogate_loss_grads_noalloc(
+            self.h, ctypes.c_void_p(pos_ptr), ctypes.c_void_p(target_ptr), int(configs),
+            ctypes.c_void_p(loss_ptr), ctypes.c_void_p(grads_ptr),
+            ctypes.c_void_p(stream_ptr) if stream_ptr else None))
 
     def run_da(self, moves, refresh_interval=2048):
         """Delayed-acceptance moves; returns per-walker (stage-1 rejections, exact evaluations)."""
