@@ -286,6 +286,7 @@ def run_gpu(args):
     sm_mhz = clk.get("sm_max_mhz") or pk.get("sm_max_mhz") or 2070.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # FFMA issue peak, TFLOP/s
     traffic = profile_traffic()
+    lanes_per_walker = b.lanes_per_walker()
     b.close()
 
     # ---- end to end through the C ABI with host buffers ------------------------------
@@ -341,7 +342,7 @@ def run_gpu(args):
             "dtype": "f32 pair energies, f64 ln g / gamma / energy",
             "data": "synthetic (seeded uniform-in-sphere LJ31 configurations)",
             "config": {"workload": WORKLOAD, "walkers": WALKERS, "moves_per_step": WALKERS * MOVES_PER_STEP,
-                       "lanes_per_walker": b.lanes_per_walker(),
+                       "lanes_per_walker": lanes_per_walker,
                        "launch_shape": "fixed by --lpw" if args.lpw else "autotuned",
                        "l2": "bin planes 4096 x 1004 x 64 B = 263 MB > 129 MB L2 (inputs larger than L2)"},
             "accepted_moves_per_s": value * acc_rate,
