@@ -57,6 +57,91 @@ def lj_configs(n_walkers, seed):
     return out
 
 
+def _time_run(b, moves, warm):
+    import torch
+    b.run(warm)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.run(moves)
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3
+
+
+def other_configs(G, seed=11):
+    """Device-resident moves/s of the other workloads (synthetic seeded inputs with their
+    shapes): C1 one Ising 32x32 walker, C3 an uneven WCA batch, C5 a hard-core square-well
+    batch.  Each is a short run after a warm-up, timed with CUDA events."""
+    out = {}
+    rng = np.random.default_rng(seed)
+    # C1: plain SAD, Ising 32x32, one walker, bins of 4 over [-2N, 2N]
+    L = 32
+    b = G.Batch(G.make_config(G.ISING, 1, L, method=G.SAD, min_T=0.2, e_lo=-2.0 * L * L - 8,
+                              e_hi=2.0 * L * L + 8, seed=seed),
+                [(L, 0.0, (0, 0, 0))])
+    b.upload([np.where(rng.random(L * L) < 0.5, -1.0, 1.0)])
+    b.initialize()
+    mv = 1_000_000
+    sec = _time_run(b, mv, 100_000)
+    out["C1"] = {"workload": "Ising 32x32, plain SAD (min_T 0.2), 1 walker", "moves": mv,
+                 "moves_per_s": mv / sec, "ns_per_move": 1e9 * sec / mv,
+                 "lanes_per_walker": b.lanes_per_walker()}
+    b.close()
+    # C3: WCA, N in {64,128,256,512}, density in [0.6, 0.9], 2048 walkers, SAMC t0 = 1e4,
+    # 500 bins over [0, 500) (the range this build fixes; the workload states none)
+    W3 = 2048
+    ns = rng.choice([64, 128, 256, 512], W3)
+    rhos = rng.uniform(0.6, 0.9, W3)
+    geo, states = [], []
+    for n, rho in zip(ns, rhos):
+        Lb = (n / rho) ** (1 / 3)
+        m = int(np.ceil(n ** (1 / 3)))
+        g = np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)
+        g = g[rng.permutation(len(g))[:n]]
+        pos = np.mod((g + 0.5 + rng.uniform(-0.05, 0.05, g.shape)) * (Lb / m), Lb)
+        geo.append((int(n), 0.0, (Lb, Lb, Lb)))
+        states.append(pos)
+    b = G.Batch(G.make_config(G.WCA, W3, int(ns.max()), method=G.SAMC, t0=1e4, energy_bin=1.0,
+                              e_lo=-1.0, e_hi=501.0, max_allowed=500.0, translation_scale=0.1,
+                              seed=seed, resum_interval=4096), geo)
+    b.upload(states)
+    b.initialize()
+    mv = 2048
+    sec = _time_run(b, mv, 512)
+    out["C3"] = {"workload": "WCA, N in {64,128,256,512}, density U[0.6,0.9], 2048 walkers, "
+                             "SAMC t0=1e4, 500 bins over [0,500)",
+                 "moves": W3 * mv, "moves_per_s": W3 * mv / sec,
+                 "lanes_per_walker": b.lanes_per_walker()}
+    b.close()
+    # C5: hard-core square well (lambda 1.3), N = 1024, packing fraction U[0.30, 0.50],
+    # jittered FCC, Wang-Landau over contact-count bins of width 1, 1024 walkers
+    W5, n5 = 1024, 1024
+    m = int(np.ceil((n5 / 4) ** (1 / 3)))
+    base = np.array([(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)])
+    sites = (np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)[:, None, :]
+             + base[None]).reshape(-1, 3)
+    geo, states = [], []
+    for eta in rng.uniform(0.30, 0.50, W5):
+        Lb = (n5 * np.pi / (6 * eta)) ** (1 / 3)
+        pick = sites[rng.permutation(len(sites))[:n5]]
+        pos = np.mod((pick + rng.uniform(-0.004, 0.004, pick.shape)) * (Lb / m), Lb)
+        geo.append((n5, 0.0, (Lb, Lb, Lb)))
+        states.append(pos)
+    b = G.Batch(G.make_config(G.SW, W5, n5, method=G.WL, e_lo=-6.0 * n5 - 2, e_hi=2.0,
+                              well_width=1.3, translation_scale=0.05, seed=seed), geo)
+    b.upload(states)
+    b.initialize()
+    mv = 2048
+    sec = _time_run(b, mv, 512)
+    out["C5"] = {"workload": "hard-core square well lambda=1.3, N=1024, packing U[0.30,0.50], "
+                             "jittered FCC, WL on contact bins, 1024 walkers",
+                 "moves": W5 * mv, "moves_per_s": W5 * mv / sec,
+                 "lanes_per_walker": b.lanes_per_walker()}
+    b.close()
+    return out
+
+
 def da_compare(G, rank=0, walkers=8192, moves=2048):
     """C4 shape: LJ38 (R=3.5), SAD; the surrogate is trained on configurations the walkers
     visit, then plain and delayed-acceptance moves are timed on the same batch state."""
@@ -325,6 +410,9 @@ def run_gpu(args):
     da = None
     if not args.no_da and world == 1:
         da = da_compare(G, rank)
+    others = None
+    if not args.no_other and rank == 0:
+        others = other_configs(G)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -360,6 +448,7 @@ def run_gpu(args):
             "e2e": e2e,
             "cpu_baseline": cpu,
             "delayed_acceptance": da,
+            "other_configs": others,
         }
         print(json.dumps(line))
     if world > 1:
@@ -380,6 +469,7 @@ def main():
     ap.add_argument("--moves", type=int, default=MOVES_PER_STEP, help="moves per walker per step")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-da", action="store_true", help="skip the delayed-acceptance comparison")
+    ap.add_argument("--no-other", action="store_true", help="skip the C1/C3/C5 measurements")
     args = ap.parse_args()
     WALKERS, MOVES_PER_STEP = args.walkers, args.moves
     if args.impl == "reference":

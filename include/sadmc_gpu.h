@@ -237,6 +237,14 @@ int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, 
 int32_t sadmc_surrogate_predict(sadmc_handle* h, const float* pos, int32_t configs,
                                 float* energies);
 
+/* Self-check of the exact FP64 rewrites the decision path uses in place of FP64
+ * instructions (a diagnostic with no counterpart in the reference): over n seeded cases,
+ * mismatches[0] counts divisions by a known reciprocal that differ from a / b,
+ * mismatches[1] integer float-to-double conversions that differ from the cast (n bit
+ * patterns), mismatches[2] binary32-first Metropolis tests that differ from the FP64 one;
+ * first (optional) gets the first division mismatch (a, b). */
+int32_t sadmc_check_numerics(uint64_t n, uint64_t seed, uint64_t* mismatches, double* first);
+
 /* The counter-based draws the kernels consume for moves t0 .. t0+count-1 of one walker
  * (Philox4x32-10 keyed by (walker, seed); stream_pair 0 moves, 1 descent): idx2 gets
  * (atom or i, j) pairs, g3 the three normals, u the Metropolis uniform.  Host arrays.

@@ -1285,6 +1285,23 @@ int32_t sadmc_draws(int32_t system, uint32_t n, uint64_t seed, uint32_t walker, 
   return SADMC_OK;
 }
 
+int32_t sadmc_check_numerics(uint64_t n, uint64_t seed, uint64_t* mismatches, double* first) {
+  if (!mismatches) return fail(SADMC_ERR_INVALID, "null argument");
+  unsigned long long* d = nullptr;
+  double* df = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(unsigned long long) * 3);
+  if (e == cudaSuccess) e = cudaMalloc(&df, sizeof(double) * 2);
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(unsigned long long) * 3);
+  if (e == cudaSuccess) e = cudaMemset(df, 0, sizeof(double) * 2);
+  if (e == cudaSuccess) e = launch_numerics_check(n, seed, d, df, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && first) e = cudaMemcpy(first, df, sizeof(double) * 2, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cudaFree(df);
+  if (e != cudaSuccess) return fail(SADMC_ERR_CUDA, cudaGetErrorString(e));
+  return SADMC_OK;
+}
+
 int32_t sadmc_heat_capacity(const double* T, int32_t nT, const double* E, const double* S,
                             int32_t n, double* C) {
   if (!T || !E || !S || !C || nT < 0 || n <= 0) return fail(SADMC_ERR_INVALID, "bad argument");

@@ -62,6 +62,47 @@ __device__ __forceinline__ bool dgt(double x, double y) {
   if ((a | b) >= 0) return a > b;
   return x > y;
 }
+// x is NaN, by integer instructions
+__device__ __forceinline__ bool is_nan64(double x) {
+  return (unsigned long long)(__double_as_longlong(x) & 0x7fffffffffffffffll) > 0x7ff0000000000000ull;
+}
+// (double)f for a binary32 value, by integer instructions for zero and normal numbers
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e == 0u && (b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)(b & 0x80000000u) << 32);
+  if (e == 0u || e == 255u) return (double)f;
+  const unsigned long long d = ((unsigned long long)(b >> 31) << 63) |
+                               ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                               ((unsigned long long)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)d);
+}
+// a / b, correctly rounded, for a divisor b whose correctly rounded reciprocal y = 1/b is
+// known: q = a y, r = a - b q (exact, one FMA), a / b = RN(q + r y) (P. Markstein,
+// IBM J. Res. Dev. 34(1), 1990).  Finite normal operands and quotient.
+__device__ __forceinline__ double div_by(double a, double b, double y) {
+  const double q = __dmul_rn(a, y);
+  const double r = __fma_rn(-b, q, a);
+  return __fma_rn(r, y, q);
+}
+// rejected = (u > exp(lnw1 - lnw2)) for lnw1 - lnw2 <= 0, taken on the binary32 copies
+// of the two weights when far enough from the threshold; otherwise the FP64 difference
+// goes through metropolis_reject.
+__device__ __forceinline__ bool metropolis_reject2(double lnw1, double lnw2, uint64_t u53) {
+  const float a = f32_trunc(lnw1), b = f32_trunc(lnw2);
+  const float df = a - b;
+  // |df - (lnw1 - lnw2)| <= (|a| + |b|) 2^-23 + |df| 2^-24; exp's relative error is that
+  const float dd = (fabsf(a) + fabsf(b)) * 1.2e-7f + fabsf(df) * 6.0e-8f + 1e-30f;
+  if (df + dd < -80.0f) return u53 != 0;
+  if (df - dd > -80.0f && dd < 0.25f) {
+    const float e32 = __expf(df);
+    const float m = 4.0e-6f + fabsf(df) * 4.0e-7f + 2.0f * dd;
+    const float uf = (float)(u53 >> 29) * (1.0f / 16777216.0f);
+    if (uf > e32 * (1.0f + m)) return true;
+    if (uf + (1.0f / 16777216.0f) < e32 * (1.0f - m)) return false;
+  }
+  return metropolis_reject(lnw1 - lnw2, u53);
+}
 
 // FAM: the method a kernel is specialised for (M_SAD, ...), or FAM_ANY for the kind held
 // in each walker's state (WL and 1/t-WL, whose walkers switch to SAMC at run time).
@@ -102,6 +143,10 @@ struct Fh {
   bool tscale_changed;  // set when the SAD discovery adapted translation_scale
   // binary32 copies for the FP32-first comparisons of decide_de (refreshed on change)
   float Ef, cminf, cmaxf, maxf, minf, inv_wf;
+  // correctly rounded reciprocals for div_by: 1/min_T, and 1/tF, 1/num_states for the
+  // tF and num_states they were taken for
+  double inv_minT, inv_tF, inv_ns;
+  uint64_t inv_tF_of, inv_ns_of;
   bool inverted;        // too_lo > too_hi (never true for SAD; kept exact)
 
   // ---- index helpers ---------------------------------------------------------------
@@ -206,6 +251,8 @@ struct Fh {
     maxf = f32_trunc(max_allowed);
     minf = f32_trunc(min_allowed);
     inv_wf = (float)inv_width;
+    inv_minT = 1.0 / c.min_T;
+    inv_tF_of = 0; inv_ns_of = 0; inv_tF = inv_ns = 0.0;
   }
   __device__ void store(WalkerCore* cores, int w) {
     if (c.kind != M_DESCENT) flush_cur();
@@ -219,7 +266,8 @@ struct Fh {
         double p = c.latest_param, tF = (double)c.tF, ns = (double)c.num_states;
         if (p * tF * ns == 0.0) return 0.0;
         double td = (double)t;
-        return (p + td / tF) / (p + td / ns * (td / tF));
+        const double t_tF = div_by(td, tF, inv_tF);  // inv_tF, inv_ns refreshed by gamma()
+        return (p + t_tF) / (p + div_by(td, ns, inv_ns) * t_tF);
       }
       case M_SAMC: {
         double td = (double)t;
@@ -236,6 +284,10 @@ struct Fh {
     if (kind() != M_SAD && kind() != M_SAMC) return gamma_at(c.moves);
     if (!gb_valid || c.moves < gb_base || c.moves - gb_base >= (uint64_t)(4 * LPW)) {
       gb_base = c.moves;
+      if (kind() == M_SAD) {
+        if (c.tF != inv_tF_of) { inv_tF = 1.0 / (double)c.tF; inv_tF_of = c.tF; }
+        if (c.num_states != inv_ns_of) { inv_ns = 1.0 / (double)c.num_states; inv_ns_of = c.num_states; }
+      }
 #pragma unroll
       for (int q = 0; q < 4; ++q) gb_val[q] = gamma_at(c.moves + (uint64_t)(glane + LPW * q));
       gb_valid = true;
@@ -289,7 +341,7 @@ struct Fh {
     return g > win_hi ? true : (g < win_hi ? false : e > c.too_hi);
   }
   __device__ double sad_lnw(double e, int g) const {  // energy.rs:451-464
-    if (below(e, g)) return ld_lnw(win_lo) + (e - c.too_lo) / c.min_T;
+    if (below(e, g)) return ld_lnw(win_lo) + div_by(e - c.too_lo, c.min_T, inv_minT);
     if (above(e, g)) return ld_lnw(win_hi);
     return ld_lnw(g);
   }
@@ -308,7 +360,7 @@ struct Fh {
     else if (e >= cur_max) g = c.b_hi + 1;
     else g = gidx_exact(e);
     if (kind() == M_SAD) {
-      if (e < c.too_lo) return ld_lnw(win_lo) + (e - c.too_lo) / c.min_T;
+      if (e < c.too_lo) return ld_lnw(win_lo) + div_by(e - c.too_lo, c.min_T, inv_minT);
       if (e > c.too_hi) return ld_lnw(win_hi);
     }
     if (g < c.b_lo || g > c.b_hi) return 0.0;
@@ -344,7 +396,7 @@ struct Fh {
     const bool accepted = uni(!rejects(possible, de, u53, has_first, lnw_first, e2, have));
     if (accepted) {
       if (c.kind != M_DESCENT) { c.accepted += 1; c.acc_rate += rs; }
-      set_E(have ? e2 : c.E + (double)de);
+      set_E(have ? e2 : c.E + f2d(de));
     }
     return accepted;
   }
@@ -354,7 +406,7 @@ struct Fh {
     const float e2f = Ef + de;
     const float tol = (fabsf(Ef) + fabsf(e2f)) * 2.5e-7f + 1e-30f;
     auto exact = [&]() -> double {
-      if (!have) { e2 = c.E + (double)de; have = true; }
+      if (!have) { e2 = c.E + f2d(de); have = true; }
       return e2;
     };
     // e2 > T (T's binary32 copy Tf within |T| 2^-23)
@@ -409,7 +461,7 @@ struct Fh {
         const double lnw1 = has_first ? lnw_first : sad_lnw(c.E, cur);
         if (i2 <= win_lo || i2 >= win_hi) exact();  // extrapolation / edge comparisons
         const double lnw2 = sad_lnw(e2, i2);
-        rejected = dgt(lnw2, lnw1) && metropolis_reject(lnw1 - lnw2, u53);
+        rejected = dgt(lnw2, lnw1) && metropolis_reject2(lnw1, lnw2, u53);
         if (!rejected && hist2 == 0) {  // energy.rs:466-483
           exact();
           if (e2 < c.too_hi && e2 > c.too_lo) {
@@ -423,13 +475,13 @@ struct Fh {
       }
       case M_SAMC: {
         const double lnw1 = has_first ? lnw_first : k_lnw;
-        rejected = dgt(lnw2_raw, lnw1) && metropolis_reject(lnw1 - lnw2_raw, u53);
+        rejected = dgt(lnw2_raw, lnw1) && metropolis_reject2(lnw1, lnw2_raw, u53);
         break;
       }
       case M_WL:
       case M_INV_T_WL: {
         const double lnw1 = has_first ? lnw_first : k_lnw;
-        rejected = dgt(lnw2_raw, lnw1) && metropolis_reject(lnw1 - lnw2_raw, u53);
+        rejected = dgt(lnw2_raw, lnw1) && metropolis_reject2(lnw1, lnw2_raw, u53);
         if (!rejected && hist2 == 0 && c.lowest_hist > 0) c.wl_num_states += 1.0;
         break;
       }
@@ -473,7 +525,7 @@ struct Fh {
   // energy.rs:514-761
   __device__ void update_weights(double energy) {
     double g = gamma();
-    if (g != g) c.status |= ST_NAN_GAMMA;
+    if (is_nan64(g)) c.status |= ST_NAN_GAMMA;
     double old = k_lnw;
     k_lnw += g;
     if (kind() == M_SAD) sad_update(energy, old);

@@ -91,6 +91,9 @@ cudaError_t launch_heat_capacity(const double* T, int nT, const double* E, const
                                  int n, double* C, cudaStream_t st);
 
 // The per-move draws of walker `walker` for moves t0 .. t0+count-1 (device pointers).
+// Self-check of the exact FP64 rewrites of the decision path (diagnostic).
+cudaError_t launch_numerics_check(uint64_t n, uint64_t seed, unsigned long long* out, double* first,
+                                  cudaStream_t st);
 cudaError_t launch_draws(int system, uint32_t n, uint64_t seed, uint32_t walker, uint64_t t0,
                          int count, uint32_t stream_pair, uint32_t* idx2, float* g3, double* u,
                          cudaStream_t st);

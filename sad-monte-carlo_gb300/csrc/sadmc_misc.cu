@@ -131,3 +131,75 @@ cudaError_t launch_draws(int system, uint32_t n, uint64_t seed, uint32_t walker,
   return cudaGetLastError();
 }
 }  // namespace sadmc
+
+// ---- self-check of the exact rewrites of the decision path --------------------------
+namespace sadmc {
+namespace dev {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {  // splitmix64 finaliser
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+__device__ __forceinline__ double rnd_double(uint64_t r, int emin, int emax) {
+  const uint64_t span = (uint64_t)(emax - emin + 1);
+  const int e = emin + (int)((r >> 52) % span);
+  const uint64_t mant = mix64(r) & 0xFFFFFFFFFFFFFull;
+  return __longlong_as_double((long long)(((uint64_t)(e + 1023) << 52) | mant));
+}
+
+// out[0]: div_by(a, b, 1/b) != a / b; out[1]: f2d(f) != (double)f over the 2^32 bit
+// patterns visited; out[2]: metropolis_reject2 != metropolis_reject; out[3..4]: the
+// first division mismatch (a, b).
+__global__ void numerics_check_kernel(uint64_t n, uint64_t seed, unsigned long long* out, double* first) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = mix64(seed ^ (i * 0x2545F4914F6CDD1Dull));
+    const uint64_t r2 = mix64(r);
+    double a, b;
+    switch (i & 3) {
+      case 0:  // wide exponents, both signs of a
+        a = rnd_double(r, -60, 60) * ((r2 & 1) ? -1.0 : 1.0);
+        b = rnd_double(r2, -60, 60);
+        break;
+      case 1:  // integer move counters over integer tF / num_states
+        a = (double)(1 + (r >> 24));
+        b = (double)(1 + (r2 >> (24 + (r & 15))));
+        break;
+      case 2:  // SAD extrapolation: (e - too_lo) / min_T
+        a = -300.0 * (double)(r >> 11) * (1.0 / 9007199254740992.0);
+        b = 0.01 + 2.0 * (double)(r2 >> 11) * (1.0 / 9007199254740992.0);
+        break;
+      default: {  // divisors with near-all-ones or near-zero mantissas
+        const uint64_t m = (r2 & 1) ? (0xFFFFFFFFFFFFFull ^ (r2 >> 40)) : (r2 >> 40);
+        b = __longlong_as_double((long long)(((uint64_t)(1023 + (int)(r2 >> 58) - 32) << 52) | m));
+        a = rnd_double(r, -40, 40);
+        break;
+      }
+    }
+    const double q = div_by(a, b, 1.0 / b), want = a / b;
+    if (__double_as_longlong(q) != __double_as_longlong(want)) {
+      if (atomicAdd(&out[0], 1ull) == 0ull) { first[0] = a; first[1] = b; }
+    }
+    const float f = __uint_as_float((unsigned)i ^ (unsigned)(seed >> 32));
+    const double fd = f2d(f), fw = (double)f;
+    if (!(f != f) && __double_as_longlong(fd) != __double_as_longlong(fw)) atomicAdd(&out[1], 1ull);
+    // Metropolis on two weights of SAD-like magnitude (up to 2^20) and close differences
+    const double l1 = (double)(r >> 44) + (double)(r2 >> 11) * (1.0 / 9007199254740992.0);
+    const double l2 = l1 + (double)((r2 >> 3) & 0xFFFF) * (1.0 / 4096.0) * ((r & 2) ? 1.0 : 1e-6);
+    const uint64_t u53 = mix64(r ^ r2) >> 11;
+    if (metropolis_reject2(l1, l2, u53) != metropolis_reject(l1 - l2, u53)) atomicAdd(&out[2], 1ull);
+  }
+}
+
+}  // namespace dev
+
+cudaError_t launch_numerics_check(uint64_t n, uint64_t seed, unsigned long long* out, double* first,
+                                  cudaStream_t st) {
+  dev::numerics_check_kernel<<<152 * 8, 256, 0, st>>>(n, seed, out, first);
+  return cudaGetLastError();
+}
+
+}  // namespace sadmc
+

@@ -108,6 +108,7 @@ def lib():
         "sadmc_surrogate_train": (I32, [P, I32, I32, ctypes.c_float, U64, P]),
         "sadmc_surrogate_loss_grads": (I32, [P, P, P, I32, P, P]),
         "sadmc_surrogate_loss_grads_noalloc": (I32, [P, P, P, I32, P, P, P]),
+        "sadmc_check_numerics": (I32, [U64, U64, P, P]),
         "sadmc_surrogate_predict": (I32, [P, P, I32, P]),
         "sadmc_run_da": (I32, [P, U64, I32, P]),
         "sadmc_draws": (I32, [I32, ctypes.c_uint32, U64, ctypes.c_uint32, U64, I32, ctypes.c_uint32,
@@ -425,6 +426,15 @@ def heat_capacity(T, E, S):
     C = np.zeros(len(T))
     _check(lib().sadmc_heat_capacity(_p(T), len(T), _p(E), _p(S), len(E), _p(C)))
     return C
+
+
+def check_numerics(n, seed=1):
+    """Mismatch counts of the exact FP64 rewrites against CUDA's own operations (see
+    sadmc_check_numerics) and the first mismatching division (a, b)."""
+    out = np.zeros(3, np.uint64)
+    first = np.zeros(2)
+    _check(lib().sadmc_check_numerics(int(n), int(seed), _p(out), _p(first)))
+    return out, first
 
 
 def cv_from_bins(bins, T):

@@ -139,3 +139,34 @@ def test_wca_uneven_trace_replay(gpu, oracle, lpw):
     # incremental binary32 dE since the last FP64 re-sum (500 moves) vs the FP64 re-sum
     np.testing.assert_allclose(b.energies(), b.compute_energies(), atol=1e-3, rtol=2e-6)
     assert not (b.status() & ~np.uint32(gpu.ST_DESCENT_FAILED)).any()
+
+
+def test_square_well_initial_descent_bit_exact(gpu, oracle):
+    """The descent of energy.rs:840-851 on the square well: walkers start above
+    max_allowed_energy and gain contacts downhill; states and bins equal the oracle's."""
+    n, moves, seed = 108, 6000, 13
+    ws = sw_walkers(oracle, n, [0.30, 0.40, 0.45, 0.35], 90)
+    E_start = np.array([oracle.Walker(oracle.make_config(oracle.SW, n, box=box), p).energy()
+                        for p, box in ws])
+    max_allowed = float(E_start.max() - 15.0)
+    kw = dict(method=0, min_T=0.5)
+    cfg = gpu.make_config(gpu.SW, len(ws), n, e_lo=-6.0 * n - 2, e_hi=2.0, well_width=1.3,
+                          seed=seed, translation_scale=0.05, max_allowed=max_allowed,
+                          lanes_per_walker=8, **kw)
+    b = gpu.Batch(cfg, [(n, 0.0, box) for _, box in ws])
+    b.upload([p for p, _ in ws])
+    b.initialize()
+    E0 = b.energies()
+    assert (E0 < max_allowed).all()
+    b.run(moves)
+    for w, (pos, box) in enumerate(ws):
+        ow = oracle.Walker(oracle.make_config(oracle.SW, n, box=box, well_width=1.3, seed=seed,
+                                              walker=w, translation_scale=0.05,
+                                              max_allowed=max_allowed, **kw), pos)
+        assert ow.energy() == E0[w]
+        ow.run(moves)
+        label = f"sw descent walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_array_equal(b.state(w), ow.state())
+    assert not b.status().any()

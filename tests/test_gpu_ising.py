@@ -68,3 +68,31 @@ def test_device_draws_match_oracle(gpu, oracle, system, n):
     for k in range(0, count, 7):
         idx, g, u = oracle.draws(system, n, seed, walker, t0 + k)
         assert np.array_equal(idx, gi[k]) and np.array_equal(g, gg[k]) and u == gu[k], k
+
+
+def test_ising_initial_descent_bit_exact(gpu, oracle):
+    """from_params descent (energy.rs:840-851) on the descent stream: walkers starting above
+    max_allowed_energy flip downhill until below it (each makes at least one proposal), then
+    run; spins, energies and bins equal the oracle's."""
+    L, W, moves, seed = 12, 16, 20000, 31
+    N = L * L
+    kw = dict(method=0, min_T=0.2)
+    cfg = gpu.make_config(gpu.ISING, W, L, e_lo=-2.0 * N - 4, e_hi=2.0 * N + 4, seed=seed,
+                          max_allowed=-100.0, **kw)
+    b = gpu.Batch(cfg, [(L, 0.0, (0, 0, 0))] * W)
+    spins = [ising_spins(L, 700 + w) for w in range(W)]
+    b.upload(spins)
+    b.initialize()
+    E0 = b.energies()
+    assert (E0 < -100.0).all()
+    b.run(moves)
+    for w in range(W):
+        ow = oracle.Walker(oracle.make_config(oracle.ISING, L, seed=seed, walker=w,
+                                              max_allowed=-100.0, **kw), spins[w])
+        assert ow.energy() == E0[w]
+        ow.run(moves)
+        label = f"descent walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_array_equal(b.state(w), ow.state())
+    assert not b.status().any()
