@@ -130,6 +130,7 @@ struct Fh {
   double p_lnw, p_sE, p_sE2;
   uint64_t p_hist, p_tf, p_stamp;
   double cur_max;      // upper edge of the allocated range
+  double E2;           // c.E * c.E, formed when E changes (energy_squared_total term)
   int win_lo, win_hi;  // SAD window as bin indices
   // gamma batch (see gamma())
   double gb_val[4];
@@ -246,6 +247,7 @@ struct Fh {
     tscale_changed = false;
     // binary32 shadows of decide_de (each within |x| 2^-23 of its FP64 value)
     Ef = f32_trunc(c.E);
+    E2 = c.E * c.E;
     cminf = f32_trunc(c.cur_min);
     cmaxf = f32_trunc(cur_max);
     maxf = f32_trunc(max_allowed);
@@ -348,6 +350,7 @@ struct Fh {
 
   __device__ void set_E(double e) {
     c.E = e;
+    E2 = e * e;
     Ef = f32_trunc(e);
   }
 
@@ -506,7 +509,7 @@ struct Fh {
     }
     k_hist += 1;
     k_sE += E;
-    k_sE2 += E * E;
+    k_sE2 += E2;  // E2 == E * E (set_E)
     update_weights(E);
     const int li = cur - c.b_lo;
     if (dgt(k_lnw, c.max_S)) {
