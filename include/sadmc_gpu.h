@@ -257,6 +257,55 @@ int32_t sadmc_draws(int32_t system, uint32_t n, uint64_t seed, uint32_t walker, 
 int32_t sadmc_heat_capacity(const double* T, int32_t nT, const double* E, const double* S,
                             int32_t n, double* C);
 
+/* ---- Grand-canonical LJ cluster with the energy-number method ----------------------
+ * EnergyNumberMC<Lj> (src/mc/energy_number.rs) with the GrandSystem moves of
+ * src/system/lj.rs:291-319: translations, adds at a uniform point of the sphere and
+ * removals of a uniform atom, weighted by ln w(E, N) (SAMC or Wang-Landau).  Every walker
+ * starts empty (E = 0, N = 0), as GrandLjParams does.  The bins are returned in the
+ * reference's layout: index = E row * (max_N + 1) + N, rows from bins.min. */
+typedef struct sadmc_grand sadmc_grand;
+typedef struct sadmc_grand_config {
+  int32_t method;            /* SADMC_SAMC or SADMC_WL (energy_number.rs:18-27) */
+  int32_t n_walkers;
+  int32_t max_N;             /* EnergyNumberMCParams::max_N, required here (1..63) */
+  int32_t acceptance_rate_mode; /* MoveParams::AcceptanceRate(target_rate), else _Explicit */
+  double t0;                 /* SAMC t0 */
+  double energy_bin;         /* bin width (default 1.0) */
+  double radius;             /* LJ spherical wall radius (GrandLjParams::radius) */
+  int32_t has_min_allowed, has_max_allowed;
+  double min_allowed, max_allowed;
+  double target_rate;
+  double translation_scale;  /* _Explicit translation scale (0.05 in acceptance-rate mode) */
+  double addremove_probability; /* _Explicit add/remove probability (0.5 initially otherwise) */
+  double e_lo, e_hi;         /* energies the preallocated bins must cover (e_lo < 0 < e_hi) */
+  uint64_t seed;
+  int32_t resum_interval;    /* moves between FP64 energy re-sums; 0 = 2048 */
+  int32_t pad;
+  double drift_tol;          /* 0 = 1e-2 */
+} sadmc_grand_config;
+int32_t sadmc_grand_create(const sadmc_grand_config* cfg, sadmc_grand** out);
+int32_t sadmc_grand_destroy(sadmc_grand* h);
+/* `moves` calls of EnergyNumberMC::move_once (energy_number.rs:540-666) per walker. */
+int32_t sadmc_grand_run(sadmc_grand* h, uint64_t moves);
+/* Record (E before, proposed E or NaN when impossible) for the next `capacity` moves. */
+int32_t sadmc_grand_set_trace(sadmc_grand* h, uint64_t capacity);
+int32_t sadmc_grand_read_trace(sadmc_grand* h, int32_t walker, double* e1, double* e2, uint64_t* n);
+/* Positions (x,y,z per atom, *n atoms) of one walker. */
+int32_t sadmc_grand_read_state(sadmc_grand* h, int32_t walker, double* pos, int32_t* n);
+/* SADMC_GRAND_N_SCALARS doubles: moves, accepted, addremove_probability, N, E,
+ * num_states, t_last, gamma (WL), lowest, highest, total (WL), max_S, max_S_index,
+ * bins.min, width, max_N (of the bins), num_E, add/remove attempts, add/remove accepted,
+ * drift, status. */
+#define SADMC_GRAND_N_SCALARS 21
+int32_t sadmc_grand_read_scalars(sadmc_grand* h, int32_t walker, double* out);
+/* Bins in the reference's layout: *n_e rows by *n_n columns (N = 0..max_N). */
+int32_t sadmc_grand_read_bins(sadmc_grand* h, int32_t walker, double* lnw, uint64_t* histogram,
+                              uint64_t* wl_histogram, uint8_t* visited, uint64_t* round_trips,
+                              int64_t* n_e, int64_t* n_n);
+/* num_translation_attempts / num_translation_accepted per N (n_n entries). */
+int32_t sadmc_grand_translation_counts(sadmc_grand* h, int32_t walker, uint64_t* attempts,
+                                       uint64_t* accepted);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,14 @@ def lib():
             "orc_energy": (D, [P]), "orc_compute_energy": (D, [P]),
             "orc_override_worst": (None, [P, P]),
             "orc_extra": (I64, [P, P, P]),
+            "orc_grand_create": (P, [P]), "orc_grand_destroy": (None, [P]),
+            "orc_grand_run": (None, [P, U64]),
+            "orc_grand_run_override": (D, [P, U64, P, P, P]),
+            "orc_grand_worst": (None, [P, P]), "orc_grand_state": (I64, [P, P]),
+            "orc_grand_compute_energy": (D, [P]), "orc_grand_scalars": (None, [P, P]),
+            "orc_grand_bins": (I64, [P, P, P, P, P, P]),
+            "orc_grand_translation": (None, [P, P, P]),
+            "orc_grand_draws": (None, [U64, ctypes.c_uint32, U64, P, P, P, P]),
             "orc_verify_energy": (ctypes.c_int, [P]),
             "orc_get_state": (None, [P, P]),
             "orc_plan_move": (ctypes.c_int, [P, U32, U32, D, D, D, D, P]),
@@ -215,6 +223,110 @@ class Walker:
 
     def pressure(self):
         return lib().orc_pressure(self.h)
+
+
+class GrandConfig(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("has_energy_bin", ctypes.c_int32),
+                ("t0", ctypes.c_double), ("energy_bin", ctypes.c_double),
+                ("has_max_N", ctypes.c_int32), ("max_N", ctypes.c_int32),
+                ("has_min_allowed", ctypes.c_int32), ("has_max_allowed", ctypes.c_int32),
+                ("min_allowed", ctypes.c_double), ("max_allowed", ctypes.c_double),
+                ("acc_mode", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("target_rate", ctypes.c_double), ("translation_scale", ctypes.c_double),
+                ("addremove_probability", ctypes.c_double), ("radius", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("walker", ctypes.c_uint32), ("pad2", ctypes.c_uint32)]
+
+
+GRAND_SCALARS = ["moves", "accepted", "addremove_probability", "N", "energy", "num_states",
+                 "t_last", "gamma", "lowest_hist", "highest_hist", "total_hist", "max_S",
+                 "max_S_index", "min", "width", "max_N", "num_E", "addremove_attempts",
+                 "addremove_accepted"]
+
+
+def make_grand_config(radius, *, method=M_SAMC, t0=1e4, energy_bin=None, max_N=None,
+                      min_allowed=None, max_allowed=None, target_rate=None,
+                      translation_scale=0.05, addremove_probability=0.05, seed=0, walker=0):
+    c = GrandConfig()
+    c.kind = method
+    c.t0 = t0
+    c.has_energy_bin, c.energy_bin = int(energy_bin is not None), energy_bin or 0.0
+    c.has_max_N, c.max_N = int(max_N is not None), max_N or 0
+    c.has_min_allowed, c.min_allowed = int(min_allowed is not None), min_allowed or 0.0
+    c.has_max_allowed = int(max_allowed is not None)
+    c.max_allowed = max_allowed if max_allowed is not None else 0.0
+    c.acc_mode, c.target_rate = int(target_rate is not None), target_rate or 0.5
+    c.translation_scale, c.addremove_probability = translation_scale, addremove_probability
+    c.radius, c.seed, c.walker = radius, seed, walker
+    return c
+
+
+class GrandWalker:
+    """One oracle energy-number walker (grand-canonical LJ cluster, starting empty)."""
+
+    def __init__(self, cfg):
+        self.cfg = cfg
+        self.h = lib().orc_grand_create(ctypes.byref(cfg))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_grand_destroy(self.h)
+            self.h = None
+
+    def run(self, n):
+        lib().orc_grand_run(self.h, int(n))
+
+    def run_override(self, e1, e2):
+        e1 = np.ascontiguousarray(e1, dtype=np.float64)
+        e2 = np.ascontiguousarray(e2, dtype=np.float64)
+        mm = ctypes.c_uint64(0)
+        d = lib().orc_grand_run_override(self.h, len(e2), _p(e1), _p(e2), ctypes.byref(mm))
+        return d, mm.value
+
+    def worst(self):
+        o = np.zeros(4)
+        lib().orc_grand_worst(self.h, _p(o))
+        return o
+
+    def state(self):
+        n = lib().orc_grand_state(self.h, None)
+        out = np.zeros((max(n, 1), 3))
+        lib().orc_grand_state(self.h, _p(out))
+        return out[:n]
+
+    def compute_energy(self):
+        return lib().orc_grand_compute_energy(self.h)
+
+    def scalars(self):
+        o = np.zeros(len(GRAND_SCALARS))
+        lib().orc_grand_scalars(self.h, _p(o))
+        return dict(zip(GRAND_SCALARS, o))
+
+    def bins(self):
+        n = lib().orc_grand_bins(self.h, None, None, None, None, None)
+        lnw = np.zeros(n)
+        hist, wlh, rt = (np.zeros(n, np.uint64) for _ in range(3))
+        vis = np.zeros(n, np.uint8)
+        lib().orc_grand_bins(self.h, _p(lnw), _p(hist), _p(wlh), _p(vis), _p(rt))
+        s = self.scalars()
+        nN = int(s["max_N"]) + 1
+        return dict(lnw=lnw.reshape(-1, nN), hist=hist.reshape(-1, nN), wl_hist=wlh.reshape(-1, nN),
+                    visited=vis.reshape(-1, nN), round_trips=rt.reshape(-1, nN), min=s["min"],
+                    width=s["width"])
+
+    def translation_counts(self):
+        nN = int(self.scalars()["max_N"]) + 1
+        a, b = np.zeros(nN, np.uint64), np.zeros(nN, np.uint64)
+        lib().orc_grand_translation(self.h, _p(a), _p(b))
+        return a, b
+
+
+def grand_draws(seed, walker, t):
+    d = np.zeros(2)
+    u = np.zeros(2, np.uint32)
+    g = np.zeros(3, np.float32)
+    c = np.zeros(3)
+    lib().orc_grand_draws(seed, walker, t, _p(d), _p(u), _p(g), _p(c))
+    return dict(u_choice=d[0], u=d[1], add_bit=int(u[0]), pick=int(u[1]), g=g, cand0=c)
 
 
 def philox(ctr, key):

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "energy_mc.hpp"
+#include "energy_number.hpp"
 #include "systems.hpp"
 
 using namespace orc;
@@ -131,6 +132,7 @@ void* orc_create(const orc_config* c, const double* state) {
       s.pos.resize(n);
       for (uint32_t k = 0; k < n; ++k) s.pos[k] = {state[3 * k], state[3 * k + 1], state[3 * k + 2]};
       s.max_radius_squared = c->radius * c->radius;
+      s.max_radius = c->radius;
       s.E = s.compute_energy();
       h->lj.reset(new EnergyMC<Lj>());
       h->lj->init(std::move(s), p, src, dl);
@@ -510,4 +512,121 @@ double orc_bench(const orc_config* cfgs, const double* const* states, int32_t nw
   return std::chrono::duration<double>(t1 - t0).count();
 }
 
+
+// ---- energy-number MC (grand-canonical LJ cluster), src/mc/energy_number.rs -----------
+typedef struct orc_grand_config {
+  int32_t kind;            // 1 SAMC, 2 WL
+  int32_t has_energy_bin;
+  double t0;
+  double energy_bin;
+  int32_t has_max_N, max_N;
+  int32_t has_min_allowed, has_max_allowed;
+  double min_allowed, max_allowed;
+  int32_t acc_mode, pad;
+  double target_rate, translation_scale, addremove_probability;
+  double radius;
+  uint64_t seed;
+  uint32_t walker, pad2;
+} orc_grand_config;
+
+void* orc_grand_create(const orc_grand_config* c) {
+  Lj s;
+  s.max_radius_squared = c->radius * c->radius;
+  s.max_radius = c->radius;
+  s.E = 0.0;
+  NumberParams p;
+  p.kind = c->kind;
+  p.t0 = c->t0;
+  p.has_energy_bin = c->has_energy_bin != 0;
+  p.energy_bin = c->energy_bin;
+  p.has_max_N = c->has_max_N != 0;
+  p.max_N = (size_t)c->max_N;
+  p.has_min_allowed = c->has_min_allowed != 0;
+  p.has_max_allowed = c->has_max_allowed != 0;
+  p.min_allowed = c->min_allowed;
+  p.max_allowed = c->max_allowed;
+  p.acc_mode = c->acc_mode != 0;
+  p.target_rate = c->target_rate;
+  p.translation_scale = c->translation_scale;
+  p.addremove_probability = c->addremove_probability;
+  auto* mc = new EnergyNumberMC<Lj>();
+  mc->init(std::move(s), p, c->seed, c->walker);
+  return mc;
+}
+void orc_grand_destroy(void* h) { delete (EnergyNumberMC<Lj>*)h; }
+void orc_grand_run(void* h, uint64_t n) {
+  auto* mc = (EnergyNumberMC<Lj>*)h;
+  for (uint64_t k = 0; k < n; ++k) mc->move_once();
+}
+double orc_grand_run_override(void* h, uint64_t n, const double* e1, const double* e2,
+                              uint64_t* mismatch) {
+  auto* mc = (EnergyNumberMC<Lj>*)h;
+  mc->e1_override = e1;
+  mc->e2_override = e2;
+  mc->override_base = mc->moves;
+  for (uint64_t k = 0; k < n; ++k) mc->move_once();
+  mc->e1_override = mc->e2_override = nullptr;
+  if (mismatch) *mismatch = mc->override_mismatch;
+  return mc->max_e2_discrepancy;
+}
+void orc_grand_worst(void* h, double* out4) {
+  auto* mc = (EnergyNumberMC<Lj>*)h;
+  for (int k = 0; k < 4; ++k) out4[k] = mc->worst[k];
+}
+int64_t orc_grand_state(void* h, double* pos) {
+  auto* mc = (EnergyNumberMC<Lj>*)h;
+  if (pos)
+    for (size_t i = 0; i < mc->sys.pos.size(); ++i)
+      for (int a = 0; a < 3; ++a) pos[3 * i + a] = mc->sys.pos[i][a];
+  return (int64_t)mc->sys.pos.size();
+}
+double orc_grand_compute_energy(void* h) { return ((EnergyNumberMC<Lj>*)h)->sys.compute_energy(); }
+// moves, accepted, addremove_probability, N, E, num_states, t_last, gamma (WL), lowest,
+// highest, total (WL), max_S, max_S_index, bins.min, width, max_N, num_E, add/remove
+// attempts, add/remove accepted
+void orc_grand_scalars(void* h, double* o) {
+  auto* mc = (EnergyNumberMC<Lj>*)h;
+  const NBins& b = mc->bins;
+  const double v[19] = {(double)mc->moves, (double)mc->accepted, mc->addremove_probability,
+                        (double)mc->sys.pos.size(), mc->sys.E, (double)b.num_states,
+                        (double)b.t_last, mc->gamma_wl, (double)mc->lowest_hist,
+                        (double)mc->highest_hist, (double)mc->total_hist, b.max_S,
+                        (double)b.max_S_index, b.min, b.width, (double)b.max_N,
+                        (double)b.num_E, (double)b.num_addremove_attempts,
+                        (double)b.num_addremove_accepted};
+  for (int k = 0; k < 19; ++k) o[k] = v[k];
+}
+// The bins in the reference's layout (index E bin * (max_N + 1) + N); returns their count.
+int64_t orc_grand_bins(void* h, double* lnw, uint64_t* hist, uint64_t* wl_hist, uint8_t* visited,
+                       uint64_t* round_trips) {
+  auto* mc = (EnergyNumberMC<Lj>*)h;
+  const NBins& b = mc->bins;
+  const size_t n = b.lnw.size();
+  for (size_t i = 0; i < n; ++i) {
+    if (lnw) lnw[i] = b.lnw[i];
+    if (hist) hist[i] = b.histogram[i];
+    if (wl_hist) wl_hist[i] = mc->kind == 2 && i < mc->wl.histogram.size() ? mc->wl.histogram[i] : 0;
+    if (visited) visited[i] = b.visited[i];
+    if (round_trips) round_trips[i] = b.round_trips[i];
+  }
+  return (int64_t)n;
+}
+// Translation attempts and acceptances per N (max_N + 1 entries).
+void orc_grand_translation(void* h, uint64_t* attempts, uint64_t* accepted) {
+  auto* mc = (EnergyNumberMC<Lj>*)h;
+  for (size_t n = 0; n <= mc->bins.max_N; ++n) {
+    attempts[n] = mc->bins.num_translation_attempts[n];
+    accepted[n] = mc->bins.num_translation_accepted[n];
+  }
+}
+void orc_grand_draws(uint64_t seed, uint32_t walker, uint64_t t, double* dbl3, uint32_t* u2,
+                     float* g3, double* cand) {
+  const GrandDraws d = draws_grand(seed, walker, t);
+  dbl3[0] = d.u_choice; dbl3[1] = d.u;
+  u2[0] = d.add_bit; u2[1] = d.pick;
+  for (int a = 0; a < 3; ++a) g3[a] = d.g[a];
+  if (cand) add_candidate(seed, walker, t, 0, cand);
+}
+
 }  // extern "C"
+

@@ -91,13 +91,16 @@ struct Lj {
   double E = 0, error = 0;
   std::vector<V3> pos;
   double max_radius_squared = 0;
+  double max_radius = 0;
   double last_abs = 0;  // sum of lj_gross over the pair terms of the last plan
   bool have_change = false;
+  int ch_kind = 0;  // Change::Move / Add / Remove (lj.rs:56-74)
   size_t ch_which = 0;
   V3 ch_to{};
   double ch_e = 0;
 
   size_t n() const { return pos.size(); }
+  size_t num_atoms() const { return pos.size(); }
   double compute_energy() const {  // lj.rs:236-244
     double e = 0.0;
     for (size_t w = 0; w < pos.size(); ++w)
@@ -119,8 +122,41 @@ struct Lj {
       last_abs += lj_gross(rn) + lj_gross(ro);
     }
     have_change = true;
+    ch_kind = 0;
     ch_which = which;
     ch_to = r;
+    ch_e = e;
+    return e;
+  }
+  // compute_one_atom_energy (lj.rs:220-230) for an atom at r2 with index i (skipped)
+  double one_atom_energy(const V3& r2, size_t i) {
+    double e = 0.0;
+    last_abs = 0.0;
+    for (size_t j = 0; j < pos.size(); ++j) {
+      if (j == i) continue;
+      const double q = norm2(sub(pos[j], r2));
+      e += lj_potential(q);
+      last_abs += lj_gross(q);
+    }
+    return e;
+  }
+  // GrandSystem::plan_add (lj.rs:292-309) with the accepted point of the unit ball
+  double plan_add_at(const V3& unit) {
+    const double R = max_radius;  // r * self.max_radius (lj.rs:303)
+    const V3 to = {unit[0] * R, unit[1] * R, unit[2] * R};
+    const double e = E + one_atom_energy(to, pos.size());
+    have_change = true;
+    ch_kind = 1;
+    ch_to = to;
+    ch_e = e;
+    return e;
+  }
+  // GrandSystem::plan_remove (lj.rs:310-315)
+  double plan_remove(size_t which) {
+    const double e = E - one_atom_energy(pos[which], which);
+    have_change = true;
+    ch_kind = 2;
+    ch_which = which;
     ch_e = e;
     return e;
   }
@@ -148,9 +184,11 @@ struct Lj {
              f[2] + (double)d.g[2] * scale};
     return move_atom(which, to);
   }
-  void confirm() {  // lj.rs:339-358 (Move arm)
+  void confirm() {  // lj.rs:339-358
     if (!have_change) return;
-    pos[ch_which] = ch_to;
+    if (ch_kind == 0) pos[ch_which] = ch_to;
+    else if (ch_kind == 1) pos.push_back(ch_to);
+    else { pos[ch_which] = pos.back(); pos.pop_back(); }  // swap_remove
     have_change = false;
     set_energy(ch_e);
   }

@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "sadmc_grand.h"
 #include "sadmc_launch.h"
 #include "sadmc_surrogate.h"
 #include "sadmc_types.h"
@@ -298,6 +299,34 @@ std::vector<int> lpw_candidates(const sadmc_handle* h) {
 }
 
 }  // namespace
+
+struct sadmc_grand {
+  sadmc_grand_config cfg{};
+  int W = 0, np = 0, rows = 0, ncol = 0;
+  GrandCore* d_cores = nullptr;
+  void* plane_mem = nullptr;
+  GrandPlanes planes{};
+  float* d_pos = nullptr;
+  TraceRec* d_trace = nullptr;
+  uint64_t trace_cap = 0, trace_t0 = 0, moves_done = 0;
+  cudaStream_t stream = nullptr;
+  GrandLaunch launch() const {
+    GrandLaunch m{};
+    m.cores = d_cores; m.B = planes; m.pos = d_pos; m.np = np; m.rows = rows; m.ncol = ncol;
+    m.n_walkers = W; m.seed = cfg.seed;
+    m.width = cfg.energy_bin > 0 ? cfg.energy_bin : 1.0; m.inv_width = 1.0 / m.width;
+    m.radius = cfg.radius; m.radius2 = cfg.radius * cfg.radius; m.t0 = cfg.t0;
+    m.target_rate = cfg.target_rate;
+    m.translation_scale = cfg.acceptance_rate_mode ? 0.05 : cfg.translation_scale;
+    m.min_allowed = cfg.min_allowed; m.max_allowed = cfg.max_allowed;
+    m.has_min_allowed = cfg.has_min_allowed; m.has_max_allowed = cfg.has_max_allowed;
+    m.has_max_N = 1; m.max_N = cfg.max_N; m.acc_mode = cfg.acceptance_rate_mode;
+    m.trace = d_trace; m.trace_cap = trace_cap; m.trace_t0 = trace_t0;
+    m.resum_interval = cfg.resum_interval > 0 ? cfg.resum_interval : 2048;
+    m.drift_tol = cfg.drift_tol > 0 ? cfg.drift_tol : 1e-2;
+    return m;
+  }
+};
 
 extern "C" {
 
@@ -1320,4 +1349,186 @@ int32_t sadmc_heat_capacity(const double* T, int32_t nT, const double* E, const 
   return SADMC_OK;
 }
 
+
+// ---- energy-number MC (grand-canonical LJ cluster) ------------------------------------
+
+int32_t sadmc_grand_create(const sadmc_grand_config* c, sadmc_grand** out) {
+  if (!c || !out) return fail(SADMC_ERR_INVALID, "null argument");
+  if (c->n_walkers <= 0) return fail(SADMC_ERR_INVALID, "n_walkers must be positive");
+  if (c->method != SADMC_SAMC && c->method != SADMC_WL)
+    return fail(SADMC_ERR_INVALID, "the energy-number method supports SAMC and WL (energy_number.rs:18-27)");
+  if (c->max_N < 1 || c->max_N > 63)
+    return fail(SADMC_ERR_INVALID, "max_N (the cap on atoms) must be 1..63 on the GPU");
+  if (!(c->radius > 0)) return fail(SADMC_ERR_INVALID, "radius must be positive");
+  const double w = c->energy_bin > 0 ? c->energy_bin : 1.0;
+  if (!(c->e_hi > 0.0 && c->e_lo < 0.0)) return fail(SADMC_ERR_INVALID, "need e_lo < 0 < e_hi (walkers start empty, E = 0)");
+  auto* h = new sadmc_grand();
+  h->cfg = *c;
+  h->W = c->n_walkers;
+  h->np = c->max_N < 32 ? 32 : 64;
+  h->ncol = c->max_N + 1;
+  const int below = (int)std::ceil(-c->e_lo / w) + 2, above = (int)std::ceil(c->e_hi / w) + 2;
+  h->rows = below + above;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  const size_t W = h->W, cells = (size_t)h->rows * h->ncol;
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_cores, sizeof(GrandCore) * W);
+  if (e == cudaSuccess) e = cudaMalloc(&h->plane_mem, W * cells * 8 * 5 + W * h->ncol * 8 * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_pos, sizeof(float) * W * 6 * h->np);
+  if (e != cudaSuccess) { sadmc_grand_destroy(h); return fail(SADMC_ERR_NOMEM, cudaGetErrorString(e)); }
+  char* b = (char*)h->plane_mem;
+  h->planes.lnw = (double*)b;
+  h->planes.hist = (uint64_t*)(b + 1 * W * cells * 8);
+  h->planes.wl_hist = (uint64_t*)(b + 2 * W * cells * 8);
+  h->planes.visit = (uint64_t*)(b + 3 * W * cells * 8);
+  h->planes.round_trips = (uint64_t*)(b + 4 * W * cells * 8);
+  h->planes.tr_att = (uint64_t*)(b + 5 * W * cells * 8);
+  h->planes.tr_acc = h->planes.tr_att + W * h->ncol;
+  e = cudaMemsetAsync(h->plane_mem, 0, W * cells * 8 * 5 + W * h->ncol * 8 * 2, h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->d_pos, 0, sizeof(float) * W * 6 * h->np, h->stream);
+  // from_params (energy_number.rs:474-533) on the empty GrandLjParams system
+  std::vector<GrandCore> cores(W);
+  for (size_t k = 0; k < W; ++k) {
+    GrandCore& g = cores[k];
+    g = GrandCore{};
+    g.E = 0.0;
+    g.addremove_prob = c->acceptance_rate_mode ? 0.5 : c->addremove_probability;
+    g.min = 0.0 - w * 0.5;
+    g.gamma = 1.0;
+    g.num_states = 1;
+    g.t_last = 1;
+    g.lowest = 1;
+    g.highest = 1;
+    g.N = 0;
+    g.max_N_ref = 0;
+    g.num_E = 1;
+    g.e_base = below;
+    g.kind = c->method == SADMC_WL ? 2 : 1;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_cores, cores.data(), sizeof(GrandCore) * W, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = launch_grand_init(h->launch(), h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) { sadmc_grand_destroy(h); return fail(SADMC_ERR_CUDA, cudaGetErrorString(e)); }
+  *out = h;
+  return SADMC_OK;
+}
+
+int32_t sadmc_grand_destroy(sadmc_grand* h) {
+  if (!h) return SADMC_OK;
+  cudaFree(h->d_cores);
+  cudaFree(h->plane_mem);
+  cudaFree(h->d_pos);
+  cudaFree(h->d_trace);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return SADMC_OK;
+}
+
+int32_t sadmc_grand_set_trace(sadmc_grand* h, uint64_t capacity) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  cudaFree(h->d_trace);
+  h->d_trace = nullptr;
+  h->trace_cap = capacity;
+  h->trace_t0 = h->moves_done;
+  if (capacity) CUDA_TRY(cudaMalloc(&h->d_trace, sizeof(TraceRec) * capacity * h->W));
+  return SADMC_OK;
+}
+
+int32_t sadmc_grand_run(sadmc_grand* h, uint64_t moves) {
+  if (!h) return fail(SADMC_ERR_INVALID, "null handle");
+  GrandLaunch m = h->launch();
+  for (uint64_t left = moves; left > 0;) {
+    m.n_moves = std::min<uint64_t>(left, 8192);
+    CUDA_TRY(launch_grand_move(m, h->stream));
+    left -= m.n_moves;
+  }
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->moves_done += moves;
+  return SADMC_OK;
+}
+
+int32_t sadmc_grand_read_trace(sadmc_grand* h, int32_t walker, double* e1, double* e2, uint64_t* n) {
+  if (!h || walker < 0 || walker >= h->W || !n) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->d_trace) return fail(SADMC_ERR_STATE, "tracing disabled");
+  const uint64_t cnt = std::min<uint64_t>(h->trace_cap, h->moves_done - h->trace_t0);
+  *n = cnt;
+  if (!e1 && !e2) return SADMC_OK;
+  std::vector<TraceRec> r(cnt);
+  CUDA_TRY(cudaMemcpy(r.data(), h->d_trace + (size_t)walker * h->trace_cap, sizeof(TraceRec) * cnt, cudaMemcpyDeviceToHost));
+  for (uint64_t k = 0; k < cnt; ++k) {
+    if (e1) e1[k] = r[k].e1;
+    if (e2) e2[k] = r[k].e2;
+  }
+  return SADMC_OK;
+}
+
+int32_t sadmc_grand_read_state(sadmc_grand* h, int32_t walker, double* pos, int32_t* n) {
+  if (!h || walker < 0 || walker >= h->W || !n) return fail(SADMC_ERR_INVALID, "bad argument");
+  GrandCore g;
+  CUDA_TRY(cudaMemcpy(&g, h->d_cores + walker, sizeof(g), cudaMemcpyDeviceToHost));
+  *n = g.N;
+  if (pos) {
+    std::vector<float> p(6 * (size_t)h->np);
+    CUDA_TRY(cudaMemcpy(p.data(), h->d_pos + (size_t)walker * 6 * h->np, sizeof(float) * p.size(), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < g.N; ++j)
+      for (int a = 0; a < 3; ++a)
+        pos[3 * j + a] = (double)p[(size_t)a * h->np + j] + (double)p[(size_t)(3 + a) * h->np + j];
+  }
+  return SADMC_OK;
+}
+
+int32_t sadmc_grand_read_scalars(sadmc_grand* h, int32_t walker, double* o) {
+  if (!h || !o || walker < 0 || walker >= h->W) return fail(SADMC_ERR_INVALID, "bad argument");
+  GrandCore g;
+  CUDA_TRY(cudaMemcpy(&g, h->d_cores + walker, sizeof(g), cudaMemcpyDeviceToHost));
+  const double w = h->cfg.energy_bin > 0 ? h->cfg.energy_bin : 1.0;
+  const double v[SADMC_GRAND_N_SCALARS] = {
+      (double)g.moves, (double)g.accepted, g.addremove_prob, (double)g.N, g.E,
+      (double)g.num_states, (double)g.t_last, g.gamma, (double)g.lowest, (double)g.highest,
+      (double)g.total, g.max_S, (double)g.max_S_index, g.min, w, (double)g.max_N_ref,
+      (double)g.num_E, (double)g.ar_attempts, (double)g.ar_accepted, g.drift, (double)g.status};
+  for (int k = 0; k < SADMC_GRAND_N_SCALARS; ++k) o[k] = v[k];
+  return SADMC_OK;
+}
+
+int32_t sadmc_grand_read_bins(sadmc_grand* h, int32_t walker, double* lnw, uint64_t* hist,
+                              uint64_t* wl_hist, uint8_t* visited, uint64_t* round_trips,
+                              int64_t* n_e, int64_t* n_n) {
+  if (!h || walker < 0 || walker >= h->W || !n_e || !n_n) return fail(SADMC_ERR_INVALID, "bad argument");
+  GrandCore g;
+  CUDA_TRY(cudaMemcpy(&g, h->d_cores + walker, sizeof(g), cudaMemcpyDeviceToHost));
+  *n_e = g.num_E;
+  *n_n = g.max_N_ref + 1;
+  if (!lnw && !hist && !wl_hist && !visited && !round_trips) return SADMC_OK;
+  const size_t cells = (size_t)h->rows * h->ncol, off = (size_t)walker * cells;
+  std::vector<double> L(cells);
+  std::vector<uint64_t> H(cells), WH(cells), V(cells), R(cells);
+  CUDA_TRY(cudaMemcpy(L.data(), h->planes.lnw + off, cells * 8, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(H.data(), h->planes.hist + off, cells * 8, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(WH.data(), h->planes.wl_hist + off, cells * 8, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(V.data(), h->planes.visit + off, cells * 8, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(R.data(), h->planes.round_trips + off, cells * 8, cudaMemcpyDeviceToHost));
+  const int nn = g.max_N_ref + 1;
+  for (int k = 0; k < g.num_E; ++k)
+    for (int q = 0; q < nn; ++q) {
+      const size_t src = (size_t)(g.e_base + k) * h->ncol + q, dst = (size_t)k * nn + q;
+      if (lnw) lnw[dst] = L[src];
+      if (hist) hist[dst] = H[src];
+      if (wl_hist) wl_hist[dst] = WH[src];
+      if (visited) visited[dst] = (V[src] >> 1) == g.fill_gen ? (uint8_t)(V[src] & 1) : (uint8_t)(g.fill_val != 0);
+      if (round_trips) round_trips[dst] = R[src];
+    }
+  return SADMC_OK;
+}
+
+int32_t sadmc_grand_translation_counts(sadmc_grand* h, int32_t walker, uint64_t* attempts,
+                                       uint64_t* accepted) {
+  if (!h || walker < 0 || walker >= h->W || !attempts || !accepted) return fail(SADMC_ERR_INVALID, "bad argument");
+  GrandCore g;
+  CUDA_TRY(cudaMemcpy(&g, h->d_cores + walker, sizeof(g), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(attempts, h->planes.tr_att + (size_t)walker * h->ncol, sizeof(uint64_t) * (g.max_N_ref + 1), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(accepted, h->planes.tr_acc + (size_t)walker * h->ncol, sizeof(uint64_t) * (g.max_N_ref + 1), cudaMemcpyDeviceToHost));
+  return SADMC_OK;
+}
+
 }  // extern "C"
+

@@ -136,6 +136,44 @@ __device__ __forceinline__ Draws draws_ising(uint64_t seed, uint32_t walker, uin
   return d;
 }
 
+// Draws of one energy-number move (src/mc/energy_number.rs:540-606), Philox stream pair 2
+// (counter word 2 = 4, 5, 6): translate iff u_choice > addremove probability, add iff
+// add_bit == 0, the atom to move or remove is mulhi_range(pick, N), three normals, and
+// the Metropolis uniform.
+struct GrandDraws {
+  uint64_t u_choice53, u53;
+  uint32_t add_bit, pick;
+  float g0, g1, g2;
+};
+__device__ __forceinline__ GrandDraws draws_grand(uint64_t seed, uint32_t walker, uint64_t t) {
+  const uint32_t k0 = walker, k1 = (uint32_t)seed, shi = (uint32_t)(seed >> 32);
+  const Philox4 A = philox4x32_10(Philox4{(uint32_t)t, (uint32_t)(t >> 32), 4u, shi}, k0, k1);
+  const Philox4 B = philox4x32_10(Philox4{(uint32_t)t, (uint32_t)(t >> 32), 5u, shi}, k0, k1);
+  const Philox4 C = philox4x32_10(Philox4{(uint32_t)t, (uint32_t)(t >> 32), 6u, shi}, k0, k1);
+  GrandDraws d;
+  d.u_choice53 = u53_bits(A.x, A.y);
+  d.add_bit = A.z & 1u;
+  d.pick = A.w;
+  float z3;
+  normal_pair(B.x, B.y, d.g0, d.g1);
+  normal_pair(B.z, B.w, d.g2, z3);
+  (void)z3;
+  d.u53 = u53_bits(C.x, C.y);
+  return d;
+}
+// Candidate k of an LJ add, uniform in (-1, 1)^3 (lj.rs:294-302), counter word 2 = 8 + 2k
+// and 9 + 2k.
+__device__ __forceinline__ void add_candidate(uint64_t seed, uint32_t walker, uint64_t t, int k,
+                                              double& x, double& y, double& z) {
+  const uint32_t k0 = walker, k1 = (uint32_t)seed, shi = (uint32_t)(seed >> 32);
+  const Philox4 D = philox4x32_10(Philox4{(uint32_t)t, (uint32_t)(t >> 32), 8u + 2u * (uint32_t)k, shi}, k0, k1);
+  const Philox4 E = philox4x32_10(Philox4{(uint32_t)t, (uint32_t)(t >> 32), 9u + 2u * (uint32_t)k, shi}, k0, k1);
+  const double s53 = 1.0 / 9007199254740992.0;
+  x = -1.0 + 2.0 * ((double)u53_bits(D.x, D.y) * s53);
+  y = -1.0 + 2.0 * ((double)u53_bits(D.z, D.w) * s53);
+  z = -1.0 + 2.0 * ((double)u53_bits(E.x, E.y) * s53);
+}
+
 // Lane glane of a walker's group holds the draws of move base + glane; a move reads its
 // draws with six group shuffles, so Philox and Box-Muller run once per LPW moves.
 template <int LPW, bool ISING>

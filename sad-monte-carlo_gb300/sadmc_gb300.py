@@ -109,6 +109,13 @@ def lib():
         "sadmc_surrogate_loss_grads": (I32, [P, P, P, I32, P, P]),
         "sadmc_surrogate_loss_grads_noalloc": (I32, [P, P, P, I32, P, P, P]),
         "sadmc_check_numerics": (I32, [U64, U64, P, P]),
+        "sadmc_grand_create": (I32, [P, P]), "sadmc_grand_destroy": (I32, [P]),
+        "sadmc_grand_run": (I32, [P, U64]), "sadmc_grand_set_trace": (I32, [P, U64]),
+        "sadmc_grand_read_trace": (I32, [P, I32, P, P, P]),
+        "sadmc_grand_read_state": (I32, [P, I32, P, P]),
+        "sadmc_grand_read_scalars": (I32, [P, I32, P]),
+        "sadmc_grand_read_bins": (I32, [P, I32, P, P, P, P, P, P, P]),
+        "sadmc_grand_translation_counts": (I32, [P, I32, P, P]),
         "sadmc_surrogate_predict": (I32, [P, P, I32, P]),
         "sadmc_run_da": (I32, [P, U64, I32, P]),
         "sadmc_draws": (I32, [I32, ctypes.c_uint32, U64, ctypes.c_uint32, U64, I32, ctypes.c_uint32,
@@ -426,6 +433,106 @@ def heat_capacity(T, E, S):
     C = np.zeros(len(T))
     _check(lib().sadmc_heat_capacity(_p(T), len(T), _p(E), _p(S), len(E), _p(C)))
     return C
+
+
+class GrandConfig(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int32), ("n_walkers", ctypes.c_int32),
+                ("max_N", ctypes.c_int32), ("acceptance_rate_mode", ctypes.c_int32),
+                ("t0", ctypes.c_double), ("energy_bin", ctypes.c_double),
+                ("radius", ctypes.c_double),
+                ("has_min_allowed", ctypes.c_int32), ("has_max_allowed", ctypes.c_int32),
+                ("min_allowed", ctypes.c_double), ("max_allowed", ctypes.c_double),
+                ("target_rate", ctypes.c_double), ("translation_scale", ctypes.c_double),
+                ("addremove_probability", ctypes.c_double),
+                ("e_lo", ctypes.c_double), ("e_hi", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("resum_interval", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("drift_tol", ctypes.c_double)]
+
+
+GRAND_SCALARS = ["moves", "accepted", "addremove_probability", "N", "energy", "num_states",
+                 "t_last", "gamma", "lowest_hist", "highest_hist", "total_hist", "max_S",
+                 "max_S_index", "min", "width", "max_N", "num_E", "addremove_attempts",
+                 "addremove_accepted", "drift", "status"]
+
+
+def make_grand_config(n_walkers, max_N, radius, *, method=SAMC, t0=1e4, energy_bin=1.0,
+                      min_allowed=None, max_allowed=None, target_rate=None,
+                      translation_scale=0.05, addremove_probability=0.05, e_lo=-200.0,
+                      e_hi=50.0, seed=0, resum_interval=0, drift_tol=0.0):
+    c = GrandConfig()
+    c.method, c.n_walkers, c.max_N = method, n_walkers, max_N
+    c.acceptance_rate_mode, c.target_rate = int(target_rate is not None), target_rate or 0.5
+    c.t0, c.energy_bin, c.radius = t0, energy_bin, radius
+    c.has_min_allowed, c.min_allowed = int(min_allowed is not None), min_allowed or 0.0
+    c.has_max_allowed = int(max_allowed is not None)
+    c.max_allowed = max_allowed if max_allowed is not None else 0.0
+    c.translation_scale, c.addremove_probability = translation_scale, addremove_probability
+    c.e_lo, c.e_hi, c.seed = e_lo, e_hi, seed
+    c.resum_interval, c.drift_tol = resum_interval, drift_tol
+    return c
+
+
+class GrandBatch:
+    """Energy-number walkers of a grand-canonical LJ cluster (one sadmc_grand handle)."""
+
+    def __init__(self, cfg):
+        self.cfg = cfg
+        self.h = ctypes.c_void_p()
+        _check(lib().sadmc_grand_create(ctypes.byref(cfg), ctypes.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().sadmc_grand_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, moves):
+        _check(lib().sadmc_grand_run(self.h, int(moves)))
+
+    def set_trace(self, capacity):
+        _check(lib().sadmc_grand_set_trace(self.h, int(capacity)))
+
+    def trace(self, w, n):
+        e1, e2 = np.zeros(n), np.zeros(n)
+        cnt = ctypes.c_uint64(0)
+        _check(lib().sadmc_grand_read_trace(self.h, w, _p(e1), _p(e2), ctypes.byref(cnt)))
+        return e1[:cnt.value], e2[:cnt.value]
+
+    def state(self, w):
+        n = ctypes.c_int32(0)
+        out = np.zeros((64, 3))
+        _check(lib().sadmc_grand_read_state(self.h, w, _p(out), ctypes.byref(n)))
+        return out[:n.value]
+
+    def scalars(self, w):
+        o = np.zeros(len(GRAND_SCALARS))
+        _check(lib().sadmc_grand_read_scalars(self.h, w, _p(o)))
+        return dict(zip(GRAND_SCALARS, o))
+
+    def bins(self, w):
+        ne, nn = ctypes.c_int64(0), ctypes.c_int64(0)
+        _check(lib().sadmc_grand_read_bins(self.h, w, None, None, None, None, None,
+                                          ctypes.byref(ne), ctypes.byref(nn)))
+        n = ne.value * nn.value
+        lnw = np.zeros(n)
+        hist, wlh, rt = (np.zeros(n, np.uint64) for _ in range(3))
+        vis = np.zeros(n, np.uint8)
+        _check(lib().sadmc_grand_read_bins(self.h, w, _p(lnw), _p(hist), _p(wlh), _p(vis), _p(rt),
+                                          ctypes.byref(ne), ctypes.byref(nn)))
+        shape = (ne.value, nn.value)
+        return dict(lnw=lnw.reshape(shape), hist=hist.reshape(shape), wl_hist=wlh.reshape(shape),
+                    visited=vis.reshape(shape), round_trips=rt.reshape(shape))
+
+    def translation_counts(self, w):
+        nn = int(self.scalars(w)["max_N"]) + 1
+        a, b = np.zeros(nn, np.uint64), np.zeros(nn, np.uint64)
+        _check(lib().sadmc_grand_translation_counts(self.h, w, _p(a), _p(b)))
+        return a, b
 
 
 def check_numerics(n, seed=1):

@@ -107,6 +107,31 @@ def test_wca_pressure_datum(oracle):
     assert int(np.nonzero(c)[0][0]) == int((w.energy() - b["min"]) / b["width"])
 
 
+@pytest.mark.parametrize("method", ["samc", "wl"])
+def test_grand_energy_number_invariants(oracle, method):
+    """The energy-number walker (src/mc/energy_number.rs) on the grand-canonical LJ
+    cluster (lj.rs:291-319): the incremental energy equals compute_energy, N stays within
+    max_N, every move is counted once, the histogram holds every visit."""
+    m = oracle.M_SAMC if method == "samc" else oracle.M_WL
+    w = oracle.GrandWalker(oracle.make_grand_config(2.5, method=m, t0=500.0, energy_bin=0.5,
+                                                    max_N=10, max_allowed=5.0, seed=4,
+                                                    translation_scale=0.1,
+                                                    addremove_probability=0.2))
+    moves = 60000
+    w.run(moves)
+    s = w.scalars()
+    assert 0 <= s["N"] <= 10 and s["max_N"] <= 10
+    assert s["energy"] == pytest.approx(w.compute_energy(), rel=1e-9, abs=1e-9)
+    assert len(w.state()) == s["N"]
+    b = w.bins()
+    assert int(b["hist"].sum()) == moves + 1            # the initial bin starts at 1
+    att, acc = w.translation_counts()
+    assert int(att.sum()) + s["addremove_attempts"] == moves
+    assert int(acc.sum()) + s["addremove_accepted"] == s["accepted"]
+    assert (b["lnw"][b["hist"] > 0] > 0).all()
+    assert (b["lnw"][b["hist"] == 0] == 0).all()
+
+
 def test_max_balls_within(oracle):
     # optsquare.rs:290-322 counts lattice points of its own construction
     assert oracle.max_balls_within(1.3) == 6
