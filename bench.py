@@ -82,6 +82,7 @@ def other_configs(G, seed=11):
                 [(L, 0.0, (0, 0, 0))])
     b.upload([np.where(rng.random(L * L) < 0.5, -1.0, 1.0)])
     b.initialize()
+    b.autotune(20000)
     mv = 1_000_000
     sec = _time_run(b, mv, 100_000)
     out["C1"] = {"workload": "Ising 32x32, plain SAD (min_T 0.2), 1 walker", "moves": mv,
@@ -107,6 +108,7 @@ def other_configs(G, seed=11):
                               seed=seed, resum_interval=4096), geo)
     b.upload(states)
     b.initialize()
+    b.autotune(256)
     mv = 2048
     sec = _time_run(b, mv, 512)
     out["C3"] = {"workload": "WCA, N in {64,128,256,512}, density U[0.6,0.9], 2048 walkers, "
@@ -132,6 +134,7 @@ def other_configs(G, seed=11):
                               well_width=1.3, translation_scale=0.05, seed=seed), geo)
     b.upload(states)
     b.initialize()
+    b.autotune(256)
     mv = 2048
     sec = _time_run(b, mv, 512)
     out["C5"] = {"workload": "hard-core square well lambda=1.3, N=1024, packing U[0.30,0.50], "
@@ -139,6 +142,25 @@ def other_configs(G, seed=11):
                  "moves": W5 * mv, "moves_per_s": W5 * mv / sec,
                  "lanes_per_walker": b.lanes_per_walker()}
     b.close()
+    # grand-canonical LJ cluster, energy-number SAMC (src/mc/energy_number.rs), walkers
+    # start empty and grow to at most 31 atoms in a sphere of radius 2.5
+    import torch
+    Wg = 4096
+    gb = G.GrandBatch(G.make_grand_config(Wg, 31, 2.5, method=G.SAMC, t0=1e4, energy_bin=0.5,
+                                          max_allowed=10.0, translation_scale=0.1,
+                                          addremove_probability=0.1, e_lo=-150.0, e_hi=12.0,
+                                          seed=seed))
+    gb.run(4096)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mv = 4096
+    gb.run(mv)
+    sec = time.perf_counter() - t0
+    out["grand"] = {"workload": "grand-canonical LJ cluster (R=2.5, N <= 31), energy-number SAMC "
+                                "t0=1e4, 4096 walkers, one warp per walker",
+                    "moves": Wg * mv, "moves_per_s": Wg * mv / sec,
+                    "mean_N": float(np.mean([gb.scalars(w)["N"] for w in range(0, Wg, 256)]))}
+    gb.close()
     return out
 
 
