@@ -257,21 +257,23 @@ int32_t sadmc_draws(int32_t system, uint32_t n, uint64_t seed, uint32_t walker, 
 int32_t sadmc_heat_capacity(const double* T, int32_t nT, const double* E, const double* S,
                             int32_t n, double* C);
 
-/* ---- Grand-canonical LJ cluster with the energy-number method ----------------------
- * EnergyNumberMC<Lj> (src/mc/energy_number.rs) with the GrandSystem moves of
- * src/system/lj.rs:291-319: translations, adds at a uniform point of the sphere and
- * removals of a uniform atom, weighted by ln w(E, N) (SAMC or Wang-Landau).  Every walker
- * starts empty (E = 0, N = 0), as GrandLjParams does.  The bins are returned in the
- * reference's layout: index = E row * (max_N + 1) + N, rows from bins.min. */
+/* ---- Grand-canonical systems with the energy-number method ------------------------
+ * EnergyNumberMC<S> (src/mc/energy_number.rs) for the LJ cluster (GrandSystem of
+ * src/system/lj.rs:291-319: adds at a uniform point of the sphere) or the WCA fluid
+ * (wca.rs:307-323: adds at a uniform point of the periodic box, subcell lists):
+ * translations, adds and removals of a uniform atom, weighted by ln w(E, N) (SAMC or
+ * Wang-Landau).  Every walker starts empty (E = 0, N = 0), as GrandLjParams / WcaParams
+ * do.  The bins are returned in the reference's layout: index = E row * (max_N + 1) + N,
+ * rows from bins.min. */
 typedef struct sadmc_grand sadmc_grand;
 typedef struct sadmc_grand_config {
   int32_t method;            /* SADMC_SAMC or SADMC_WL (energy_number.rs:18-27) */
   int32_t n_walkers;
-  int32_t max_N;             /* EnergyNumberMCParams::max_N, required here (1..63) */
+  int32_t max_N;             /* EnergyNumberMCParams::max_N, required here (LJ 1..63, WCA 1..1024) */
   int32_t acceptance_rate_mode; /* MoveParams::AcceptanceRate(target_rate), else _Explicit */
   double t0;                 /* SAMC t0 */
   double energy_bin;         /* bin width (default 1.0) */
-  double radius;             /* LJ spherical wall radius (GrandLjParams::radius) */
+  double radius;             /* LJ: spherical wall radius (GrandLjParams::radius) */
   int32_t has_min_allowed, has_max_allowed;
   double min_allowed, max_allowed;
   double target_rate;
@@ -280,8 +282,9 @@ typedef struct sadmc_grand_config {
   double e_lo, e_hi;         /* energies the preallocated bins must cover (e_lo < 0 < e_hi) */
   uint64_t seed;
   int32_t resum_interval;    /* moves between FP64 energy re-sums; 0 = 2048 */
-  int32_t pad;
+  int32_t system;            /* SADMC_LJ or SADMC_WCA */
   double drift_tol;          /* 0 = 1e-2 */
+  double box[3];             /* WCA: periodic box (at least 3 subcells of 2^(1/6) per axis) */
 } sadmc_grand_config;
 int32_t sadmc_grand_create(const sadmc_grand_config* cfg, sadmc_grand** out);
 int32_t sadmc_grand_destroy(sadmc_grand* h);

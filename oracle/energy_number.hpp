@@ -64,6 +64,37 @@ inline void add_candidate(uint64_t seed, uint32_t walker, uint64_t t, int k, dou
   out[2] = -1.0 + 2.0 * u53(E.x, E.y);
 }
 
+// A uniform point of the periodic box for a WCA add (wca.rs:309-313: Uniform::new(0, L)
+// per axis, then put_in_cell), from the words of add candidate 0.
+inline V3 add_point_box(uint64_t seed, uint32_t walker, uint64_t t, const V3& box) {
+  const uint32_t k0 = walker, k1 = (uint32_t)seed, shi = (uint32_t)(seed >> 32);
+  U4 D = philox4x32_10(U4{(uint32_t)t, (uint32_t)(t >> 32), 8u, shi}, k0, k1);
+  U4 E = philox4x32_10(U4{(uint32_t)t, (uint32_t)(t >> 32), 9u, shi}, k0, k1);
+  return {box[0] * u53(D.x, D.y), box[1] * u53(D.z, D.w), box[2] * u53(E.x, E.y)};
+}
+
+// The system-specific moves of move_once: translation (plan_move), add, remove.
+inline std::optional<double> grand_translate(Lj& s, size_t which, const float g[3], double sc) {
+  const V3& f = s.pos[which];  // lj.rs:365-374
+  return s.move_atom(which, {f[0] + (double)g[0] * sc, f[1] + (double)g[1] * sc, f[2] + (double)g[2] * sc});
+}
+inline std::optional<double> grand_translate(Wca& s, size_t which, const float g[3], double sc) {
+  const V3& f = s.cell.pos[which];  // wca.rs:342-353
+  return s.move_atom(which, s.cell.put_in_cell({f[0] + (double)g[0] * sc, f[1] + (double)g[1] * sc,
+                                                f[2] + (double)g[2] * sc}));
+}
+inline std::optional<double> grand_add(Lj& s, uint64_t seed, uint32_t walker, uint64_t t) {
+  double c[3];  // lj.rs:292-309
+  for (int k = 0; k < kAddTries; ++k) {
+    add_candidate(seed, walker, t, k, c);
+    if (c[0] * c[0] + c[1] * c[1] + c[2] * c[2] < 1.0) return s.plan_add_at({c[0], c[1], c[2]});
+  }
+  return std::nullopt;
+}
+inline std::optional<double> grand_add(Wca& s, uint64_t seed, uint32_t walker, uint64_t t) {
+  return s.plan_add_at(s.cell.put_in_cell(add_point_box(seed, walker, t, s.cell.box)));
+}
+
 // Bins of energy_number.rs:115-150, 225-300
 struct NBins {
   double min = 0, width = 1;
@@ -274,13 +305,8 @@ struct EnergyNumberMC {
     if (d.u_choice > addremove_probability) {
       bins.num_translation_attempts[N1] += 1;
       std::optional<double> e2;
-      if (N1 > 0) {
-        const size_t which = mulhi_range(d.pick, (uint32_t)N1);
-        const auto& f = sys.pos[which];
-        const double sc = bins.translation_scale[N1];
-        V3 to = {f[0] + (double)d.g[0] * sc, f[1] + (double)d.g[1] * sc, f[2] + (double)d.g[2] * sc};
-        e2 = sys.move_atom(which, to);
-      }
+      if (N1 > 0)
+        e2 = grand_translate(sys, mulhi_range(d.pick, (uint32_t)N1), d.g, bins.translation_scale[N1]);
       if (e2) {
         const double E2 = given(*e2);
         if (!oob(E2, E1)) {
@@ -301,14 +327,7 @@ struct EnergyNumberMC {
       size_t N2 = 0;
       if (d.add_bit == 0) {
         if (!(has_max_N && N1 == max_N)) {
-          double c[3];
-          for (int k = 0; k < kAddTries; ++k) {
-            add_candidate(seed, walker, moves, k, c);
-            if (c[0] * c[0] + c[1] * c[1] + c[2] * c[2] < 1.0) {
-              e2 = sys.plan_add_at({c[0], c[1], c[2]});
-              break;
-            }
-          }
+          e2 = grand_add(sys, seed, walker, moves);
           N2 = N1 + 1;
         }
       } else if (N1 > 0) {

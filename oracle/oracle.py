@@ -71,6 +71,7 @@ def lib():
             "orc_grand_compute_energy": (D, [P]), "orc_grand_scalars": (None, [P, P]),
             "orc_grand_bins": (I64, [P, P, P, P, P, P]),
             "orc_grand_translation": (None, [P, P, P]),
+            "orc_grand_check_cells": (I64, [P]),
             "orc_grand_draws": (None, [U64, ctypes.c_uint32, U64, P, P, P, P]),
             "orc_verify_energy": (ctypes.c_int, [P]),
             "orc_get_state": (None, [P, P]),
@@ -231,9 +232,10 @@ class GrandConfig(ctypes.Structure):
                 ("has_max_N", ctypes.c_int32), ("max_N", ctypes.c_int32),
                 ("has_min_allowed", ctypes.c_int32), ("has_max_allowed", ctypes.c_int32),
                 ("min_allowed", ctypes.c_double), ("max_allowed", ctypes.c_double),
-                ("acc_mode", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("acc_mode", ctypes.c_int32), ("system", ctypes.c_int32),
                 ("target_rate", ctypes.c_double), ("translation_scale", ctypes.c_double),
                 ("addremove_probability", ctypes.c_double), ("radius", ctypes.c_double),
+                ("box", ctypes.c_double * 3),
                 ("seed", ctypes.c_uint64), ("walker", ctypes.c_uint32), ("pad2", ctypes.c_uint32)]
 
 
@@ -243,10 +245,14 @@ GRAND_SCALARS = ["moves", "accepted", "addremove_probability", "N", "energy", "n
                  "addremove_accepted"]
 
 
-def make_grand_config(radius, *, method=M_SAMC, t0=1e4, energy_bin=None, max_N=None,
-                      min_allowed=None, max_allowed=None, target_rate=None,
+def make_grand_config(radius=0.0, *, box=None, method=M_SAMC, t0=1e4, energy_bin=None,
+                      max_N=None, min_allowed=None, max_allowed=None, target_rate=None,
                       translation_scale=0.05, addremove_probability=0.05, seed=0, walker=0):
+    """Energy-number walker: the LJ cluster of `radius`, or (box given) the WCA fluid."""
     c = GrandConfig()
+    c.system = 2 if box is not None else 1
+    if box is not None:
+        c.box[0], c.box[1], c.box[2] = box
     c.kind = method
     c.t0 = t0
     c.has_energy_bin, c.energy_bin = int(energy_bin is not None), energy_bin or 0.0
@@ -312,6 +318,10 @@ class GrandWalker:
         return dict(lnw=lnw.reshape(-1, nN), hist=hist.reshape(-1, nN), wl_hist=wlh.reshape(-1, nN),
                     visited=vis.reshape(-1, nN), round_trips=rt.reshape(-1, nN), min=s["min"],
                     width=s["width"])
+
+    def check_cells(self):
+        """Subcells whose lists differ from a rebuild (WCA; 0 for the LJ cluster)."""
+        return lib().orc_grand_check_cells(self.h)
 
     def translation_counts(self):
         nN = int(self.scalars()["max_N"]) + 1

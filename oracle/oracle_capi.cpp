@@ -1,6 +1,7 @@
 // ORACLE / TEST INFRASTRUCTURE ONLY.  ctypes-facing C API over the FP64 restatement
 // (systems.hpp, energy_mc.hpp).  Only tests/, __graft_entry__.smoke() and bench.py's
 // CPU-baseline leg load this library; the CUDA product never links it.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstring>
@@ -513,7 +514,7 @@ double orc_bench(const orc_config* cfgs, const double* const* states, int32_t nw
 }
 
 
-// ---- energy-number MC (grand-canonical LJ cluster), src/mc/energy_number.rs -----------
+// ---- energy-number MC (grand-canonical LJ cluster / WCA fluid), src/mc/energy_number.rs
 typedef struct orc_grand_config {
   int32_t kind;            // 1 SAMC, 2 WL
   int32_t has_energy_bin;
@@ -522,18 +523,31 @@ typedef struct orc_grand_config {
   int32_t has_max_N, max_N;
   int32_t has_min_allowed, has_max_allowed;
   double min_allowed, max_allowed;
-  int32_t acc_mode, pad;
+  int32_t acc_mode, system;  // system: 1 LJ cluster, 2 WCA fluid
   double target_rate, translation_scale, addremove_probability;
-  double radius;
+  double radius;           // LJ
+  double box[3];           // WCA
   uint64_t seed;
   uint32_t walker, pad2;
 } orc_grand_config;
 
+}  // extern "C"
+
+namespace {
+inline const std::vector<V3>& grand_positions(const Lj& s) { return s.pos; }
+inline const std::vector<V3>& grand_positions(const Wca& s) { return s.cell.pos; }
+struct AnyGrand {
+  int system = 1;
+  std::unique_ptr<EnergyNumberMC<Lj>> lj;
+  std::unique_ptr<EnergyNumberMC<Wca>> wca;
+  template <class F>
+  auto visit(F&& f) { return system == 1 ? f(*lj) : f(*wca); }
+};
+}  // namespace
+
+extern "C" {
+
 void* orc_grand_create(const orc_grand_config* c) {
-  Lj s;
-  s.max_radius_squared = c->radius * c->radius;
-  s.max_radius = c->radius;
-  s.E = 0.0;
   NumberParams p;
   p.kind = c->kind;
   p.t0 = c->t0;
@@ -549,75 +563,128 @@ void* orc_grand_create(const orc_grand_config* c) {
   p.target_rate = c->target_rate;
   p.translation_scale = c->translation_scale;
   p.addremove_probability = c->addremove_probability;
-  auto* mc = new EnergyNumberMC<Lj>();
-  mc->init(std::move(s), p, c->seed, c->walker);
-  return mc;
+  auto* h = new AnyGrand();
+  h->system = c->system == 2 ? 2 : 1;
+  if (h->system == 1) {
+    Lj s;
+    s.max_radius_squared = c->radius * c->radius;
+    s.max_radius = c->radius;
+    s.E = 0.0;
+    h->lj.reset(new EnergyNumberMC<Lj>());
+    h->lj->init(std::move(s), p, c->seed, c->walker);
+  } else {
+    Wca s;  // wca.rs:368-390 on an empty box
+    s.cell.box = {c->box[0], c->box[1], c->box[2]};
+    s.cell.r_cutoff = wca_r_cutoff();
+    s.cell.update_caches();
+    s.E = 0.0;
+    h->wca.reset(new EnergyNumberMC<Wca>());
+    h->wca->init(std::move(s), p, c->seed, c->walker);
+  }
+  return h;
 }
-void orc_grand_destroy(void* h) { delete (EnergyNumberMC<Lj>*)h; }
+void orc_grand_destroy(void* h) { delete (AnyGrand*)h; }
 void orc_grand_run(void* h, uint64_t n) {
-  auto* mc = (EnergyNumberMC<Lj>*)h;
-  for (uint64_t k = 0; k < n; ++k) mc->move_once();
+  ((AnyGrand*)h)->visit([&](auto& mc) {
+    for (uint64_t k = 0; k < n; ++k) mc.move_once();
+    return 0;
+  });
 }
 double orc_grand_run_override(void* h, uint64_t n, const double* e1, const double* e2,
                               uint64_t* mismatch) {
-  auto* mc = (EnergyNumberMC<Lj>*)h;
-  mc->e1_override = e1;
-  mc->e2_override = e2;
-  mc->override_base = mc->moves;
-  for (uint64_t k = 0; k < n; ++k) mc->move_once();
-  mc->e1_override = mc->e2_override = nullptr;
-  if (mismatch) *mismatch = mc->override_mismatch;
-  return mc->max_e2_discrepancy;
+  return ((AnyGrand*)h)->visit([&](auto& mc) {
+    mc.e1_override = e1;
+    mc.e2_override = e2;
+    mc.override_base = mc.moves;
+    for (uint64_t k = 0; k < n; ++k) mc.move_once();
+    mc.e1_override = mc.e2_override = nullptr;
+    if (mismatch) *mismatch = mc.override_mismatch;
+    return mc.max_e2_discrepancy;
+  });
 }
 void orc_grand_worst(void* h, double* out4) {
-  auto* mc = (EnergyNumberMC<Lj>*)h;
-  for (int k = 0; k < 4; ++k) out4[k] = mc->worst[k];
+  ((AnyGrand*)h)->visit([&](auto& mc) {
+    for (int k = 0; k < 4; ++k) out4[k] = mc.worst[k];
+    return 0;
+  });
 }
 int64_t orc_grand_state(void* h, double* pos) {
-  auto* mc = (EnergyNumberMC<Lj>*)h;
-  if (pos)
-    for (size_t i = 0; i < mc->sys.pos.size(); ++i)
-      for (int a = 0; a < 3; ++a) pos[3 * i + a] = mc->sys.pos[i][a];
-  return (int64_t)mc->sys.pos.size();
+  return ((AnyGrand*)h)->visit([&](auto& mc) {
+    const auto& P = grand_positions(mc.sys);
+    if (pos)
+      for (size_t i = 0; i < P.size(); ++i)
+        for (int a = 0; a < 3; ++a) pos[3 * i + a] = P[i][a];
+    return (int64_t)P.size();
+  });
 }
-double orc_grand_compute_energy(void* h) { return ((EnergyNumberMC<Lj>*)h)->sys.compute_energy(); }
+double orc_grand_compute_energy(void* h) {
+  return ((AnyGrand*)h)->visit([&](auto& mc) { return mc.sys.compute_energy(); });
+}
 // moves, accepted, addremove_probability, N, E, num_states, t_last, gamma (WL), lowest,
 // highest, total (WL), max_S, max_S_index, bins.min, width, max_N, num_E, add/remove
 // attempts, add/remove accepted
 void orc_grand_scalars(void* h, double* o) {
-  auto* mc = (EnergyNumberMC<Lj>*)h;
-  const NBins& b = mc->bins;
-  const double v[19] = {(double)mc->moves, (double)mc->accepted, mc->addremove_probability,
-                        (double)mc->sys.pos.size(), mc->sys.E, (double)b.num_states,
-                        (double)b.t_last, mc->gamma_wl, (double)mc->lowest_hist,
-                        (double)mc->highest_hist, (double)mc->total_hist, b.max_S,
-                        (double)b.max_S_index, b.min, b.width, (double)b.max_N,
-                        (double)b.num_E, (double)b.num_addremove_attempts,
-                        (double)b.num_addremove_accepted};
-  for (int k = 0; k < 19; ++k) o[k] = v[k];
+  ((AnyGrand*)h)->visit([&](auto& mc) {
+    const NBins& b = mc.bins;
+    const double v[19] = {(double)mc.moves, (double)mc.accepted, mc.addremove_probability,
+                          (double)mc.sys.num_atoms(), mc.sys.E, (double)b.num_states,
+                          (double)b.t_last, mc.gamma_wl, (double)mc.lowest_hist,
+                          (double)mc.highest_hist, (double)mc.total_hist, b.max_S,
+                          (double)b.max_S_index, b.min, b.width, (double)b.max_N,
+                          (double)b.num_E, (double)b.num_addremove_attempts,
+                          (double)b.num_addremove_accepted};
+    for (int k = 0; k < 19; ++k) o[k] = v[k];
+    return 0;
+  });
 }
 // The bins in the reference's layout (index E bin * (max_N + 1) + N); returns their count.
 int64_t orc_grand_bins(void* h, double* lnw, uint64_t* hist, uint64_t* wl_hist, uint8_t* visited,
                        uint64_t* round_trips) {
-  auto* mc = (EnergyNumberMC<Lj>*)h;
-  const NBins& b = mc->bins;
-  const size_t n = b.lnw.size();
-  for (size_t i = 0; i < n; ++i) {
-    if (lnw) lnw[i] = b.lnw[i];
-    if (hist) hist[i] = b.histogram[i];
-    if (wl_hist) wl_hist[i] = mc->kind == 2 && i < mc->wl.histogram.size() ? mc->wl.histogram[i] : 0;
-    if (visited) visited[i] = b.visited[i];
-    if (round_trips) round_trips[i] = b.round_trips[i];
+  return ((AnyGrand*)h)->visit([&](auto& mc) {
+    const NBins& b = mc.bins;
+    const size_t n = b.lnw.size();
+    for (size_t i = 0; i < n; ++i) {
+      if (lnw) lnw[i] = b.lnw[i];
+      if (hist) hist[i] = b.histogram[i];
+      if (wl_hist) wl_hist[i] = mc.kind == 2 && i < mc.wl.histogram.size() ? mc.wl.histogram[i] : 0;
+      if (visited) visited[i] = b.visited[i];
+      if (round_trips) round_trips[i] = b.round_trips[i];
+    }
+    return (int64_t)n;
+  });
+}
+// Subcell lists of a WCA grand walker against a rebuild from its positions (as
+// multisets of (index, image offset)); returns the number of differing subcells.
+int64_t orc_grand_check_cells(void* hv) {
+  auto* h = (AnyGrand*)hv;
+  if (h->system != 2) return 0;
+  const Cell& c = h->wca->sys.cell;
+  Cell fresh = c;
+  fresh.update_caches();
+  int64_t bad = 0;
+  for (size_t k = 0; k < c.subcells.size(); ++k) {
+    auto key = [](const Neighbor& n) {
+      return ((uint64_t)n.index << 24) | ((uint64_t)(uint8_t)n.off[0] << 16) |
+             ((uint64_t)(uint8_t)n.off[1] << 8) | (uint64_t)(uint8_t)n.off[2];
+    };
+    std::vector<uint64_t> a, b;
+    for (const auto& n : c.subcells[k]) a.push_back(key(n));
+    for (const auto& n : fresh.subcells[k]) b.push_back(key(n));
+    std::sort(a.begin(), a.end());
+    std::sort(b.begin(), b.end());
+    if (a != b) ++bad;
   }
-  return (int64_t)n;
+  return bad;
 }
 // Translation attempts and acceptances per N (max_N + 1 entries).
 void orc_grand_translation(void* h, uint64_t* attempts, uint64_t* accepted) {
-  auto* mc = (EnergyNumberMC<Lj>*)h;
-  for (size_t n = 0; n <= mc->bins.max_N; ++n) {
-    attempts[n] = mc->bins.num_translation_attempts[n];
-    accepted[n] = mc->bins.num_translation_accepted[n];
-  }
+  ((AnyGrand*)h)->visit([&](auto& mc) {
+    for (size_t n = 0; n <= mc.bins.max_N; ++n) {
+      attempts[n] = mc.bins.num_translation_attempts[n];
+      accepted[n] = mc.bins.num_translation_accepted[n];
+    }
+    return 0;
+  });
 }
 void orc_grand_draws(uint64_t seed, uint32_t walker, uint64_t t, double* dbl3, uint32_t* u2,
                      float* g3, double* cand) {

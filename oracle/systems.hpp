@@ -242,10 +242,31 @@ struct Cell {
       subcells[index(scp)].push_back(nb);
     }
   }
-  void add_atom_at(const V3& r) {
+  void add_atom_at(const V3& r) {  // optcell.rs:126-130
     uint32_t idx = (uint32_t)pos.size();
     pos.push_back(r);
     add_to_subcells(idx, r);
+  }
+  void remove_atom(size_t which) {  // optcell.rs:177-193 (swap_remove, then rename)
+    const V3 r = pos[which];
+    pos[which] = pos.back();
+    pos.pop_back();
+    long sc[3];
+    get_subcell(r, sc);
+    for (int k = 0; k < 27; ++k) {
+      long q[3] = {sc[0] + NEIGHBORS[k][0], sc[1] + NEIGHBORS[k][1], sc[2] + NEIGHBORS[k][2]};
+      remove_if_index(subcells[index(q)], (uint32_t)which);
+    }
+    if (pos.size() != which) {
+      const uint32_t oldindex = (uint32_t)pos.size();
+      long s2[3];
+      get_subcell(pos[which], s2);
+      for (int k = 0; k < 27; ++k) {
+        long q[3] = {s2[0] + NEIGHBORS[k][0], s2[1] + NEIGHBORS[k][1], s2[2] + NEIGHBORS[k][2]};
+        for (Neighbor& nb : subcells[index(q)])  // rename_neighbor (optcell.rs:419-426)
+          if (nb.index == oldindex) { nb.index = (uint32_t)which; break; }
+      }
+    }
   }
   static void remove_if_index(std::vector<Neighbor>& v, uint32_t idx) {  // optcell.rs:407-418
     for (size_t i = 0; i < v.size(); ++i)
@@ -344,6 +365,7 @@ struct Wca {
   double last_abs = 0;
   Cell cell;
   bool have_change = false;
+  int ch_kind = 0;  // Change::Move / Add / Remove (wca.rs:34-55)
   size_t ch_which = 0;
   V3 ch_to{};
   double ch_e = 0, ch_dabse = 0;
@@ -411,11 +433,49 @@ struct Wca {
     });
     last_abs = gross;
     have_change = true;
+    ch_kind = 0;
     ch_which = which;
     ch_to = r;
     ch_e = e;
     ch_dabse = dabse;
     return e;
+  }
+  // GrandSystem (wca.rs:307-323): add_atom_at (wca.rs:105-116), remove_atom_number
+  // (wca.rs:151-163)
+  double plan_add_at(const V3& r) {
+    double dabse = 0.0, gross = 0.0;
+    const double rc2 = wca_r_cutoff() * wca_r_cutoff();
+    cell.for_each_candidate(r, SIZE_MAX, [&](const V3& r1) {
+      const double q = norm2(sub(r1, r));
+      dabse += wca_potential(q);
+      if (q < rc2) gross += lj_gross(q) + 1.0;
+      return true;
+    });
+    last_abs = gross;
+    have_change = true;
+    ch_kind = 1;
+    ch_to = r;
+    ch_e = E + dabse;
+    ch_dabse = dabse;
+    return ch_e;
+  }
+  double plan_remove(size_t which) {
+    const V3 r = cell.pos[which];
+    double dabse = 0.0, gross = 0.0;
+    const double rc2 = wca_r_cutoff() * wca_r_cutoff();
+    cell.for_each_candidate(r, which, [&](const V3& r1) {
+      const double q = norm2(sub(r1, r));
+      dabse += wca_potential(q);
+      if (q < rc2) gross += lj_gross(q) + 1.0;
+      return true;
+    });
+    last_abs = gross;
+    have_change = true;
+    ch_kind = 2;
+    ch_which = which;
+    ch_e = E - dabse;
+    ch_dabse = dabse;
+    return ch_e;
   }
   std::optional<double> plan_move(const Draws& d, double scale) {  // wca.rs:342-353
     if (cell.pos.empty()) return std::nullopt;
@@ -424,9 +484,11 @@ struct Wca {
                               f[2] + (double)d.g[2] * scale});
     return move_atom(d.which, to);
   }
-  void confirm() {  // wca.rs:276-301 (Move arm)
+  void confirm() {  // wca.rs:276-301
     if (!have_change) return;
-    cell.move_atom(ch_which, ch_to);
+    if (ch_kind == 0) cell.move_atom(ch_which, ch_to);
+    else if (ch_kind == 1) cell.add_atom_at(ch_to);
+    else cell.remove_atom(ch_which);
     set_energy(ch_e, ch_dabse);
     have_change = false;
   }

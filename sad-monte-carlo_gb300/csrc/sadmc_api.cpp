@@ -307,9 +307,15 @@ struct sadmc_grand {
   void* plane_mem = nullptr;
   GrandPlanes planes{};
   float* d_pos = nullptr;
+  // WCA fluid: FP64 positions, binary32 copies, subcell of each atom, bucket lists
+  double* d_pos64 = nullptr;
+  float* d_pos32 = nullptr;
+  int *d_cell_of = nullptr, *d_cnt = nullptr, *d_atoms = nullptr;
+  int nc[3] = {0, 0, 0}, cell_cap = 0, bucket = 32;
   TraceRec* d_trace = nullptr;
   uint64_t trace_cap = 0, trace_t0 = 0, moves_done = 0;
   cudaStream_t stream = nullptr;
+  bool wca() const { return cfg.system == SADMC_WCA; }
   GrandLaunch launch() const {
     GrandLaunch m{};
     m.cores = d_cores; m.B = planes; m.pos = d_pos; m.np = np; m.rows = rows; m.ncol = ncol;
@@ -324,6 +330,11 @@ struct sadmc_grand {
     m.trace = d_trace; m.trace_cap = trace_cap; m.trace_t0 = trace_t0;
     m.resum_interval = cfg.resum_interval > 0 ? cfg.resum_interval : 2048;
     m.drift_tol = cfg.drift_tol > 0 ? cfg.drift_tol : 1e-2;
+    m.system = wca() ? 2 : 1;
+    m.pos64 = d_pos64; m.pos32 = d_pos32; m.cell_of = d_cell_of; m.cell_count = d_cnt;
+    m.cell_atoms = d_atoms; m.cell_cap = cell_cap; m.bucket = bucket;
+    for (int a = 0; a < 3; ++a) { m.box[a] = cfg.box[a]; m.nc[a] = nc[a]; }
+    m.r_cut = std::pow(2.0, 1.0 / 6.0);
     return m;
   }
 };
@@ -1357,16 +1368,26 @@ int32_t sadmc_grand_create(const sadmc_grand_config* c, sadmc_grand** out) {
   if (c->n_walkers <= 0) return fail(SADMC_ERR_INVALID, "n_walkers must be positive");
   if (c->method != SADMC_SAMC && c->method != SADMC_WL)
     return fail(SADMC_ERR_INVALID, "the energy-number method supports SAMC and WL (energy_number.rs:18-27)");
-  if (c->max_N < 1 || c->max_N > 63)
-    return fail(SADMC_ERR_INVALID, "max_N (the cap on atoms) must be 1..63 on the GPU");
-  if (!(c->radius > 0)) return fail(SADMC_ERR_INVALID, "radius must be positive");
+  const bool wca = c->system == SADMC_WCA;
+  if (!wca && c->system != SADMC_LJ) return fail(SADMC_ERR_INVALID, "grand-canonical systems: SADMC_LJ or SADMC_WCA");
+  if (c->max_N < 1 || c->max_N > (wca ? 1024 : 63))
+    return fail(SADMC_ERR_INVALID, "max_N (the cap on atoms) must be 1..63 (LJ) or 1..1024 (WCA)");
+  if (!wca && !(c->radius > 0)) return fail(SADMC_ERR_INVALID, "radius must be positive");
+  int ncell[3] = {0, 0, 0};
+  if (wca)
+    for (int a = 0; a < 3; ++a) {
+      ncell[a] = (int)std::floor(c->box[a] / std::pow(2.0, 1.0 / 6.0));  // optcell.rs:64-66
+      if (ncell[a] < 3) return fail(SADMC_ERR_INVALID, "box: fewer than 3 subcells per axis");
+    }
   const double w = c->energy_bin > 0 ? c->energy_bin : 1.0;
   if (!(c->e_hi > 0.0 && c->e_lo < 0.0)) return fail(SADMC_ERR_INVALID, "need e_lo < 0 < e_hi (walkers start empty, E = 0)");
   auto* h = new sadmc_grand();
   h->cfg = *c;
   h->W = c->n_walkers;
-  h->np = c->max_N < 32 ? 32 : 64;
+  h->np = wca ? (c->max_N + 31) / 32 * 32 : (c->max_N < 32 ? 32 : 64);
   h->ncol = c->max_N + 1;
+  for (int a = 0; a < 3; ++a) h->nc[a] = ncell[a];
+  h->cell_cap = ncell[0] * ncell[1] * ncell[2];
   const int below = (int)std::ceil(-c->e_lo / w) + 2, above = (int)std::ceil(c->e_hi / w) + 2;
   h->rows = below + above;
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
@@ -1374,6 +1395,16 @@ int32_t sadmc_grand_create(const sadmc_grand_config* c, sadmc_grand** out) {
   if (e == cudaSuccess) e = cudaMalloc(&h->d_cores, sizeof(GrandCore) * W);
   if (e == cudaSuccess) e = cudaMalloc(&h->plane_mem, W * cells * 8 * 5 + W * h->ncol * 8 * 2);
   if (e == cudaSuccess) e = cudaMalloc(&h->d_pos, sizeof(float) * W * 6 * h->np);
+  if (e == cudaSuccess && wca) {
+    e = cudaMalloc(&h->d_pos64, sizeof(double) * W * 3 * h->np);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_pos32, sizeof(float) * W * 4 * h->np);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_cell_of, sizeof(int) * W * h->np);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_cnt, sizeof(int) * W * h->cell_cap);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_atoms, sizeof(int) * W * h->cell_cap * h->bucket);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_cnt, 0, sizeof(int) * W * h->cell_cap, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_pos64, 0, sizeof(double) * W * 3 * h->np, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_pos32, 0, sizeof(float) * W * 4 * h->np, h->stream);
+  }
   if (e != cudaSuccess) { sadmc_grand_destroy(h); return fail(SADMC_ERR_NOMEM, cudaGetErrorString(e)); }
   char* b = (char*)h->plane_mem;
   h->planes.lnw = (double*)b;
@@ -1417,6 +1448,11 @@ int32_t sadmc_grand_destroy(sadmc_grand* h) {
   cudaFree(h->d_cores);
   cudaFree(h->plane_mem);
   cudaFree(h->d_pos);
+  cudaFree(h->d_pos64);
+  cudaFree(h->d_pos32);
+  cudaFree(h->d_cell_of);
+  cudaFree(h->d_cnt);
+  cudaFree(h->d_atoms);
   cudaFree(h->d_trace);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1438,7 +1474,7 @@ int32_t sadmc_grand_run(sadmc_grand* h, uint64_t moves) {
   GrandLaunch m = h->launch();
   for (uint64_t left = moves; left > 0;) {
     m.n_moves = std::min<uint64_t>(left, 8192);
-    CUDA_TRY(launch_grand_move(m, h->stream));
+    CUDA_TRY(h->wca() ? launch_wca_grand_move(m, h->stream) : launch_grand_move(m, h->stream));
     left -= m.n_moves;
   }
   CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -1466,7 +1502,12 @@ int32_t sadmc_grand_read_state(sadmc_grand* h, int32_t walker, double* pos, int3
   GrandCore g;
   CUDA_TRY(cudaMemcpy(&g, h->d_cores + walker, sizeof(g), cudaMemcpyDeviceToHost));
   *n = g.N;
-  if (pos) {
+  if (pos && h->wca()) {
+    std::vector<double> p(3 * (size_t)h->np);
+    CUDA_TRY(cudaMemcpy(p.data(), h->d_pos64 + (size_t)walker * 3 * h->np, sizeof(double) * p.size(), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < g.N; ++j)
+      for (int a = 0; a < 3; ++a) pos[3 * j + a] = p[(size_t)a * h->np + j];
+  } else if (pos) {
     std::vector<float> p(6 * (size_t)h->np);
     CUDA_TRY(cudaMemcpy(p.data(), h->d_pos + (size_t)walker * 6 * h->np, sizeof(float) * p.size(), cudaMemcpyDeviceToHost));
     for (int j = 0; j < g.N; ++j)

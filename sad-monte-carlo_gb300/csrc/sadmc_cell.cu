@@ -21,6 +21,7 @@
 
 #include "sadmc_common.cuh"
 #include "sadmc_fh.cuh"
+#include "sadmc_grand_book.cuh"
 #include "sadmc_launch.h"
 #include "sadmc_rng.cuh"
 
@@ -156,6 +157,13 @@ struct CellOps {
           if (e2 < 1.0) { if (newq) overlap = true; else ++contacts; }
           else if (e2 < wsqr) ++contacts;
         }
+      } else if (d2 < 0.81f) {
+        // a close pair (V > 7): the binary32 copies lose relative precision in r^2 as r
+        // shrinks, so take the distance from the FP64 positions
+        const double bx = (cw.p[j] - (double)ox * cw.L[0]) - qx;
+        const double by = (cw.p[cw.np + j] - (double)oy * cw.L[1]) - qy;
+        const double bz = (cw.p[2 * cw.np + j] - (double)oz * cw.L[2]) - qz;
+        e32 += (float)wca_v64(bx * bx + by * by + bz * bz, wsqr);
       } else {
         e32 += wca_v32(d2, rc2_32);
       }
@@ -473,6 +481,186 @@ __global__ void cell_energy_kernel(const WalkerCore* cores, CellSys s, int n_wal
   }
 }
 
+// Grand-canonical WCA fluid with the energy-number method (src/mc/energy_number.rs,
+// wca.rs:307-323): translations (wca.rs:342-353), adds at a uniform point of the box
+// (add_atom_at, wca.rs:105-116; optcell.rs:126-130) and removals of a uniform atom
+// (remove_atom_number, wca.rs:151-163; optcell.rs:177-193: swap_remove, the last atom
+// takes the removed index).  One warp per walker over the subcell buckets.
+__global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
+  const int lane = threadIdx.x & 31;
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (w >= m.n_walkers) return;
+  const unsigned full = 0xffffffffu;
+  GrandBook bk;
+  bk.load(m, w, lane);
+  CellWalker cw;
+  cw.np = m.np;
+  cw.bucket = m.bucket;
+  cw.p = m.pos64 + (size_t)w * 3 * m.np;
+  cw.p32 = reinterpret_cast<float4*>(m.pos32) + (size_t)w * m.np;
+  cw.cell_of = m.cell_of + (size_t)w * m.np;
+  cw.cnt = m.cell_count + (size_t)w * m.cell_cap;
+  cw.atoms = m.cell_atoms + (size_t)w * m.cell_cap * m.bucket;
+  for (int a = 0; a < 3; ++a) {
+    cw.L[a] = m.box[a];
+    cw.L32[a] = (float)m.box[a];
+    cw.nc[a] = m.nc[a];
+  }
+  const double wsqr = m.r_cut * m.r_cut;
+  const float wsqr32 = (float)wsqr;
+  auto cell_xyz = [&](int c, int& x, int& y, int& z) {
+    x = c / (cw.nc[1] * cw.nc[2]);
+    y = (c / cw.nc[2]) % cw.nc[1];
+    z = c % cw.nc[2];
+  };
+  // binary32 energy of a query point against the candidates of its 27 subcells
+  auto near32 = [&](double qx, double qy, double qz, int c, int skip) -> float {
+    int cx, cy, cz;
+    cell_xyz(c, cx, cy, cz);
+    int cn = 0;
+    bool ov = false;
+    float e = 0.0f;
+    for (int k = lane; k < 27; k += 32)
+      CellOps<32, SYS_WCA>::scan(cw, k, cx, cy, cz, qx, qy, qz, (float)qx, (float)qy, (float)qz,
+                                 skip, wsqr, wsqr32, true, cn, ov, e, wsqr32);
+    return group_sum<32>(e, full);
+  };
+  const double sc = m.translation_scale;
+  Every resum;
+  resum.init(bk.c.moves, m.resum_interval > 0 ? (uint64_t)m.resum_interval : 0);
+  for (uint64_t it = 0; it < m.n_moves; ++it) {
+    bk.c.moves += 1;
+    const uint64_t t = bk.c.moves;
+    const GrandDraws d = draws_grand(m.seed, (uint32_t)w, t);
+    const double E1 = bk.c.E;
+    const int N1 = bk.c.N;
+    int kind_move = -1, which = 0, N2 = N1, new_c = 0;
+    double tx = 0, ty = 0, tz = 0;
+    float de = 0.0f;
+    const bool translation = bk.choose(d);
+    if (translation) {
+      if (N1 > 0) {  // plan_move: put_in_cell(from + g * scale)
+        which = (int)mulhi_range(d.pick, (uint32_t)N1);
+        const double fx = cw.p[which], fy = cw.p[cw.np + which], fz = cw.p[2 * cw.np + which];
+        bool bad = false;
+        tx = wrap_axis(fx + (double)d.g0 * sc, cw.L[0], &bad);
+        ty = wrap_axis(fy + (double)d.g1 * sc, cw.L[1], &bad);
+        tz = wrap_axis(fz + (double)d.g2 * sc, cw.L[2], &bad);
+        new_c = cw.cell_index(subcell_axis(tx, cw.L[0], cw.nc[0]), subcell_axis(ty, cw.L[1], cw.nc[1]),
+                              subcell_axis(tz, cw.L[2], cw.nc[2]));
+        const int old_c = cw.cell_of[which];
+        de = near32(tx, ty, tz, new_c, which) - near32(fx, fy, fz, old_c, which);
+        if (!bad && !(new_c != old_c && min(cw.cnt[new_c], cw.bucket) >= cw.bucket)) kind_move = 0;
+        else if (!bad) bk.c.status |= ST_CELL_OVERFLOW;
+      }
+    } else if (d.add_bit == 0) {
+      if (!(m.has_max_N && N1 == m.max_N) && N1 < cw.np) {
+        // a uniform point of the box (words of add candidate 0), then put_in_cell
+        const uint32_t k0 = (uint32_t)w, k1 = (uint32_t)m.seed, shi = (uint32_t)(m.seed >> 32);
+        const Philox4 D = philox4x32_10(Philox4{(uint32_t)t, (uint32_t)(t >> 32), 8u, shi}, k0, k1);
+        const Philox4 Q = philox4x32_10(Philox4{(uint32_t)t, (uint32_t)(t >> 32), 9u, shi}, k0, k1);
+        const double s53 = 1.0 / 9007199254740992.0;
+        bool bad = false;
+        tx = wrap_axis(cw.L[0] * ((double)u53_bits(D.x, D.y) * s53), cw.L[0], &bad);
+        ty = wrap_axis(cw.L[1] * ((double)u53_bits(D.z, D.w) * s53), cw.L[1], &bad);
+        tz = wrap_axis(cw.L[2] * ((double)u53_bits(Q.x, Q.y) * s53), cw.L[2], &bad);
+        new_c = cw.cell_index(subcell_axis(tx, cw.L[0], cw.nc[0]), subcell_axis(ty, cw.L[1], cw.nc[1]),
+                              subcell_axis(tz, cw.L[2], cw.nc[2]));
+        de = near32(tx, ty, tz, new_c, -1);
+        if (min(cw.cnt[new_c], cw.bucket) < cw.bucket) {
+          kind_move = 1;
+          N2 = N1 + 1;
+        } else {
+          bk.c.status |= ST_CELL_OVERFLOW;
+        }
+      }
+    } else if (N1 > 0) {
+      which = (int)mulhi_range(d.pick, (uint32_t)N1);
+      de = -near32(cw.p[which], cw.p[cw.np + which], cw.p[2 * cw.np + which], cw.cell_of[which], which);
+      kind_move = 2;
+      N2 = N1 - 1;
+    }
+    const bool possible = kind_move >= 0 && fabsf(de) <= 3.0e38f;
+    if (m.trace && lane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
+      TraceRec r;
+      r.e1 = E1;
+      r.e2 = possible ? E1 + (double)de : __longlong_as_double(0x7ff8000000000000ll);
+      m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = r;
+    }
+    if (possible && bk.decide(m, E1, N1, E1 + (double)de, N2, translation, d.u53)) {
+      // ConfirmSystem::confirm (wca.rs:276-301) on the buckets
+      if (kind_move == 0 || kind_move == 2) {
+        // take `which` out of its bucket (kept for a move within the same subcell)
+        const int oc = cw.cell_of[which];
+        if (kind_move == 2 || new_c != oc) {
+          int* lo = cw.atoms + (size_t)oc * cw.bucket;
+          const int mo = min(cw.cnt[oc], cw.bucket);
+          int pos = -1;
+          for (int k = lane; k < mo; k += 32)
+            if (lo[k] == which) pos = k;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const int x = __shfl_xor_sync(full, pos, o);
+            pos = x > pos ? x : pos;
+          }
+          __syncwarp(full);
+          if (lane == 0 && pos >= 0) {
+            lo[pos] = lo[mo - 1];
+            cw.cnt[oc] = mo - 1;
+          }
+          __syncwarp(full);
+        }
+      }
+      if (kind_move == 0 || kind_move == 1) {
+        const int a = kind_move == 0 ? which : N1;
+        const int oc = kind_move == 0 ? cw.cell_of[which] : -1;
+        if (lane == 0) {
+          if (kind_move == 1 || new_c != oc) {
+            const int cnt = cw.cnt[new_c];
+            cw.atoms[(size_t)new_c * cw.bucket + cnt] = a;
+            cw.cnt[new_c] = cnt + 1;
+          }
+          cw.cell_of[a] = new_c;
+          cw.p[a] = tx; cw.p[cw.np + a] = ty; cw.p[2 * cw.np + a] = tz;
+          cw.p32[a] = make_float4((float)tx, (float)ty, (float)tz, 0.0f);
+        }
+      } else if (which != N1 - 1) {
+        // swap_remove: atom N1 - 1 takes index `which` (rename_neighbor, optcell.rs:419)
+        const int last = N1 - 1, lc = cw.cell_of[last];
+        int* ll = cw.atoms + (size_t)lc * cw.bucket;
+        const int ml = min(cw.cnt[lc], cw.bucket);
+        int pos = -1;
+        for (int k = lane; k < ml; k += 32)
+          if (ll[k] == last) pos = k;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const int x = __shfl_xor_sync(full, pos, o);
+          pos = x > pos ? x : pos;
+        }
+        __syncwarp(full);
+        if (lane == 0) {
+          if (pos >= 0) ll[pos] = which;
+          cw.cell_of[which] = lc;
+          cw.p[which] = cw.p[last];
+          cw.p[cw.np + which] = cw.p[cw.np + last];
+          cw.p[2 * cw.np + which] = cw.p[2 * cw.np + last];
+          cw.p32[which] = cw.p32[last];
+        }
+      }
+      __syncwarp(full);
+    }
+    bk.finish(m, t, E1, N1);
+    if (resum.tick()) {
+      double e = 0.0;
+      const int n = bk.c.N;
+      for (int i = lane; i < n; i += 32)
+        e += cw.pair_sum64(i, [&](double r2) { return wca_v64(r2, wsqr); });
+      bk.resummed(m, group_sum<32>(e, full) * 0.5);
+    }
+  }
+  bk.store(m.cores, w);
+}
+
 }  // namespace dev
 
 #define SADMC_CELL_CASE(L, K)                                                           \
@@ -506,3 +694,11 @@ cudaError_t launch_cell_energy(const WalkerCore* cores, const CellSys& s, int n_
 }
 
 }  // namespace sadmc
+
+namespace sadmc {
+cudaError_t launch_wca_grand_move(const GrandLaunch& m, cudaStream_t st) {
+  dev::wca_grand_kernel<<<(m.n_walkers + 3) / 4, 128, 0, st>>>(m);
+  return cudaGetLastError();
+}
+}  // namespace sadmc
+

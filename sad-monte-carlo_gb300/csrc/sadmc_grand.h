@@ -55,9 +55,22 @@ struct GrandLaunch {
   uint64_t trace_cap, trace_t0;
   int resum_interval;
   double drift_tol;
+  // WCA fluid (system 2): FP64 positions [walker][3][np], binary32 copies [walker][np],
+  // subcell of each atom, bucket counts [walker][cells], buckets [walker][cells][bucket]
+  int system;            // 1 LJ cluster, 2 WCA fluid
+  double* pos64;
+  float* pos32;
+  int* cell_of;
+  int* cell_count;
+  int* cell_atoms;
+  int cell_cap, bucket;
+  double box[3];
+  int nc[3];
+  double r_cut;
 };
 
 cudaError_t launch_grand_move(const GrandLaunch& m, cudaStream_t st);
+cudaError_t launch_wca_grand_move(const GrandLaunch& m, cudaStream_t st);
 cudaError_t launch_grand_init(const GrandLaunch& m, cudaStream_t st);
 
 }  // namespace sadmc

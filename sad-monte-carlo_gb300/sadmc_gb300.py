@@ -446,7 +446,8 @@ class GrandConfig(ctypes.Structure):
                 ("addremove_probability", ctypes.c_double),
                 ("e_lo", ctypes.c_double), ("e_hi", ctypes.c_double),
                 ("seed", ctypes.c_uint64), ("resum_interval", ctypes.c_int32),
-                ("pad", ctypes.c_int32), ("drift_tol", ctypes.c_double)]
+                ("system", ctypes.c_int32), ("drift_tol", ctypes.c_double),
+                ("box", ctypes.c_double * 3)]
 
 
 GRAND_SCALARS = ["moves", "accepted", "addremove_probability", "N", "energy", "num_states",
@@ -455,11 +456,15 @@ GRAND_SCALARS = ["moves", "accepted", "addremove_probability", "N", "energy", "n
                  "addremove_accepted", "drift", "status"]
 
 
-def make_grand_config(n_walkers, max_N, radius, *, method=SAMC, t0=1e4, energy_bin=1.0,
-                      min_allowed=None, max_allowed=None, target_rate=None,
+def make_grand_config(n_walkers, max_N, radius=0.0, *, box=None, method=SAMC, t0=1e4,
+                      energy_bin=1.0, min_allowed=None, max_allowed=None, target_rate=None,
                       translation_scale=0.05, addremove_probability=0.05, e_lo=-200.0,
                       e_hi=50.0, seed=0, resum_interval=0, drift_tol=0.0):
+    """Energy-number walkers: the LJ cluster of `radius`, or (box given) the WCA fluid."""
     c = GrandConfig()
+    c.system = WCA if box is not None else LJ
+    if box is not None:
+        c.box[0], c.box[1], c.box[2] = box
     c.method, c.n_walkers, c.max_N = method, n_walkers, max_N
     c.acceptance_rate_mode, c.target_rate = int(target_rate is not None), target_rate or 0.5
     c.t0, c.energy_bin, c.radius = t0, energy_bin, radius
@@ -505,7 +510,7 @@ class GrandBatch:
 
     def state(self, w):
         n = ctypes.c_int32(0)
-        out = np.zeros((64, 3))
+        out = np.zeros((max(64, int(self.cfg.max_N)), 3))
         _check(lib().sadmc_grand_read_state(self.h, w, _p(out), ctypes.byref(n)))
         return out[:n.value]
 

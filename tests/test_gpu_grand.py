@@ -42,3 +42,34 @@ def test_grand_trace_replay(gpu, oracle, method, target):
         np.testing.assert_array_equal(gc, oc)
         np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
         assert gs["energy"] == pytest.approx(ow.compute_energy(), abs=1e-3)
+
+
+@pytest.mark.parametrize("method", ["samc", "wl"])
+def test_grand_wca_trace_replay(gpu, oracle, method):
+    """The WCA fluid's grand moves (wca.rs:307-323): adds at a uniform point of the box,
+    removals by swap_remove out of the subcell lists (optcell.rs:177-193)."""
+    W, moves, max_N, L, seed = 6, 20000, 40, 4.5, 5
+    m = gpu.SAMC if method == "samc" else gpu.WL
+    common = dict(t0=1000.0, energy_bin=0.5, max_allowed=20.0, translation_scale=0.1,
+                  addremove_probability=0.2, seed=seed)
+    b = gpu.GrandBatch(gpu.make_grand_config(W, max_N, box=(L, L, L), method=m, e_lo=-1.0,
+                                             e_hi=25.0, **common))
+    b.set_trace(moves)
+    b.run(moves)
+    for w in range(W):
+        e1, e2 = b.trace(w, moves)
+        ow = oracle.GrandWalker(oracle.make_grand_config(box=(L, L, L), method=m, max_N=max_N,
+                                                         walker=w, **common))
+        disc, mismatch = ow.run_override(e1, e2)
+        assert mismatch == 0 and disc < 2e-5, (w, mismatch, disc, ow.worst())
+        gb, ob = b.bins(w), ow.bins()
+        for k in ("lnw", "hist", "visited", "round_trips"):
+            np.testing.assert_array_equal(gb[k], ob[k], err_msg=f"walker {w} {k}")
+        if method == "wl":
+            np.testing.assert_array_equal(gb["wl_hist"], ob["wl_hist"], err_msg=f"walker {w}")
+        gs, os_ = b.scalars(w), ow.scalars()
+        for k in SAME:
+            assert gs[k] == os_[k], (w, k, gs[k], os_[k])
+        assert gs["status"] == 0
+        np.testing.assert_array_equal(b.state(w), ow.state())
+        assert gs["energy"] == pytest.approx(ow.compute_energy(), abs=1e-3)

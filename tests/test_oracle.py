@@ -132,6 +132,27 @@ def test_grand_energy_number_invariants(oracle, method):
     assert (b["lnw"][b["hist"] == 0] == 0).all()
 
 
+@pytest.mark.parametrize("method", ["samc", "wl"])
+def test_grand_wca_invariants(oracle, method):
+    """The WCA fluid's grand moves (wca.rs:307-323): adds, swap_remove with the subcell
+    renaming of optcell.rs:177-193; the lists always equal a rebuild from the positions
+    and the incremental energy equals compute_energy."""
+    m = oracle.M_SAMC if method == "samc" else oracle.M_WL
+    L = 4.5
+    w = oracle.GrandWalker(oracle.make_grand_config(box=(L, L, L), method=m, t0=500.0,
+                                                    energy_bin=0.5, max_N=40, max_allowed=20.0,
+                                                    translation_scale=0.1,
+                                                    addremove_probability=0.3, seed=6))
+    for _ in range(10):
+        w.run(5000)
+        assert w.check_cells() == 0
+    s = w.scalars()
+    assert 0 <= s["N"] <= 40 and s["addremove_accepted"] > 100
+    assert s["energy"] == pytest.approx(w.compute_energy(), rel=1e-9, abs=1e-9)
+    x = w.state()
+    assert len(x) == s["N"] and ((x >= 0) & (x < L)).all()
+
+
 def test_max_balls_within(oracle):
     # optsquare.rs:290-322 counts lattice points of its own construction
     assert oracle.max_balls_within(1.3) == 6
