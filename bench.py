@@ -23,6 +23,7 @@ import re
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -90,7 +91,7 @@ def other_configs(G, seed=11):
                  "lanes_per_walker": b.lanes_per_walker()}
     b.close()
     # C3: WCA, N in {64,128,256,512}, density in [0.6, 0.9], 2048 walkers, SAMC t0 = 1e4,
-    # 500 bins over [0, 500) (the range this build fixes; the workload states none)
+    # 500 bins over [0, 500) (a range fixed here; the workload states none)
     W3 = 2048
     ns = rng.choice([64, 128, 256, 512], W3)
     rhos = rng.uniform(0.6, 0.9, W3)
@@ -231,8 +232,7 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out" if os.path.isdir(os.path.join(REPO, "gpurun_out")) else ".",
-                                 ".bench_clocks.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"sadmc_bench_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
@@ -463,7 +463,7 @@ def run_gpu(args):
                          "traffic": traffic,
                          "note": "30(N-1) FLOP/move algorithmic; peak = 152 SM x 128 FFMA x 2 x "
                                  "max SM clock (FP32 issue, not in MEASURED_PEAKS.json); the "
-                                 "kernel is FP64/latency bound, see DESIGN.md"},
+                                 "kernel is bound by the FP64 pipe and the latency of the per-move bookkeeping"},
             "launch_ms": launch_ms,
             "clocks": clk,
             "gpu_launches": args.steps * launches_per_step,

@@ -1,8 +1,8 @@
 """ORACLE / TEST INFRASTRUCTURE ONLY: FP64 numpy statement of the learned surrogate.
 
 The reference has no learned component; this module defines, in plain FP64 numpy, the
-radial-descriptor MLP that the CUDA surrogate kernels implement, and is the checker of
-their forward pass, gradients and optimizer step:
+radial-descriptor MLP that the CUDA surrogate kernels implement; the tests compare the
+kernels' forward pass, gradients and optimizer step with it:
 
   descriptor  G[i,k] = sum_{j != i} exp(-(r_ij - c_k)^2 / (2 w^2)),  32 centres c_k evenly
               spaced over [0.8, 3.0] sigma, width w = 0.1 sigma

@@ -1,5 +1,5 @@
 // ORACLE / TEST INFRASTRUCTURE ONLY.  FP64 C++ restatement of the reference's systems,
-// used as the correctness judge of the CUDA kernels and as the timed CPU baseline.
+// the FP64 statement the CUDA kernels are compared with and as the timed CPU baseline.
 // Parity is pinned by the reference's own invariant tests (energy == compute_energy
 // after every move, minimum-image agreement), re-run on this restatement in
 // tests/test_oracle.py; the reference ships no golden numeric vectors.

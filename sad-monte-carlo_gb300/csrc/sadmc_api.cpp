@@ -756,7 +756,7 @@ int32_t sadmc_plan_move_injected(sadmc_handle* h, int32_t walker, const sadmc_pr
                                  double* e_out, int32_t* possible) {
   if (!h || !p || !e_out || !possible || walker < 0 || walker >= h->W)
     return fail(SADMC_ERR_INVALID, "bad argument");
-  if (h->cfg.system != SADMC_LJ) return fail(SADMC_ERR_INVALID, "injected plans: LJ only in this build");
+  if (h->cfg.system != SADMC_LJ) return fail(SADMC_ERR_INVALID, "injected plans support the LJ cluster");
   if (p->which < 0 || p->which >= h->geom[walker].n) return fail(SADMC_ERR_INVALID, "bad atom index");
   if (!h->uploaded) return fail(SADMC_ERR_STATE, "upload a state first");
   int32_t r = h->prep_cores();
