@@ -134,7 +134,7 @@ struct Fh {
   int win_lo, win_hi;  // SAD window as bin indices
   // gamma batch (see gamma())
   double gb_val[4];
-  uint64_t gb_base;
+  uint32_t gb_off;  // moves since the batch was taken
   bool gb_valid;
   // per-move scratch
   double e1;
@@ -280,12 +280,12 @@ struct Fh {
       default: return 0.0;
     }
   }
-  // gamma(gb_base + glane + LPW*q) sits in gb_val[q]; four independent divide chains per
+  // gamma(batch start + glane + LPW*q) sits in gb_val[q]; four independent divide chains per
   // lane hide the FP64 divide latency and cover 4*LPW moves per evaluation.
   __device__ double gamma() {
     if (kind() != M_SAD && kind() != M_SAMC) return gamma_at(c.moves);
-    if (!gb_valid || c.moves < gb_base || c.moves - gb_base >= (uint64_t)(4 * LPW)) {
-      gb_base = c.moves;
+    if (!gb_valid || gb_off >= (uint32_t)(4 * LPW)) {
+      gb_off = 0;
       if (kind() == M_SAD) {
         if (c.tF != inv_tF_of) { inv_tF = 1.0 / (double)c.tF; inv_tF_of = c.tF; }
         if (c.num_states != inv_ns_of) { inv_ns = 1.0 / (double)c.num_states; inv_ns_of = c.num_states; }
@@ -294,7 +294,7 @@ struct Fh {
       for (int q = 0; q < 4; ++q) gb_val[q] = gamma_at(c.moves + (uint64_t)(glane + LPW * q));
       gb_valid = true;
     }
-    const int off = (int)(c.moves - gb_base);
+    const int off = (int)gb_off++;  // gamma() runs once per move
     const int q = off / LPW;
     double v = q == 0 ? gb_val[0] : q == 1 ? gb_val[1] : q == 2 ? gb_val[2] : gb_val[3];
     if (LPW == 1) return v;
@@ -697,17 +697,18 @@ struct Fh {
 
 // sqrt(1/t) and 1 - sqrt(1/t) (energy.rs:913) for 32 consecutive t, one per lane.
 struct RecentScale {
-  uint64_t base;
+  uint32_t off;  // calls since the batch was taken (32: take the next batch)
   double rs, omrs;
-  __device__ void init() { base = ~0ull; }
+  __device__ void init() { off = 32; }
+  // called once per move with consecutive t
   __device__ void get(uint64_t t, int lane, double& r, double& om) {
-    if (base == ~0ull || t < base || t - base >= 32) {
-      base = t;
+    if (off >= 32) {
+      off = 0;
       double v = sqrt(1.0 / (double)(t + (uint64_t)lane));
       rs = v;
       omrs = 1. - v;
     }
-    int src = (int)(t - base);
+    const int src = (int)off++;
     r = __shfl_sync(0xffffffffu, rs, src);
     om = __shfl_sync(0xffffffffu, omrs, src);
   }

@@ -178,18 +178,19 @@ __device__ __forceinline__ void add_candidate(uint64_t seed, uint32_t walker, ui
 // draws with six group shuffles, so Philox and Box-Muller run once per LPW moves.
 template <int LPW, bool ISING>
 struct DrawCache {
-  uint64_t base;
+  uint32_t off;  // calls since the batch was drawn (LPW: draw the next batch)
   Draws mine;
-  __device__ void init() { base = ~0ull; }
+  __device__ void init() { off = LPW; }
+  // called once per move with consecutive t
   __device__ Draws get(uint64_t seed, uint32_t walker, uint64_t t, uint32_t n, unsigned gmask,
                        int glane) {
-    if (base == ~0ull || t < base || t - base >= (uint64_t)LPW) {
-      base = t;
+    if (off >= (uint32_t)LPW) {
+      off = 0;
       mine = ISING ? draws_ising(seed, walker, t + (uint64_t)glane, n)
                    : draws_continuous(seed, walker, t + (uint64_t)glane, n, 0u);
     }
+    const int src = (int)off++;
     if (LPW == 1) return mine;
-    const int src = (int)(t - base);
     Draws d;
     d.which = __shfl_sync(gmask, mine.which, src, LPW);
     d.j = ISING ? __shfl_sync(gmask, mine.j, src, LPW) : 0u;
