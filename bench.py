@@ -59,42 +59,59 @@ def lj_configs(n_walkers, seed):
 
 
 def _time_run(b, moves, warm):
+    """Seconds for `moves` moves per walker after `warm` warm-up moves: CUDA events on the
+    stream the kernels are launched on (a batch's run_async takes the stream; a grand batch
+    runs on its own stream and returns when done, so its events bracket the whole call)."""
+    import ctypes
     import torch
     b.run(warm)
     torch.cuda.synchronize()
+    st = torch.cuda.Stream()  # a stream of its own: a null handle means the library's stream
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    b.run(moves)
-    e1.record()
+    torch.cuda.nvtx.range_push("timed")
+    e0.record(st)
+    if hasattr(b, "run_async"):
+        b.run_async(moves, ctypes.c_void_p(st.cuda_stream))
+    else:
+        b.run(moves)
+    e1.record(st)
+    torch.cuda.nvtx.range_pop()
     e1.synchronize()
     return e0.elapsed_time(e1) * 1e-3
 
 
-def other_configs(G, seed=11):
-    """Device-resident moves/s of the other workloads (synthetic seeded inputs with their
-    shapes): C1 one Ising 32x32 walker, C3 an uneven WCA batch, C5 a hard-core square-well
-    batch.  Each is a short run after a warm-up, timed with CUDA events."""
-    out = {}
+def _lanes(b, lpw, tune_moves):
+    """The shape: fixed by --lpw, else autotuned on a snapshot of the batch."""
+    if not lpw:
+        b.autotune(tune_moves)
+    return b.lanes_per_walker()
+
+
+def case_c1(G, seed=11, moves=1_000_000, lpw=0, **_):
+    """C1: plain SAD, Ising 32x32, one walker, bins of 4 over [-2N, 2N]."""
     rng = np.random.default_rng(seed)
-    # C1: plain SAD, Ising 32x32, one walker, bins of 4 over [-2N, 2N]
     L = 32
     b = G.Batch(G.make_config(G.ISING, 1, L, method=G.SAD, min_T=0.2, e_lo=-2.0 * L * L - 8,
-                              e_hi=2.0 * L * L + 8, seed=seed),
+                              e_hi=2.0 * L * L + 8, seed=seed, lanes_per_walker=lpw),
                 [(L, 0.0, (0, 0, 0))])
     b.upload([np.where(rng.random(L * L) < 0.5, -1.0, 1.0)])
     b.initialize()
-    b.autotune(20000)
-    mv = 1_000_000
-    sec = _time_run(b, mv, 100_000)
-    out["C1"] = {"workload": "Ising 32x32, plain SAD (min_T 0.2), 1 walker", "moves": mv,
-                 "moves_per_s": mv / sec, "ns_per_move": 1e9 * sec / mv,
-                 "lanes_per_walker": b.lanes_per_walker()}
+    lanes = _lanes(b, lpw, 20000)
+    sec = _time_run(b, moves, 100_000)
     b.close()
-    # C3: WCA, N in {64,128,256,512}, density in [0.6, 0.9], 2048 walkers, SAMC t0 = 1e4,
-    # 500 bins over [0, 500) (a range fixed here; the workload states none)
-    W3 = 2048
-    ns = rng.choice([64, 128, 256, 512], W3)
-    rhos = rng.uniform(0.6, 0.9, W3)
+    return {"workload": "Ising 32x32, plain SAD (min_T 0.2), 1 walker", "moves": moves,
+            "moves_per_s": moves / sec, "ns_per_move": 1e9 * sec / moves,
+            "lanes_per_walker": lanes}
+
+
+def case_c3(G, seed=11, walkers=2048, moves=2048, lpw=0):
+    """C3: WCA, N in {64,128,256,512}, density in [0.6, 0.9], SAMC t0 = 1e4, 500 bins over
+    [0, 500) (a range fixed here; the workload states none); simple-cubic starts with a
+    jitter, brought below 500 by the descent of initialize()."""
+    rng = np.random.default_rng(seed)
+    rng.random(32 * 32)  # the C1 spins come first from this seed
+    ns = rng.choice([64, 128, 256, 512], walkers)
+    rhos = rng.uniform(0.6, 0.9, walkers)
     geo, states = [], []
     for n, rho in zip(ns, rhos):
         Lb = (n / rho) ** (1 / 3)
@@ -104,65 +121,78 @@ def other_configs(G, seed=11):
         pos = np.mod((g + 0.5 + rng.uniform(-0.05, 0.05, g.shape)) * (Lb / m), Lb)
         geo.append((int(n), 0.0, (Lb, Lb, Lb)))
         states.append(pos)
-    b = G.Batch(G.make_config(G.WCA, W3, int(ns.max()), method=G.SAMC, t0=1e4, energy_bin=1.0,
-                              e_lo=-1.0, e_hi=501.0, max_allowed=500.0, translation_scale=0.1,
-                              seed=seed, resum_interval=4096), geo)
+    b = G.Batch(G.make_config(G.WCA, walkers, int(ns.max()), method=G.SAMC, t0=1e4,
+                              energy_bin=1.0, e_lo=-1.0, e_hi=501.0, max_allowed=500.0,
+                              translation_scale=0.1, seed=seed, resum_interval=4096,
+                              lanes_per_walker=lpw), geo)
     b.upload(states)
     b.initialize()
-    b.autotune(256)
-    mv = 2048
-    sec = _time_run(b, mv, 512)
-    out["C3"] = {"workload": "WCA, N in {64,128,256,512}, density U[0.6,0.9], 2048 walkers, "
-                             "SAMC t0=1e4, 500 bins over [0,500)",
-                 "moves": W3 * mv, "moves_per_s": W3 * mv / sec,
-                 "lanes_per_walker": b.lanes_per_walker()}
+    lanes = _lanes(b, lpw, 256)
+    sec = _time_run(b, moves, 512)
     b.close()
-    # C5: hard-core square well (lambda 1.3), N = 1024, packing fraction U[0.30, 0.50],
-    # jittered FCC, Wang-Landau over contact-count bins of width 1, 1024 walkers
-    W5, n5 = 1024, 1024
+    return {"workload": f"WCA, N in {{64,128,256,512}}, density U[0.6,0.9], {walkers} walkers, "
+                        "SAMC t0=1e4, 500 bins over [0,500)",
+            "moves": walkers * moves, "moves_per_s": walkers * moves / sec,
+            "lanes_per_walker": lanes}
+
+
+def case_c5(G, seed=11, walkers=1024, moves=2048, lpw=0):
+    """C5: hard-core square well (lambda 1.3), N = 1024, packing fraction U[0.30, 0.50],
+    jittered FCC, Wang-Landau over contact-count bins of width 1."""
+    rng = np.random.default_rng(seed + 1)
+    n5 = 1024
     m = int(np.ceil((n5 / 4) ** (1 / 3)))
     base = np.array([(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)])
     sites = (np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)[:, None, :]
              + base[None]).reshape(-1, 3)
     geo, states = [], []
-    for eta in rng.uniform(0.30, 0.50, W5):
+    for eta in rng.uniform(0.30, 0.50, walkers):
         Lb = (n5 * np.pi / (6 * eta)) ** (1 / 3)
         pick = sites[rng.permutation(len(sites))[:n5]]
         pos = np.mod((pick + rng.uniform(-0.004, 0.004, pick.shape)) * (Lb / m), Lb)
         geo.append((n5, 0.0, (Lb, Lb, Lb)))
         states.append(pos)
-    b = G.Batch(G.make_config(G.SW, W5, n5, method=G.WL, e_lo=-6.0 * n5 - 2, e_hi=2.0,
-                              well_width=1.3, translation_scale=0.05, seed=seed), geo)
+    b = G.Batch(G.make_config(G.SW, walkers, n5, method=G.WL, e_lo=-6.0 * n5 - 2, e_hi=2.0,
+                              well_width=1.3, translation_scale=0.05, seed=seed,
+                              lanes_per_walker=lpw), geo)
     b.upload(states)
     b.initialize()
-    b.autotune(256)
-    mv = 2048
-    sec = _time_run(b, mv, 512)
-    out["C5"] = {"workload": "hard-core square well lambda=1.3, N=1024, packing U[0.30,0.50], "
-                             "jittered FCC, WL on contact bins, 1024 walkers",
-                 "moves": W5 * mv, "moves_per_s": W5 * mv / sec,
-                 "lanes_per_walker": b.lanes_per_walker()}
+    lanes = _lanes(b, lpw, 256)
+    sec = _time_run(b, moves, 512)
     b.close()
-    # grand-canonical LJ cluster, energy-number SAMC (src/mc/energy_number.rs), walkers
-    # start empty and grow to at most 31 atoms in a sphere of radius 2.5
-    import torch
-    Wg = 4096
-    gb = G.GrandBatch(G.make_grand_config(Wg, 31, 2.5, method=G.SAMC, t0=1e4, energy_bin=0.5,
-                                          max_allowed=10.0, translation_scale=0.1,
-                                          addremove_probability=0.1, e_lo=-150.0, e_hi=12.0,
-                                          seed=seed))
-    gb.run(4096)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    mv = 4096
-    gb.run(mv)
-    sec = time.perf_counter() - t0
-    out["grand"] = {"workload": "grand-canonical LJ cluster (R=2.5, N <= 31), energy-number SAMC "
-                                "t0=1e4, 4096 walkers, one warp per walker",
-                    "moves": Wg * mv, "moves_per_s": Wg * mv / sec,
-                    "mean_N": float(np.mean([gb.scalars(w)["N"] for w in range(0, Wg, 256)]))}
+    return {"workload": f"hard-core square well lambda=1.3, N=1024, packing U[0.30,0.50], "
+                        f"jittered FCC, WL on contact bins, {walkers} walkers",
+            "moves": walkers * moves, "moves_per_s": walkers * moves / sec,
+            "lanes_per_walker": lanes}
+
+
+def case_grand(G, seed=11, walkers=4096, moves=4096, lpw=0):
+    """Grand-canonical LJ cluster, energy-number SAMC (src/mc/energy_number.rs): walkers
+    start empty and grow to at most 31 atoms in a sphere of radius 2.5."""
+    gb = G.GrandBatch(G.make_grand_config(walkers, 31, 2.5, method=G.SAMC, t0=1e4,
+                                          energy_bin=0.5, max_allowed=10.0,
+                                          translation_scale=0.1, addremove_probability=0.1,
+                                          e_lo=-150.0, e_hi=12.0, seed=seed,
+                                          lanes_per_walker=lpw))
+    sec = _time_run(gb, moves, 4096)
+    out = {"workload": f"grand-canonical LJ cluster (R=2.5, N <= 31), energy-number SAMC "
+                       f"t0=1e4, {walkers} walkers",
+           "moves": walkers * moves, "moves_per_s": walkers * moves / sec,
+           "mean_N": float(np.mean([gb.scalars(w)["N"] for w in range(0, walkers, 256)])),
+           "lanes_per_walker": lpw or 8}
     gb.close()
     return out
+
+
+CASES = {"C1": case_c1, "C3": case_c3, "C5": case_c5, "grand": case_grand}
+
+
+def other_configs(G, seed=11):
+    """Device-resident moves/s of the other workloads (synthetic seeded inputs with their
+    shapes): C1 one Ising 32x32 walker, C3 an uneven WCA batch, C5 a hard-core square-well
+    batch, and the grand-canonical LJ cluster.  Each is a short run after a warm-up, timed
+    with CUDA events."""
+    return {k: f(G, seed) for k, f in CASES.items()}
 
 
 def da_compare(G, rank=0, walkers=8192, moves=2048):
@@ -477,6 +507,22 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_case(args):
+    import torch
+    import build as B
+    import sadmc_gb300 as G
+    torch.cuda.set_device(0)
+    B.build()
+    G.lib()
+    kw = {"lpw": args.lpw}
+    if args.walkers:
+        kw["walkers"] = args.walkers
+    if args.moves:
+        kw["moves"] = args.moves
+    out = CASES[args.only](G, **kw)
+    print(json.dumps({"case": args.only, **out}))
+
+
 def main():
     global WALKERS, MOVES_PER_STEP
     ap = argparse.ArgumentParser()
@@ -486,14 +532,21 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--lpw", type=int, default=0, help="lanes per walker (0: library default)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--walkers", type=int, default=WALKERS,
+    ap.add_argument("--walkers", type=int, default=None,
                     help="walkers (profiling a smaller case; the bench line uses 4096)")
-    ap.add_argument("--moves", type=int, default=MOVES_PER_STEP, help="moves per walker per step")
+    ap.add_argument("--moves", type=int, default=None, help="moves per walker per step")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-da", action="store_true", help="skip the delayed-acceptance comparison")
     ap.add_argument("--no-other", action="store_true", help="skip the C1/C3/C5 measurements")
+    ap.add_argument("--only", choices=sorted(CASES),
+                    help="time one other workload alone (with --walkers, --moves, --lpw) and "
+                         "print its line; for profiling a small case")
     args = ap.parse_args()
-    WALKERS, MOVES_PER_STEP = args.walkers, args.moves
+    if args.only:
+        run_case(args)
+        return
+    WALKERS = args.walkers or WALKERS
+    MOVES_PER_STEP = args.moves or MOVES_PER_STEP
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -302,7 +302,7 @@ std::vector<int> lpw_candidates(const sadmc_handle* h) {
 
 struct sadmc_grand {
   sadmc_grand_config cfg{};
-  int W = 0, np = 0, rows = 0, ncol = 0;
+  int W = 0, np = 0, rows = 0, ncol = 0, lanes = 8;
   GrandCore* d_cores = nullptr;
   void* plane_mem = nullptr;
   GrandPlanes planes{};
@@ -319,7 +319,7 @@ struct sadmc_grand {
   GrandLaunch launch() const {
     GrandLaunch m{};
     m.cores = d_cores; m.B = planes; m.pos = d_pos; m.np = np; m.rows = rows; m.ncol = ncol;
-    m.n_walkers = W; m.seed = cfg.seed;
+    m.n_walkers = W; m.seed = cfg.seed; m.lanes = lanes;
     m.width = cfg.energy_bin > 0 ? cfg.energy_bin : 1.0; m.inv_width = 1.0 / m.width;
     m.radius = cfg.radius; m.radius2 = cfg.radius * cfg.radius; m.t0 = cfg.t0;
     m.target_rate = cfg.target_rate;
@@ -1381,10 +1381,16 @@ int32_t sadmc_grand_create(const sadmc_grand_config* c, sadmc_grand** out) {
     }
   const double w = c->energy_bin > 0 ? c->energy_bin : 1.0;
   if (!(c->e_hi > 0.0 && c->e_lo < 0.0)) return fail(SADMC_ERR_INVALID, "need e_lo < 0 < e_hi (walkers start empty, E = 0)");
+  if (!wca && c->lanes_per_walker != 0) {
+    const int l = c->lanes_per_walker, np = c->max_N < 32 ? 32 : 64;
+    if (!(l == 4 || l == 8 || l == 16 || l == 32) || np / l > 8)
+      return fail(SADMC_ERR_INVALID, "lanes_per_walker: 32, 16, 8 or 4 (at least 8 when max_N >= 32)");
+  }
   auto* h = new sadmc_grand();
   h->cfg = *c;
   h->W = c->n_walkers;
   h->np = wca ? (c->max_N + 31) / 32 * 32 : (c->max_N < 32 ? 32 : 64);
+  h->lanes = c->lanes_per_walker ? c->lanes_per_walker : 8;
   h->ncol = c->max_N + 1;
   for (int a = 0; a < 3; ++a) h->nc[a] = ncell[a];
   h->cell_cap = ncell[0] * ncell[1] * ncell[2];

@@ -3,9 +3,10 @@
 // of src/system/lj.rs:291-319 (add at a uniform point of the sphere, remove a uniform
 // atom by swap_remove) and translations (lj.rs:86-105, 365-374).
 //
-// One warp per walker: atom j in lane j % 32, register slot j / 32, double-single
-// positions; pair energies in binary32 over double-single differences with a warp
-// reduction, every decision on the FP64 energy E + de as the reference takes it.  The
+// LPW lanes per walker (32 / LPW walkers per warp): atom j in lane j % LPW of the
+// walker's group, register slot j / LPW, double-single positions; pair energies in
+// binary32 over double-single differences with a group reduction, every decision on the
+// FP64 energy E + de as the reference takes it.  The
 // (E, N) bins keep the reference's layout parameters (min, num_E, max_N) and its index
 // arithmetic, including the quirks that affect results (max_S_index is not remapped
 // when the layout grows; Wang-Landau's histogram is a second set of bins).
@@ -21,17 +22,21 @@
 namespace sadmc {
 namespace dev {
 
-template <int APL>
+template <int LPW, int APL>
 __global__ void __launch_bounds__(128) lj_grand_kernel(GrandLaunch m) {
+  constexpr int WPW = 32 / LPW;
   const int lane = threadIdx.x & 31;
-  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int group = lane / LPW, glane = lane % LPW;
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * WPW + group;
+  // every collective below is over the walker's own group: a group past the last walker
+  // leaves without disturbing the others
   if (w >= m.n_walkers) return;
-  const unsigned full = 0xffffffffu;
-  GrandBook bk;
-  bk.load(m, w, lane);
-  LjWalker<32, APL> lj;
-  lj.glane = lane;
-  lj.gmask = full;
+  const unsigned gmask = group_mask<LPW>(group);
+  GrandBook<LPW> bk;
+  bk.load(m, w, glane, gmask);
+  LjWalker<LPW, APL> lj;
+  lj.glane = glane;
+  lj.gmask = gmask;
   lj.n = bk.c.N;
   float* pw = m.pos + (size_t)w * 6 * (size_t)m.np;
   lj.load(pw, m.np);
@@ -57,7 +62,7 @@ __global__ void __launch_bounds__(128) lj_grand_kernel(GrandLaunch m) {
       }
     } else if (d.add_bit == 0) {
       // plan_add (lj.rs:292-309): a uniform point of the unit ball times the radius
-      if (!(m.has_max_N && N1 == m.max_N) && N1 + 1 < m.ncol && N1 < 32 * APL) {
+      if (!(m.has_max_N && N1 == m.max_N) && N1 + 1 < m.ncol && N1 < LPW * APL) {
         double ux = 0, uy = 0, uz = 0;
         bool found = false;
         for (int k = 0; k < 64 && !found; ++k) {
@@ -71,7 +76,7 @@ __global__ void __launch_bounds__(128) lj_grand_kernel(GrandLaunch m) {
           float e = 0.0f;
 #pragma unroll
           for (int k = 0; k < APL; ++k) {
-            const int j = lane + 32 * k;
+            const int j = glane + LPW * k;
             if (j < N1) {
               const float dx = (lj.x[k].h - tx.h) + (lj.x[k].l - tx.l);
               const float dy = (lj.y[k].h - ty.h) + (lj.y[k].l - ty.l);
@@ -79,7 +84,7 @@ __global__ void __launch_bounds__(128) lj_grand_kernel(GrandLaunch m) {
               e += lj_v32(dx * dx + dy * dy + dz * dz);
             }
           }
-          de = group_sum<32>(e, full);
+          de = group_sum<LPW>(e, gmask);
           kind_move = 1;
           N2 = N1 + 1;
         }
@@ -91,7 +96,7 @@ __global__ void __launch_bounds__(128) lj_grand_kernel(GrandLaunch m) {
       float e = 0.0f;
 #pragma unroll
       for (int k = 0; k < APL; ++k) {
-        const int j = lane + 32 * k;
+        const int j = glane + LPW * k;
         if (j < N1 && j != which) {
           const float dx = (lj.x[k].h - fx.h) + (lj.x[k].l - fx.l);
           const float dy = (lj.y[k].h - fy.h) + (lj.y[k].l - fy.l);
@@ -99,12 +104,12 @@ __global__ void __launch_bounds__(128) lj_grand_kernel(GrandLaunch m) {
           e += lj_v32(dx * dx + dy * dy + dz * dz);
         }
       }
-      de = -group_sum<32>(e, full);
+      de = -group_sum<LPW>(e, gmask);
       kind_move = 2;
       N2 = N1 - 1;
     }
     const bool possible = kind_move >= 0 && fabsf(de) <= 3.0e38f;
-    if (m.trace && lane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
+    if (m.trace && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
       TraceRec r;
       r.e1 = E1;
       r.e2 = possible ? E1 + (double)de : __longlong_as_double(0x7ff8000000000000ll);
@@ -146,12 +151,17 @@ __global__ void grand_init_kernel(GrandLaunch m) {
 
 }  // namespace dev
 
+#define SADMC_GRAND_CASE(L, A)                                                          \
+  if (m.lanes == L && m.np == L * A) {                                                  \
+    const int warps = (m.n_walkers + (32 / L) - 1) / (32 / L);                          \
+    dev::lj_grand_kernel<L, A><<<(warps + 3) / 4, 128, 0, st>>>(m);                     \
+    return cudaGetLastError();                                                          \
+  }
+
 cudaError_t launch_grand_move(const GrandLaunch& m, cudaStream_t st) {
-  const int blocks = (m.n_walkers + 3) / 4;
-  if (m.np == 32) dev::lj_grand_kernel<1><<<blocks, 128, 0, st>>>(m);
-  else if (m.np == 64) dev::lj_grand_kernel<2><<<blocks, 128, 0, st>>>(m);
-  else return cudaErrorInvalidConfiguration;
-  return cudaGetLastError();
+  SADMC_GRAND_CASE(32, 1) SADMC_GRAND_CASE(16, 2) SADMC_GRAND_CASE(8, 4) SADMC_GRAND_CASE(4, 8)
+  SADMC_GRAND_CASE(32, 2) SADMC_GRAND_CASE(16, 4) SADMC_GRAND_CASE(8, 8)
+  return cudaErrorInvalidConfiguration;
 }
 
 cudaError_t launch_grand_init(const GrandLaunch& m, cudaStream_t st) {

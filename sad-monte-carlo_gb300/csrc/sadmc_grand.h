@@ -47,6 +47,7 @@ struct GrandLaunch {
   float* pos;            // [walker][6][np] double-single positions
   int np, rows, ncol;    // ncol = N_cap + 1
   int n_walkers;
+  int lanes;             // LJ: lanes per walker (32, 16, 8 or 4; np / lanes atoms a lane)
   uint64_t n_moves, seed;
   double width, inv_width, radius, radius2, t0, target_rate, translation_scale;
   double min_allowed, max_allowed;

@@ -447,7 +447,7 @@ class GrandConfig(ctypes.Structure):
                 ("e_lo", ctypes.c_double), ("e_hi", ctypes.c_double),
                 ("seed", ctypes.c_uint64), ("resum_interval", ctypes.c_int32),
                 ("system", ctypes.c_int32), ("drift_tol", ctypes.c_double),
-                ("box", ctypes.c_double * 3)]
+                ("box", ctypes.c_double * 3), ("lanes_per_walker", ctypes.c_int32)]
 
 
 GRAND_SCALARS = ["moves", "accepted", "addremove_probability", "N", "energy", "num_states",
@@ -459,8 +459,9 @@ GRAND_SCALARS = ["moves", "accepted", "addremove_probability", "N", "energy", "n
 def make_grand_config(n_walkers, max_N, radius=0.0, *, box=None, method=SAMC, t0=1e4,
                       energy_bin=1.0, min_allowed=None, max_allowed=None, target_rate=None,
                       translation_scale=0.05, addremove_probability=0.05, e_lo=-200.0,
-                      e_hi=50.0, seed=0, resum_interval=0, drift_tol=0.0):
-    """Energy-number walkers: the LJ cluster of `radius`, or (box given) the WCA fluid."""
+                      e_hi=50.0, seed=0, resum_interval=0, drift_tol=0.0, lanes_per_walker=0):
+    """Energy-number walkers: the LJ cluster of `radius`, or (box given) the WCA fluid.
+    lanes_per_walker: LJ lanes per walker (32, 16, 8, 4; 0 = 8)."""
     c = GrandConfig()
     c.system = WCA if box is not None else LJ
     if box is not None:
@@ -474,6 +475,7 @@ def make_grand_config(n_walkers, max_N, radius=0.0, *, box=None, method=SAMC, t0
     c.translation_scale, c.addremove_probability = translation_scale, addremove_probability
     c.e_lo, c.e_hi, c.seed = e_lo, e_hi, seed
     c.resum_interval, c.drift_tol = resum_interval, drift_tol
+    c.lanes_per_walker = lanes_per_walker
     return c
 
 

@@ -12,13 +12,17 @@ SAME = ("moves", "accepted", "addremove_probability", "N", "num_states", "t_last
         "max_N", "num_E", "addremove_attempts", "addremove_accepted")
 
 
-@pytest.mark.parametrize("method,target", [("samc", None), ("wl", None), ("samc", 0.5)])
-def test_grand_trace_replay(gpu, oracle, method, target):
-    W, moves, max_N, R, seed = 8, 20000, 13, 2.5, 3
+@pytest.mark.parametrize("method,target,lanes,max_N", [
+    ("samc", None, 8, 13), ("wl", None, 8, 13), ("samc", 0.5, 8, 13), ("samc", None, 32, 13),
+    ("wl", None, 4, 13), ("samc", None, 16, 40), ("wl", 0.5, 8, 40)])
+def test_grand_trace_replay(gpu, oracle, method, target, lanes, max_N):
+    """Walker groups of `lanes` lanes; 7 walkers leave the last warp partly empty."""
+    W, moves, R, seed = 7, 20000, 2.5, 3
     m = gpu.SAMC if method == "samc" else gpu.WL
     common = dict(t0=1000.0, energy_bin=0.5, max_allowed=10.0, translation_scale=0.1,
                   addremove_probability=0.1, target_rate=target, seed=seed)
-    b = gpu.GrandBatch(gpu.make_grand_config(W, max_N, R, method=m, e_lo=-60.0, e_hi=12.0, **common))
+    b = gpu.GrandBatch(gpu.make_grand_config(W, max_N, R, method=m, e_lo=-200.0, e_hi=12.0,
+                                             lanes_per_walker=lanes, **common))
     b.set_trace(moves)
     b.run(moves)
     for w in range(W):
