@@ -87,14 +87,57 @@ def _lanes(b, lpw, tune_moves):
     return b.lanes_per_walker()
 
 
+def c1_inputs(seed=11):
+    """C1: one 32x32 Ising lattice, uniform random spins from the seed."""
+    rng = np.random.default_rng(seed)
+    return 32, np.where(rng.random(32 * 32) < 0.5, -1.0, 1.0)
+
+
+def c3_inputs(seed=11, walkers=2048):
+    """C3: WCA, N in {64,128,256,512}, density U[0.6, 0.9], a random subset of a
+    jittered simple-cubic lattice filling each box: [(n, box edge, positions)]."""
+    rng = np.random.default_rng(seed)
+    rng.random(32 * 32)  # the C1 spins come first from this seed
+    ns = rng.choice([64, 128, 256, 512], walkers)
+    rhos = rng.uniform(0.6, 0.9, walkers)
+    out = []
+    for n, rho in zip(ns, rhos):
+        Lb = (n / rho) ** (1 / 3)
+        m = int(np.ceil(n ** (1 / 3)))
+        g = np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)
+        g = g[rng.permutation(len(g))[:n]]
+        out.append((int(n), Lb, np.mod((g + 0.5 + rng.uniform(-0.05, 0.05, g.shape)) * (Lb / m), Lb)))
+    return out
+
+
+def c5_inputs(seed=11, walkers=1024):
+    """C5: N = 1024 hard-core square-well atoms on a jittered FCC lattice, packing
+    fraction U[0.30, 0.50]: [(box edge, positions)]."""
+    rng = np.random.default_rng(seed + 1)
+    n5 = 1024
+    m = int(np.ceil((n5 / 4) ** (1 / 3)))
+    base = np.array([(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)])
+    sites = (np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)[:, None, :]
+             + base[None]).reshape(-1, 3)
+    out = []
+    for eta in rng.uniform(0.30, 0.50, walkers):
+        Lb = (n5 * np.pi / (6 * eta)) ** (1 / 3)
+        pick = sites[rng.permutation(len(sites))[:n5]]
+        out.append((Lb, np.mod((pick + rng.uniform(-0.004, 0.004, pick.shape)) * (Lb / m), Lb)))
+    return out
+
+
+C3_METHOD = dict(t0=1e4, energy_bin=1.0, max_allowed=500.0, translation_scale=0.1)
+C5_METHOD = dict(well_width=1.3, translation_scale=0.05)
+
+
 def case_c1(G, seed=11, moves=1_000_000, lpw=0, **_):
     """C1: plain SAD, Ising 32x32, one walker, bins of 4 over [-2N, 2N]."""
-    rng = np.random.default_rng(seed)
-    L = 32
+    L, spins = c1_inputs(seed)
     b = G.Batch(G.make_config(G.ISING, 1, L, method=G.SAD, min_T=0.2, e_lo=-2.0 * L * L - 8,
                               e_hi=2.0 * L * L + 8, seed=seed, lanes_per_walker=lpw),
                 [(L, 0.0, (0, 0, 0))])
-    b.upload([np.where(rng.random(L * L) < 0.5, -1.0, 1.0)])
+    b.upload([spins])
     b.initialize()
     lanes = _lanes(b, lpw, 20000)
     sec = _time_run(b, moves, 100_000)
@@ -104,28 +147,33 @@ def case_c1(G, seed=11, moves=1_000_000, lpw=0, **_):
             "lanes_per_walker": lanes}
 
 
+def case_c1_batch(G, seed=11, walkers=4096, moves=20000, lpw=0):
+    """The C1 lattice and method for many independent walkers (spins from seed + walker):
+    the shape in which a GPU runs Ising work; C1 itself is one serial chain."""
+    L = 32
+    b = G.Batch(G.make_config(G.ISING, walkers, L, method=G.SAD, min_T=0.2,
+                              e_lo=-2.0 * L * L - 8, e_hi=2.0 * L * L + 8, seed=seed,
+                              lanes_per_walker=lpw),
+                [(L, 0.0, (0, 0, 0))] * walkers)
+    b.upload([c1_inputs(seed + w)[1] for w in range(walkers)])
+    b.initialize()
+    lanes = _lanes(b, lpw, 2000)
+    sec = _time_run(b, moves, 4000)
+    b.close()
+    return {"workload": f"Ising 32x32, plain SAD (min_T 0.2), {walkers} independent walkers",
+            "moves": walkers * moves, "moves_per_s": walkers * moves / sec,
+            "lanes_per_walker": lanes}
+
+
 def case_c3(G, seed=11, walkers=2048, moves=2048, lpw=0):
-    """C3: WCA, N in {64,128,256,512}, density in [0.6, 0.9], SAMC t0 = 1e4, 500 bins over
-    [0, 500) (a range fixed here; the workload states none); simple-cubic starts with a
-    jitter, brought below 500 by the descent of initialize()."""
-    rng = np.random.default_rng(seed)
-    rng.random(32 * 32)  # the C1 spins come first from this seed
-    ns = rng.choice([64, 128, 256, 512], walkers)
-    rhos = rng.uniform(0.6, 0.9, walkers)
-    geo, states = [], []
-    for n, rho in zip(ns, rhos):
-        Lb = (n / rho) ** (1 / 3)
-        m = int(np.ceil(n ** (1 / 3)))
-        g = np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)
-        g = g[rng.permutation(len(g))[:n]]
-        pos = np.mod((g + 0.5 + rng.uniform(-0.05, 0.05, g.shape)) * (Lb / m), Lb)
-        geo.append((int(n), 0.0, (Lb, Lb, Lb)))
-        states.append(pos)
-    b = G.Batch(G.make_config(G.WCA, walkers, int(ns.max()), method=G.SAMC, t0=1e4,
-                              energy_bin=1.0, e_lo=-1.0, e_hi=501.0, max_allowed=500.0,
-                              translation_scale=0.1, seed=seed, resum_interval=4096,
-                              lanes_per_walker=lpw), geo)
-    b.upload(states)
+    """C3: WCA, SAMC t0 = 1e4, 500 bins over [0, 500) (a range fixed here; the workload
+    states none); the descent of initialize() brings each walker below 500."""
+    inp = c3_inputs(seed, walkers)
+    nmax = max(n for n, _, _ in inp)
+    b = G.Batch(G.make_config(G.WCA, walkers, nmax, method=G.SAMC, e_lo=-1.0, e_hi=501.0,
+                              seed=seed, resum_interval=4096, lanes_per_walker=lpw, **C3_METHOD),
+                [(n, 0.0, (Lb, Lb, Lb)) for n, Lb, _ in inp])
+    b.upload([p for _, _, p in inp])
     b.initialize()
     lanes = _lanes(b, lpw, 256)
     sec = _time_run(b, moves, 512)
@@ -137,25 +185,13 @@ def case_c3(G, seed=11, walkers=2048, moves=2048, lpw=0):
 
 
 def case_c5(G, seed=11, walkers=1024, moves=2048, lpw=0):
-    """C5: hard-core square well (lambda 1.3), N = 1024, packing fraction U[0.30, 0.50],
-    jittered FCC, Wang-Landau over contact-count bins of width 1."""
-    rng = np.random.default_rng(seed + 1)
-    n5 = 1024
-    m = int(np.ceil((n5 / 4) ** (1 / 3)))
-    base = np.array([(0, 0, 0), (0.5, 0.5, 0), (0.5, 0, 0.5), (0, 0.5, 0.5)])
-    sites = (np.array([(i, j, k) for i in range(m) for j in range(m) for k in range(m)], float)[:, None, :]
-             + base[None]).reshape(-1, 3)
-    geo, states = [], []
-    for eta in rng.uniform(0.30, 0.50, walkers):
-        Lb = (n5 * np.pi / (6 * eta)) ** (1 / 3)
-        pick = sites[rng.permutation(len(sites))[:n5]]
-        pos = np.mod((pick + rng.uniform(-0.004, 0.004, pick.shape)) * (Lb / m), Lb)
-        geo.append((n5, 0.0, (Lb, Lb, Lb)))
-        states.append(pos)
-    b = G.Batch(G.make_config(G.SW, walkers, n5, method=G.WL, e_lo=-6.0 * n5 - 2, e_hi=2.0,
-                              well_width=1.3, translation_scale=0.05, seed=seed,
-                              lanes_per_walker=lpw), geo)
-    b.upload(states)
+    """C5: hard-core square well (lambda 1.3), Wang-Landau over contact-count bins of
+    width 1."""
+    inp = c5_inputs(seed, walkers)
+    b = G.Batch(G.make_config(G.SW, walkers, 1024, method=G.WL, e_lo=-6.0 * 1024 - 2, e_hi=2.0,
+                              seed=seed, lanes_per_walker=lpw, **C5_METHOD),
+                [(1024, 0.0, (Lb, Lb, Lb)) for Lb, _ in inp])
+    b.upload([p for _, p in inp])
     b.initialize()
     lanes = _lanes(b, lpw, 256)
     sec = _time_run(b, moves, 512)
@@ -184,15 +220,52 @@ def case_grand(G, seed=11, walkers=4096, moves=4096, lpw=0):
     return out
 
 
-CASES = {"C1": case_c1, "C3": case_c3, "C5": case_c5, "grand": case_grand}
+CASES = {"C1": case_c1, "C1_batch": case_c1_batch, "C3": case_c3, "C5": case_c5,
+         "grand": case_grand}
 
 
-def other_configs(G, seed=11):
+def cpu_cases(seed=11):
+    """The FP64 oracle on the same inputs as C1, C3 and C5, each on a bounded sample (its
+    first walkers, fewer moves), on the host threads: the reference's CPU algorithm
+    beside the GPU numbers."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    out = {}
+    L, spins = c1_inputs(seed)
+    moves = 2_000_000
+    cfg = O.make_config(O.ISING, L, method=O.M_SAD, min_T=0.2, seed=seed, walker=0)
+    sec, tm, _ = O.bench([cfg], [spins], moves, 1)
+    out["C1"] = {"moves_per_s": tm / sec, "threads": 1, "sample": f"1 walker x {moves} moves"}
+    w3, m3 = 256, 8000
+    inp = c3_inputs(seed, w3)
+    cfgs = [O.make_config(O.WCA, n, box=(Lb, Lb, Lb), method=O.M_SAMC, seed=seed, walker=w,
+                          **C3_METHOD) for w, (n, Lb, _) in enumerate(inp)]
+    sec, tm, _ = O.bench(cfgs, [p for _, _, p in inp], m3, threads)
+    out["C3"] = {"moves_per_s": tm / sec, "threads": threads,
+                 "sample": f"first {w3} walkers x {m3} moves"}
+    w5, m5 = 128, 8000
+    inp = c5_inputs(seed, w5)
+    cfgs = [O.make_config(O.SW, 1024, box=(Lb, Lb, Lb), method=O.M_WL, seed=seed, walker=w,
+                          **C5_METHOD) for w, (Lb, _) in enumerate(inp)]
+    sec, tm, _ = O.bench(cfgs, [p for _, p in inp], m5, threads)
+    out["C5"] = {"moves_per_s": tm / sec, "threads": threads,
+                 "sample": f"first {w5} walkers x {m5} moves"}
+    return out
+
+
+def other_configs(G, seed=11, cpu=True):
     """Device-resident moves/s of the other workloads (synthetic seeded inputs with their
     shapes): C1 one Ising 32x32 walker, C3 an uneven WCA batch, C5 a hard-core square-well
     batch, and the grand-canonical LJ cluster.  Each is a short run after a warm-up, timed
-    with CUDA events."""
-    return {k: f(G, seed) for k, f in CASES.items()}
+    with CUDA events.  With cpu, the oracle's moves/s on a sample of the same inputs sits
+    beside C1, C3 and C5 (`cpu`)."""
+    out = {k: f(G, seed) for k, f in CASES.items()}
+    if cpu:
+        for k, v in cpu_cases(seed).items():
+            out[k]["cpu"] = v
+    return out
 
 
 def da_compare(G, rank=0, walkers=8192, moves=2048):
@@ -464,7 +537,7 @@ def run_gpu(args):
         da = da_compare(G, rank)
     others = None
     if not args.no_other and rank == 0:
-        others = other_configs(G)
+        others = other_configs(G, cpu=not args.no_cpu)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -242,7 +242,7 @@ std::vector<DevBuf> state_buffers(sadmc_handle* h) {
     case SADMC_LJ: v.push_back({h->d_pos, W * 6 * np * sizeof(float)}); break;
     default:
       v.push_back({h->d_pos64, W * 3 * np * sizeof(double)});
-      v.push_back({h->d_pos32, W * 4 * np * sizeof(float)});
+      v.push_back({h->d_pos32, W * 8 * np * sizeof(float)});
       v.push_back({h->d_ncell, W * 3 * sizeof(int)});
       v.push_back({h->d_cell_of, W * np * sizeof(int)});
       v.push_back({h->d_cnt, W * (size_t)h->cell_cap * sizeof(int)});
@@ -448,7 +448,7 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
     else if (c.system == SADMC_LJ) ok = dalloc(&h->d_pos, (size_t)h->W * 6 * h->np) == cudaSuccess;
     else {
       const size_t W = h->W, np = h->np, cap = h->cell_cap;
-      ok = dalloc(&h->d_pos64, W * 3 * np) == cudaSuccess && dalloc(&h->d_pos32, W * 4 * np) == cudaSuccess &&
+      ok = dalloc(&h->d_pos64, W * 3 * np) == cudaSuccess && dalloc(&h->d_pos32, W * 8 * np) == cudaSuccess &&
            dalloc(&h->d_box, W * 3) == cudaSuccess && dalloc(&h->d_ncell, W * 3) == cudaSuccess &&
            dalloc(&h->d_cell_of, W * np) == cudaSuccess && dalloc(&h->d_cnt, W * cap) == cudaSuccess &&
            dalloc(&h->d_atoms, W * cap * h->bucket) == cudaSuccess &&
@@ -1403,13 +1403,13 @@ int32_t sadmc_grand_create(const sadmc_grand_config* c, sadmc_grand** out) {
   if (e == cudaSuccess) e = cudaMalloc(&h->d_pos, sizeof(float) * W * 6 * h->np);
   if (e == cudaSuccess && wca) {
     e = cudaMalloc(&h->d_pos64, sizeof(double) * W * 3 * h->np);
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_pos32, sizeof(float) * W * 4 * h->np);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_pos32, sizeof(float) * W * 8 * h->np);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_cell_of, sizeof(int) * W * h->np);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_cnt, sizeof(int) * W * h->cell_cap);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_atoms, sizeof(int) * W * h->cell_cap * h->bucket);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->d_cnt, 0, sizeof(int) * W * h->cell_cap, h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->d_pos64, 0, sizeof(double) * W * 3 * h->np, h->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_pos32, 0, sizeof(float) * W * 4 * h->np, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_pos32, 0, sizeof(float) * W * 8 * h->np, h->stream);
   }
   if (e != cudaSuccess) { sadmc_grand_destroy(h); return fail(SADMC_ERR_NOMEM, cudaGetErrorString(e)); }
   char* b = (char*)h->plane_mem;

@@ -17,7 +17,7 @@ __global__ void cell_build_kernel(const WalkerCore* cores, CellSys s, int n_walk
   if (w >= n_walkers) return;
   const int n = cores[w].n;
   const double* p = s.pos + (size_t)w * 3 * s.np;
-  float4* p32 = reinterpret_cast<float4*>(s.pos32) + (size_t)w * s.np;
+  float4* p32 = reinterpret_cast<float4*>(s.pos32) + (size_t)w * 2 * s.np;
   int* cell_of = s.cell_of + (size_t)w * s.np;
   int* cnt = s.cell_count + (size_t)w * s.cell_cap;
   int* atoms = s.cell_atoms + (size_t)w * s.cell_cap * s.bucket;
@@ -37,7 +37,8 @@ __global__ void cell_build_kernel(const WalkerCore* cores, CellSys s, int n_walk
   for (int c = 0; c < nc[0] * nc[1] * nc[2]; ++c) cnt[c] = 0;
   for (int i = 0; i < n; ++i) {
     const double x = p[i], y = p[s.np + i], z = p[2 * s.np + i];
-    p32[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+    if (s.kind == SYS_WCA) put_ds<true>(p32, i, x, y, z);
+    else put_ds<false>(p32, i, x, y, z);
     if (!(x >= 0.0 && x < L[0] && y >= 0.0 && y < L[1] && z >= 0.0 && z < L[2])) {
       *status = ST_BAD_INPUT;
       return;
@@ -119,13 +120,14 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
   cw.np = m.np;
   cw.bucket = m.bucket;
   cw.p = m.pos64 + (size_t)w * 3 * m.np;
-  cw.p32 = reinterpret_cast<float4*>(m.pos32) + (size_t)w * m.np;
+  cw.p32 = reinterpret_cast<float4*>(m.pos32) + (size_t)w * 2 * m.np;
   cw.cell_of = m.cell_of + (size_t)w * m.np;
   cw.cnt = m.cell_count + (size_t)w * m.cell_cap;
   cw.atoms = m.cell_atoms + (size_t)w * m.cell_cap * m.bucket;
   for (int a = 0; a < 3; ++a) {
     cw.L[a] = m.box[a];
     cw.L32[a] = (float)m.box[a];
+    cw.Ll32[a] = (float)(m.box[a] - (double)cw.L32[a]);
     cw.nc[a] = m.nc[a];
   }
   const double wsqr = m.r_cut * m.r_cut;
@@ -142,9 +144,9 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
     int cn = 0;
     bool ov = false;
     float e = 0.0f;
+    const Query q = make_query<true>(qx, qy, qz);
     for (int k = lane; k < 27; k += 32)
-      CellOps<32, SYS_WCA>::scan(cw, k, cx, cy, cz, qx, qy, qz, (float)qx, (float)qy, (float)qz,
-                                 skip, wsqr, wsqr32, true, cn, ov, e, wsqr32);
+      CellOps<32, SYS_WCA>::scan(cw, k, cx, cy, cz, q, skip, wsqr, wsqr32, true, cn, ov, e);
     return group_sum<32>(e, full);
   };
   const double sc = m.translation_scale;
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
           }
           cw.cell_of[a] = new_c;
           cw.p[a] = tx; cw.p[cw.np + a] = ty; cw.p[2 * cw.np + a] = tz;
-          cw.p32[a] = make_float4((float)tx, (float)ty, (float)tz, 0.0f);
+          put_ds<true>(cw.p32, a, tx, ty, tz);
         }
       } else if (which != N1 - 1) {
         // swap_remove: atom N1 - 1 takes index `which` (rename_neighbor, optcell.rs:419)
@@ -266,7 +268,8 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
           cw.p[which] = cw.p[last];
           cw.p[cw.np + which] = cw.p[cw.np + last];
           cw.p[2 * cw.np + which] = cw.p[2 * cw.np + last];
-          cw.p32[which] = cw.p32[last];
+          cw.p32[2 * which] = cw.p32[2 * last];
+          cw.p32[2 * which + 1] = cw.p32[2 * last + 1];
         }
       }
       __syncwarp(full);

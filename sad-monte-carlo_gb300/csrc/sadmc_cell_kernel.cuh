@@ -15,8 +15,9 @@
 // of optsquare.rs:74-95 on the FP64 expression (p_j - off*L) - r, x*x + y*y + z*z.  They
 // are taken from binary32 copies when the binary32 r^2 lies outside a proven error
 // margin of both thresholds, else from the FP64 expression itself.  Energies are
-// integers and exact.  WCA: binary32 pair energies (wca.rs:66-76), FP64 re-sum every
-// resum_interval moves.
+// integers and exact.  WCA: binary32 pair energies (wca.rs:66-76) on differences of
+// double-single positions (close pairs keep their relative precision), FP64 re-sum
+// every resum_interval moves.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -67,12 +68,13 @@ __device__ __forceinline__ double wrap_axis(double r, double L, bool* bad) {
 
 struct CellWalker {
   double* p;       // [3][np] FP64 planes of this walker
-  float4* p32;     // [np] binary32 copy (w unused)
+  float4* p32;     // binary32 copy, 2 np float4: WCA (x, y, z) high and low parts of
+                   // atom j at 2j and 2j + 1; square well high parts at j
   int* cell_of;    // [np]
   int* cnt;        // [cells]
   int* atoms;      // [cells][bucket]
   double L[3];
-  float L32[3];
+  float L32[3], Ll32[3];  // the box as double-single binary32
   int nc[3];
   int np, bucket;
   __device__ int cell_index(int x, int y, int z) const { return (x * nc[1] + y) * nc[2] + z; }
@@ -119,14 +121,68 @@ __device__ __forceinline__ double wca_pressure64(double r2, double rc2) {
   return 4.0 * 3.0 * (2.0 * powi6(s) - powi3(s));
 }
 
+// A query point: its FP64 coordinates and their double-single binary32 copy.
+struct Query {
+  double x, y, z;
+  float hx, hy, hz, lx, ly, lz;
+};
+// WITH_LO: the low parts too (the WCA pair terms use them; the square well does not).
+template <bool WITH_LO>
+__device__ __forceinline__ Query make_query(double x, double y, double z) {
+  Query q;
+  q.x = x; q.y = y; q.z = z;
+  q.hx = (float)x; q.hy = (float)y; q.hz = (float)z;
+  q.lx = q.ly = q.lz = 0.0f;
+  if (WITH_LO) {
+    q.lx = (float)(x - (double)q.hx); q.ly = (float)(y - (double)q.hy); q.lz = (float)(z - (double)q.hz);
+  }
+  return q;
+}
+template <bool WITH_LO>
+__device__ __forceinline__ Query query_of(const CellWalker& cw, int a) {
+  const float4 h = cw.p32[WITH_LO ? 2 * a : a];
+  const float4 l = WITH_LO ? cw.p32[2 * a + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+  Query q;
+  q.x = cw.p[a]; q.y = cw.p[cw.np + a]; q.z = cw.p[2 * cw.np + a];
+  q.hx = h.x; q.hy = h.y; q.hz = h.z; q.lx = l.x; q.ly = l.y; q.lz = l.z;
+  return q;
+}
+// The binary32 copy of atom j: WITH_LO (WCA) high and low parts side by side at 2j and
+// 2j + 1, so a refined pair reads one 32-byte sector; else (square well) the high parts
+// alone at j, densely packed for the screen.
+template <bool WITH_LO>
+__device__ __forceinline__ void put_ds(float4* p32, int j, double x, double y, double z) {
+  const float hx = (float)x, hy = (float)y, hz = (float)z;
+  if (WITH_LO) {
+    p32[2 * j] = make_float4(hx, hy, hz, 0.0f);
+    p32[2 * j + 1] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
+                                 (float)(z - (double)hz), 0.0f);
+  } else {
+    p32[j] = make_float4(hx, hy, hz, 0.0f);
+  }
+}
+// (p - off L) - q on one axis, p = ph + pl, q = qh + ql, L = Lh + Ll (off in -1, 0, 1).
+// ph - qh is split exactly into a + e (two-sum); for a pair within reach of the cutoff
+// a - off Lh is exact (the two are within a factor of 2 because the box holds at least
+// 3 subcells of the cutoff), so the difference keeps its relative precision however
+// small it is.
+__device__ __forceinline__ float ds_image_diff(float ph, float pl, float qh, float ql, float off,
+                                               float Lh, float Ll) {
+  const float a = __fsub_rn(ph, qh);
+  const float bb = __fsub_rn(a, ph);
+  const float e = __fadd_rn(__fsub_rn(ph, __fsub_rn(a, bb)), __fsub_rn(-qh, bb));
+  const float b = __fsub_rn(a, off * Lh);
+  const float lo = __fadd_rn(e, __fsub_rn(__fsub_rn(pl, ql), off * Ll));
+  return __fadd_rn(b, lo);
+}
+
 template <int LPW, int KIND>
 struct CellOps {
-  // Sum over the 27 buckets around cell (cx,cy,cz) of query position q (excluding atom
-  // `skip`).  SW: counts contacts, sets *overlap; WCA: binary32 energy.
-  __device__ static void scan(const CellWalker& cw, int k0, int cx, int cy, int cz, double qx,
-                              double qy, double qz, float q32x, float q32y, float q32z, int skip,
-                              double wsqr, float wsqr32, bool newq, int& contacts, bool& overlap,
-                              float& e32, float rc2_32) {
+  // Sum over the 27 buckets around cell (cx,cy,cz) of query q (excluding atom `skip`).
+  // SW: counts contacts, sets *overlap; WCA: binary32 energy.
+  __device__ static void scan(const CellWalker& cw, int k0, int cx, int cy, int cz, const Query& q,
+                              int skip, double wsqr, float wsqr32, bool newq, int& contacts,
+                              bool& overlap, float& e32) {
     // k0: the neighbour offset handled by this lane (0..26)
     const int dx = k0 / 9 - 1, dy = (k0 / 3) % 3 - 1, dz = k0 % 3 - 1;
     int ux = cx + dx, uy = cy + dy, uz = cz + dz;
@@ -137,12 +193,16 @@ struct CellOps {
     const int c = cw.cell_index(ux, uy, uz);
     const int m = min(cw.cnt[c], cw.bucket);
     const int* list = cw.atoms + (size_t)c * cw.bucket;
-    const float sx = (float)ox * cw.L32[0], sy = (float)oy * cw.L32[1], sz = (float)oz * cw.L32[2];
+    const float fx = (float)ox, fy = (float)oy, fz = (float)oz;
+    const float sx = fx * cw.L32[0], sy = fy * cw.L32[1], sz = fz * cw.L32[2];
+    // WCA: pairs whose high-part r^2 may lie inside the cutoff (the high parts are within
+    // 2^-24 |L| of each coordinate) are refined on the double-single positions
+    const float screen = wsqr32 + 1e-3f;
     for (int k = 0; k < m; ++k) {
       const int j = list[k];
       if (j == skip) continue;
-      const float4 pj = cw.p32[j];
-      const float ax = (pj.x - sx) - q32x, ay = (pj.y - sy) - q32y, az = (pj.z - sz) - q32z;
+      const float4 pj = cw.p32[KIND == SYS_WCA ? 2 * j : j];
+      const float ax = (pj.x - sx) - q.hx, ay = (pj.y - sy) - q.hy, az = (pj.z - sz) - q.hz;
       const float d2 = ax * ax + ay * ay + az * az;
       if (KIND == SYS_SW) {
         bool near = fabsf(d2 - 1.0f) < 2e-4f || fabsf(d2 - wsqr32) < 2e-4f;
@@ -151,22 +211,19 @@ struct CellOps {
           else if (d2 < wsqr32) ++contacts;
         } else {
           // the reference's FP64 expression (optsquare.rs:78-86)
-          const double bx = (cw.p[j] - (double)ox * cw.L[0]) - qx;
-          const double by = (cw.p[cw.np + j] - (double)oy * cw.L[1]) - qy;
-          const double bz = (cw.p[2 * cw.np + j] - (double)oz * cw.L[2]) - qz;
+          const double bx = (cw.p[j] - (double)ox * cw.L[0]) - q.x;
+          const double by = (cw.p[cw.np + j] - (double)oy * cw.L[1]) - q.y;
+          const double bz = (cw.p[2 * cw.np + j] - (double)oz * cw.L[2]) - q.z;
           const double e2 = bx * bx + by * by + bz * bz;
           if (e2 < 1.0) { if (newq) overlap = true; else ++contacts; }
           else if (e2 < wsqr) ++contacts;
         }
-      } else if (d2 < 0.81f) {
-        // a close pair (V > 7): the binary32 copies lose relative precision in r^2 as r
-        // shrinks, so take the distance from the FP64 positions
-        const double bx = (cw.p[j] - (double)ox * cw.L[0]) - qx;
-        const double by = (cw.p[cw.np + j] - (double)oy * cw.L[1]) - qy;
-        const double bz = (cw.p[2 * cw.np + j] - (double)oz * cw.L[2]) - qz;
-        e32 += (float)wca_v64(bx * bx + by * by + bz * bz, wsqr);
-      } else {
-        e32 += wca_v32(d2, rc2_32);
+      } else if (d2 < screen) {
+        const float4 pl = cw.p32[2 * j + 1];
+        const float rx = ds_image_diff(pj.x, pl.x, q.hx, q.lx, fx, cw.L32[0], cw.Ll32[0]);
+        const float ry = ds_image_diff(pj.y, pl.y, q.hy, q.ly, fy, cw.L32[1], cw.Ll32[1]);
+        const float rz = ds_image_diff(pj.z, pl.z, q.hz, q.lz, fz, cw.L32[2], cw.Ll32[2]);
+        e32 += wca_v32(rx * rx + ry * ry + rz * rz, wsqr32);
       }
     }
   }
@@ -174,7 +231,7 @@ struct CellOps {
 
 // FAM: the method the kernel is specialised for, or FAM_ANY (the method each walker holds).
 template <int LPW, int KIND, int FAM>
-__global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s) {
+__global__ void __launch_bounds__(128, 1) cell_move_kernel(MoveLaunch m, CellSys s) {
   constexpr int WPW = 32 / LPW;
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -191,13 +248,14 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
   cw.np = s.np;
   cw.bucket = s.bucket;
   cw.p = s.pos + (size_t)w * 3 * s.np;
-  cw.p32 = reinterpret_cast<float4*>(s.pos32) + (size_t)w * s.np;
+  cw.p32 = reinterpret_cast<float4*>(s.pos32) + (size_t)w * 2 * s.np;
   cw.cell_of = s.cell_of + (size_t)w * s.np;
   cw.cnt = s.cell_count + (size_t)w * s.cell_cap;
   cw.atoms = s.cell_atoms + (size_t)w * s.cell_cap * s.bucket;
   for (int a = 0; a < 3; ++a) {
     cw.L[a] = s.box[3 * w + a];
     cw.L32[a] = (float)cw.L[a];
+    cw.Ll32[a] = (float)(cw.L[a] - (double)cw.L32[a]);
     cw.nc[a] = s.ncell[3 * w + a];
   }
   const int n = fh.c.n;
@@ -210,7 +268,7 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
   struct Prop {
     int a, old_c, new_c, new_count;
     double fx, fy, fz, tx, ty, tz;
-    float t32x, t32y, t32z, de;
+    float de;
     bool possible;
   };
   auto plan = [&](int a, float g0, float g1, float g2, double sc) {
@@ -227,18 +285,17 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
     p.old_c = cw.cell_of[a];
     const int ocx = p.old_c / (cw.nc[1] * cw.nc[2]), ocy = (p.old_c / cw.nc[2]) % cw.nc[1],
               ocz = p.old_c % cw.nc[2];
-    p.t32x = (float)p.tx; p.t32y = (float)p.ty; p.t32z = (float)p.tz;
-    const float4 f32 = cw.p32[a];
+    const Query qt = make_query<KIND == SYS_WCA>(p.tx, p.ty, p.tz);
+    const Query qf = query_of<KIND == SYS_WCA>(cw, a);
     int cn = 0, co = 0;
     bool overlap = false;
     float en = 0.0f, eo = 0.0f;
     for (int k = glane; k < 54; k += LPW) {
       if (k < 27)
-        CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, p.tx, p.ty, p.tz, p.t32x, p.t32y, p.t32z, a,
-                                 wsqr, wsqr32, true, cn, overlap, en, wsqr32);
+        CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, qt, a, wsqr, wsqr32, true, cn, overlap, en);
       else
-        CellOps<LPW, KIND>::scan(cw, k - 27, ocx, ocy, ocz, p.fx, p.fy, p.fz, f32.x, f32.y, f32.z,
-                                 a, wsqr, wsqr32, false, co, overlap, eo, wsqr32);
+        CellOps<LPW, KIND>::scan(cw, k - 27, ocx, ocy, ocz, qf, a, wsqr, wsqr32, false, co, overlap,
+                                 eo);
     }
     p.new_c = cw.cell_index(nx, ny, nz);
     if (KIND == SYS_SW) {
@@ -285,7 +342,7 @@ __global__ void __launch_bounds__(128) cell_move_kernel(MoveLaunch m, CellSys s)
     }
     if (wr) {
       cw.p[a] = p.tx; cw.p[s.np + a] = p.ty; cw.p[2 * s.np + a] = p.tz;
-      cw.p32[a] = make_float4(p.t32x, p.t32y, p.t32z, 0.0f);
+      put_ds<KIND == SYS_WCA>(cw.p32, a, p.tx, p.ty, p.tz);
     }
     __syncwarp(gmask);
   };

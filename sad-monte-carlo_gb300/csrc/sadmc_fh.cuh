@@ -284,7 +284,7 @@ struct Fh {
   // lane hide the FP64 divide latency and cover 4*LPW moves per evaluation.
   __device__ double gamma() {
     if (kind() != M_SAD && kind() != M_SAMC) return gamma_at(c.moves);
-    if (!gb_valid || gb_off >= (uint32_t)(4 * LPW)) {
+    if (SADMC_RARE(!gb_valid || gb_off >= (uint32_t)(4 * LPW))) {
       gb_off = 0;
       if (kind() == M_SAD) {
         if (c.tF != inv_tF_of) { inv_tF = 1.0 / (double)c.tF; inv_tF_of = c.tF; }
@@ -437,7 +437,7 @@ struct Fh {
     if (oob) return true;
     if (c.kind == M_DESCENT) return !ltE();
     // prepare_for_state: only when e2 may lie outside [cur_min, cur_max)
-    if (lt(cminf, c.cur_min) || !lt(cmaxf, cur_max)) {
+    if (SADMC_RARE(lt(cminf, c.cur_min) || !lt(cmaxf, cur_max))) {
       if (!prepare(exact())) { c.status |= ST_BIN_RANGE; return true; }
       if (grew_front) reindex_after_growth();
     }
@@ -451,7 +451,7 @@ struct Fh {
       const float m = (tol + fabsf(cminf) * 2.5e-7f) * inv_wf + fabsf(q) * 2.5e-7f + 1e-6f;
       i2 = (fr > m && fr < 1.0f - m) ? qi + c.b_lo : gidx(exact());
     }
-    if (i2 < c.b_lo || i2 > c.b_hi) {
+    if (SADMC_RARE(i2 < c.b_lo || i2 > c.b_hi)) {
       c.status |= ST_BIN_RANGE;
       return true;
     }
@@ -465,7 +465,7 @@ struct Fh {
         if (i2 <= win_lo || i2 >= win_hi) exact();  // extrapolation / edge comparisons
         const double lnw2 = sad_lnw(e2, i2);
         rejected = dgt(lnw2, lnw1) && metropolis_reject2(lnw1, lnw2, u53);
-        if (!rejected && hist2 == 0) {  // energy.rs:466-483
+        if (SADMC_RARE(!rejected && hist2 == 0)) {  // energy.rs:466-483
           exact();
           if (e2 < c.too_hi && e2 > c.too_lo) {
             c.latest_param = (c.too_hi - c.too_lo) / c.min_T;
@@ -503,7 +503,7 @@ struct Fh {
     int old_cur = cur;
     if (accepted) adopt_pending(i2);
     const double E = c.E;
-    if (k_hist == 0) {  // energy.rs:938-940
+    if (SADMC_RARE(k_hist == 0)) {  // energy.rs:938-940
       k_tf = c.moves;
       if (kind() == M_SAD && cur >= win_lo && cur <= win_hi && c.moves > c.win_tmax) c.win_tmax = c.moves;
     }
@@ -528,7 +528,7 @@ struct Fh {
   // energy.rs:514-761
   __device__ void update_weights(double energy) {
     double g = gamma();
-    if (is_nan64(g)) c.status |= ST_NAN_GAMMA;
+    if (SADMC_RARE(is_nan64(g))) c.status |= ST_NAN_GAMMA;
     double old = k_lnw;
     k_lnw += g;
     if (kind() == M_SAD) sad_update(energy, old);
@@ -538,7 +538,7 @@ struct Fh {
   __device__ void sad_update(double energy, double old_lnw) {  // energy.rs:523-636
     const bool e_below = below(energy, cur), e_above = above(energy, cur);
     if (inverted || e_below || e_above) k_lnw = old_lnw;
-    if (k_hist > c.highest_hist) {
+    if (SADMC_RARE(k_hist > c.highest_hist)) {
       c.highest_hist = k_hist;
       if (e_above) {
         const double base = ld_lnw(win_hi);
@@ -592,7 +592,7 @@ struct Fh {
         gb_valid = false;
       }
     }
-    if (c.tL == c.moves) {
+    if (SADMC_RARE(c.tL == c.moves)) {
       uint64_t old_tF = c.tF;
       c.tF = c.win_tmax;
       gb_valid = false;
@@ -702,7 +702,7 @@ struct RecentScale {
   __device__ void init() { off = 32; }
   // called once per move with consecutive t
   __device__ void get(uint64_t t, int lane, double& r, double& om) {
-    if (off >= 32) {
+    if (SADMC_RARE(off >= 32)) {
       off = 0;
       double v = sqrt(1.0 / (double)(t + (uint64_t)lane));
       rs = v;

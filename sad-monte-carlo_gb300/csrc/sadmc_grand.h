@@ -56,7 +56,8 @@ struct GrandLaunch {
   uint64_t trace_cap, trace_t0;
   int resum_interval;
   double drift_tol;
-  // WCA fluid (system 2): FP64 positions [walker][3][np], binary32 copies [walker][np],
+  // WCA fluid (system 2): FP64 positions [walker][3][np], double-single binary32 copies
+  // [walker][2 np] (float4 high and low parts of atom j at 2j and 2j + 1),
   // subcell of each atom, bucket counts [walker][cells], buckets [walker][cells][bucket]
   int system;            // 1 LJ cluster, 2 WCA fluid
   double* pos64;

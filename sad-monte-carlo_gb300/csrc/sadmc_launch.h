@@ -62,7 +62,8 @@ cudaError_t launch_ising_energy(const IsingSys& s, int n_walkers, double* out, c
 // one-bucket-per-atom subcell grid.
 struct CellSys {
   double* pos;        // [walker][3][np] FP64 planes
-  float* pos32;       // [walker][np] float4 (x, y, z, 0) binary32 copy (pre-filters)
+  float* pos32;       // [walker][2 np] float4: WCA high/low parts of atom j at 2j, 2j + 1;
+                      // square well high parts at j
   int np;
   double* box;        // [walker][3]
   int* ncell;         // [walker][3] subcells per axis (>= 3)

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
     DS tx, ty, tz;
     float de = 0.0f;
     const bool possible = lj.plan((int)d.which, d.g0, d.g1, d.g2, sc.h, sc.l, s.radius2, tx, ty, tz, de);
-    if (m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
+    if (SADMC_RARE(m.trace && wr && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap)) {
       TraceRec r;
       r.e1 = fh.c.E;
       r.e2 = possible ? fh.c.E + (double)de : __longlong_as_double(0x7ff8000000000000ll);
@@ -106,8 +106,8 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
     const bool acc = fh.decide_de(possible, de, d.u53, rs);
     if (acc) lj.put((int)d.which, tx, ty, tz);
     fh.finish_move(acc);
-    if (fh.tscale_changed) { fh.tscale_changed = false; sc = ds_from_double(fh.c.tscale); }
-    if (resum.tick()) {
+    if (SADMC_RARE(fh.tscale_changed)) { fh.tscale_changed = false; sc = ds_from_double(fh.c.tscale); }
+    if (SADMC_RARE(resum.tick())) {
       const double e64 = lj.energy64();
       const double dr = fabs(e64 - fh.c.E);
       if (dr > fh.c.drift) fh.c.drift = dr;

@@ -16,6 +16,8 @@
 #pragma once
 #include <cstdint>
 
+#include "sadmc_types.h"
+
 namespace sadmc {
 namespace dev {
 
@@ -184,7 +186,7 @@ struct DrawCache {
   // called once per move with consecutive t
   __device__ Draws get(uint64_t seed, uint32_t walker, uint64_t t, uint32_t n, unsigned gmask,
                        int glane) {
-    if (off >= (uint32_t)LPW) {
+    if (SADMC_RARE(off >= (uint32_t)LPW)) {
       off = 0;
       mine = ISING ? draws_ising(seed, walker, t + (uint64_t)glane, n)
                    : draws_continuous(seed, walker, t + (uint64_t)glane, n, 0u);

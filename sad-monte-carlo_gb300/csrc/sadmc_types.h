@@ -2,6 +2,9 @@
 #pragma once
 #include <cstdint>
 
+// A branch the per-move loops rarely take: its block is laid out away from the hot path.
+#define SADMC_RARE(x) __builtin_expect(!!(x), 0)
+
 namespace sadmc {
 
 enum SystemKind : int32_t { SYS_ISING = 0, SYS_LJ = 1, SYS_WCA = 2, SYS_SW = 3 };

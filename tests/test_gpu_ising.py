@@ -29,8 +29,11 @@ def run_pair(gpu, oracle, L, W, moves, method, seed=17, lpw=0, chunks=1):
 
 
 @pytest.mark.parametrize("method", ["sad", "wl", "inv_t_wl", "samc", "canonical"])
-def test_ising_batch_bit_exact(gpu, oracle, method):
-    b, ws = run_pair(gpu, oracle, L=8, W=40, moves=30000, method=method, chunks=3)
+@pytest.mark.parametrize("lpw", [0, 32])
+def test_ising_batch_bit_exact(gpu, oracle, method, lpw):
+    """lpw 32: one walker per warp with its bins and spins staged in shared memory for each
+    of the three launches."""
+    b, ws = run_pair(gpu, oracle, L=8, W=40, moves=30000, method=method, chunks=3, lpw=lpw)
     for w in range(b.W):
         label = f"{method} walker {w}"
         assert_bins_equal(b.bins(w), ws[w].bins(), label=label)
@@ -50,6 +53,15 @@ def test_ising_single_walker_32x32(gpu, oracle):
     b, ws = run_pair(gpu, oracle, L=32, W=1, moves=200000, method="sad", lpw=32)
     assert_bins_equal(b.bins(0), ws[0].bins(), label="L32")
     assert_scalars_equal(b.scalars(0), ws[0].scalars(), label="L32")
+    np.testing.assert_array_equal(b.state(0), ws[0].state())
+
+
+def test_ising_single_walker_unstaged(gpu, oracle):
+    """64x64: the bins and spins (about 266 KB) exceed the shared-memory stage, so the
+    lone walker runs on its planes in global memory."""
+    b, ws = run_pair(gpu, oracle, L=64, W=1, moves=60000, method="sad", lpw=32, chunks=2)
+    assert_bins_equal(b.bins(0), ws[0].bins(), label="L64")
+    assert_scalars_equal(b.scalars(0), ws[0].scalars(), label="L64")
     np.testing.assert_array_equal(b.state(0), ws[0].state())
 
 
