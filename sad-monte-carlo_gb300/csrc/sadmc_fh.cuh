@@ -134,8 +134,8 @@ struct Fh {
   int win_lo, win_hi;  // SAD window as bin indices
   // gamma batch (see gamma())
   double gb_val[4];
-  uint32_t gb_off;  // moves since the batch was taken
-  bool gb_valid;
+  uint32_t gb_base;  // low 32 bits of the move count the batch starts at
+  uint32_t gb_ok;    // bit q: gb_val[q] holds gamma for the current parameters
   // per-move scratch
   double e1;
   int i2;
@@ -242,7 +242,8 @@ struct Fh {
       cur = -1;
     }
     inverted = c.too_lo > c.too_hi;
-    gb_valid = false;
+    gb_ok = 0;
+    gb_base = ~0u;
     grew_front = false;
     tscale_changed = false;
     // binary32 shadows of decide_de (each within |x| 2^-23 of its FP64 value)
@@ -280,21 +281,42 @@ struct Fh {
       default: return 0.0;
     }
   }
-  // gamma(batch start + glane + LPW*q) sits in gb_val[q]; four independent divide chains per
-  // lane hide the FP64 divide latency and cover 4*LPW moves per evaluation.
+  // gamma(base + glane + LPW*q) sits in gb_val[q], base = the move count rounded down to a
+  // multiple of 4*LPW: four independent divide chains per lane hide the FP64 divide
+  // latency and cover 4*LPW moves.  The walkers of a launch share the move count, so the
+  // lane groups of a warp take their full refreshes at the same moves (one instruction
+  // stream).  A change of the SAD parameters mid-batch (gb_ok = 0) refreshes only the
+  // slot of the current move, one chain per lane for the next LPW moves.  (The low 32
+  // bits of the count suffice: a batch is replaced at least every 4*LPW moves.)
   __device__ double gamma() {
     if (kind() != M_SAD && kind() != M_SAMC) return gamma_at(c.moves);
-    if (SADMC_RARE(!gb_valid || gb_off >= (uint32_t)(4 * LPW))) {
-      gb_off = 0;
+    constexpr uint32_t SPAN = 4 * LPW;
+    const uint32_t m32 = (uint32_t)c.moves;
+    const uint32_t base = m32 & ~(SPAN - 1);
+    const int off = (int)(m32 - base);
+    const int qc = off / LPW;
+    if (base != gb_base) {
+      gb_base = base;
+      gb_ok = 0;
+    }
+    if (SADMC_RARE(!((gb_ok >> qc) & 1u))) {
       if (kind() == M_SAD) {
         if (c.tF != inv_tF_of) { inv_tF = 1.0 / (double)c.tF; inv_tF_of = c.tF; }
         if (c.num_states != inv_ns_of) { inv_ns = 1.0 / (double)c.num_states; inv_ns_of = c.num_states; }
       }
+      const uint64_t t0 = c.moves - (uint64_t)off;
+      if (off == 0) {  // the batch boundary: every slot
 #pragma unroll
-      for (int q = 0; q < 4; ++q) gb_val[q] = gamma_at(c.moves + (uint64_t)(glane + LPW * q));
-      gb_valid = true;
+        for (int q = 0; q < 4; ++q) gb_val[q] = gamma_at(t0 + (uint64_t)(glane + LPW * q));
+        gb_ok = 0xfu;
+      } else {
+        const double v = gamma_at(t0 + (uint64_t)(glane + LPW * qc));
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (q == qc) gb_val[q] = v;
+        gb_ok |= 1u << qc;
+      }
     }
-    const int off = (int)gb_off++;  // gamma() runs once per move
     const int q = off / LPW;
     double v = q == 0 ? gb_val[0] : q == 1 ? gb_val[1] : q == 2 ? gb_val[2] : gb_val[3];
     if (LPW == 1) return v;
@@ -471,7 +493,7 @@ struct Fh {
             c.latest_param = (c.too_hi - c.too_lo) / c.min_T;
             c.num_states += 1;
             c.tL = c.moves;
-            gb_valid = false;
+            gb_ok = 0;
           }
         }
         break;
@@ -561,7 +583,7 @@ struct Fh {
           if (t > c.win_tmax) c.win_tmax = t;
         }
         win_hi = nhi;
-        gb_valid = false;
+        gb_ok = 0;
       } else if (e_below) {
         const double base = ld_lnw(win_lo);
         const int jlo = cur > c.b_lo ? cur : c.b_lo;
@@ -589,13 +611,13 @@ struct Fh {
           if (t > c.win_tmax) c.win_tmax = t;
         }
         win_lo = nlo;
-        gb_valid = false;
+        gb_ok = 0;
       }
     }
     if (SADMC_RARE(c.tL == c.moves)) {
       uint64_t old_tF = c.tF;
       c.tF = c.win_tmax;
-      gb_valid = false;
+      gb_ok = 0;
       if (old_tF != c.tF && acc_mode) {  // energy.rs:600-609
         double s = c.acc_rate / target_rate;
         s = s < 0.8 ? 0.8 : (s > 1.2 ? 1.2 : s);
@@ -689,7 +711,7 @@ struct Fh {
       if (inv_t && c.gamma < c.wl_num_states / (double)c.moves) {  // energy.rs:747-750
         c.kind = M_SAMC;
         c.t0 = c.wl_num_states;
-        gb_valid = false;
+        gb_ok = 0;
       }
     }
   }

@@ -90,7 +90,7 @@ def test_wca_pressure_channel(gpu, oracle, lpw):
                                               translation_scale=0.1, seed=seed, walker=w,
                                               e0=float(E0[w])), pos)
         disc, mismatch = ow.run_override(e1, e2)
-        assert mismatch == 0 and disc < 2e-5, (w, mismatch, disc, ow.override_worst())
+        assert mismatch == 0 and disc < 5e-6, (w, mismatch, disc, ow.override_worst())
         gc, gt = b.extra(w)
         oc, ot = ow.extra()
         assert int(gc.sum()) == moves // (n * n), (w, gc.sum())
@@ -131,7 +131,8 @@ def test_wca_uneven_trace_replay(gpu, oracle, lpw):
                                               e0=float(E0[w])), pos)
         disc, mismatch = ow.run_override(e1, e2)
         assert mismatch == 0, (w, mismatch)
-        assert disc < 2e-5, (w, disc)
+        # double-single pair differences: measured gaps about 1.4e-6 of the gross magnitude
+        assert disc < 5e-6, (w, disc)
         label = f"wca lpw{lpw} walker {w}"
         assert_bins_equal(b.bins(w), ow.bins(), label=label)
         assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
