@@ -375,13 +375,18 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def profile_traffic():
-    """DRAM bytes per move-kernel launch from the committed ncu summary, if present."""
+def profile_value(key):
+    """A figure (`key: value` line) of the committed ncu summary of the move kernel."""
     path = os.path.join(REPO, "profiles", "lj_move_kernel_lj31_4096w.md")
     if not os.path.exists(path):
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    m = re.search(key + r":\s*([0-9.eE+]+)", open(path).read())
     return float(m.group(1)) if m else None
+
+
+def profile_traffic():
+    """DRAM bytes per move-kernel launch from the committed ncu summary, if present."""
+    return profile_value("traffic_bytes_per_launch")
 
 
 def peaks():
@@ -564,9 +569,13 @@ def run_gpu(args):
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak,
                          "unit": "TFLOP/s", "frac": achieved_tflops / fp32_peak,
                          "traffic": traffic,
+                         "limiter": {"fp64_pipe_active": profile_value("fp64_pipe_active_frac"),
+                                     "issue_active": profile_value("issue_active_frac"),
+                                     "source": "ncu, profiles/lj_move_kernel_lj31_4096w.md"},
                          "note": "30(N-1) FLOP/move algorithmic; peak = 152 SM x 128 FFMA x 2 x "
                                  "max SM clock (FP32 issue, not in MEASURED_PEAKS.json); the "
-                                 "kernel is bound by the FP64 pipe and the latency of the per-move bookkeeping"},
+                                 "kernel is bound by the FP64 pipe and the latency of the per-move "
+                                 "bookkeeping (limiter: fractions of peak from ncu)"},
             "launch_ms": launch_ms,
             "clocks": clk,
             "gpu_launches": args.steps * launches_per_step,

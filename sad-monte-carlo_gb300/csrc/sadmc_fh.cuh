@@ -286,7 +286,8 @@ struct Fh {
   // latency and cover 4*LPW moves.  The walkers of a launch share the move count, so the
   // lane groups of a warp take their full refreshes at the same moves (one instruction
   // stream).  A change of the SAD parameters mid-batch (gb_ok = 0) refreshes only the
-  // slot of the current move, one chain per lane for the next LPW moves.  (The low 32
+  // slot of the current move, one chain per lane for the next LPW moves, where other
+  // walkers share the warp.  (The low 32
   // bits of the count suffice: a batch is replaced at least every 4*LPW moves.)
   __device__ double gamma() {
     if (kind() != M_SAD && kind() != M_SAMC) return gamma_at(c.moves);
@@ -305,9 +306,12 @@ struct Fh {
         if (c.num_states != inv_ns_of) { inv_ns = 1.0 / (double)c.num_states; inv_ns_of = c.num_states; }
       }
       const uint64_t t0 = c.moves - (uint64_t)off;
-      if (off == 0) {  // the batch boundary: every slot
+      if (off == 0 || LPW == 32) {
+        // the batch boundary, or a warp that holds one walker (its chains run in parallel,
+        // so the remaining slots cost no more latency than one): every slot still ahead
 #pragma unroll
-        for (int q = 0; q < 4; ++q) gb_val[q] = gamma_at(t0 + (uint64_t)(glane + LPW * q));
+        for (int q = 0; q < 4; ++q)
+          if (q >= qc) gb_val[q] = gamma_at(t0 + (uint64_t)(glane + LPW * q));
         gb_ok = 0xfu;
       } else {
         const double v = gamma_at(t0 + (uint64_t)(glane + LPW * qc));
