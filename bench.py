@@ -127,6 +127,26 @@ def c5_inputs(seed=11, walkers=1024):
     return out
 
 
+# Peaks for the roofline of the other workloads: FP32 FFMA issue (152 SMs x 128 lanes x
+# 2 FLOP x max SM clock), FP64 from the DFMA throughput probe (0.052 warp instructions per
+# clock per SM: 152 x 0.052 x 32 lanes x 2 FLOP x clock), one SM's shared-memory port
+# (128 B per clock).
+SM_HZ = 2.07e9
+FP32_PEAK = 152 * 128 * 2 * SM_HZ
+FP64_PEAK = 152 * 0.052 * 32 * 2 * SM_HZ
+SMEM_SM_PEAK = 128 * SM_HZ
+
+
+def _roof(achieved, peak, unit, note):
+    return {"achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak, "note": note}
+
+
+def candidates(n, L, r_cut):
+    """C = 27 N / n_c^3 - 1 candidate partners of a query, n_c = floor(L / r_cut)."""
+    nc = np.floor(np.asarray(L) / r_cut)
+    return 27.0 * np.asarray(n) / nc ** 3 - 1.0
+
+
 C3_METHOD = dict(t0=1e4, energy_bin=1.0, max_allowed=500.0, translation_scale=0.1)
 C5_METHOD = dict(well_width=1.3, translation_scale=0.05)
 
@@ -142,9 +162,12 @@ def case_c1(G, seed=11, moves=1_000_000, lpw=0, **_):
     lanes = _lanes(b, lpw, 20000)
     sec = _time_run(b, moves, 100_000)
     b.close()
+    rate = moves / sec
     return {"workload": "Ising 32x32, plain SAD (min_T 0.2), 1 walker", "moves": moves,
-            "moves_per_s": moves / sec, "ns_per_move": 1e9 * sec / moves,
-            "lanes_per_walker": lanes}
+            "moves_per_s": rate, "ns_per_move": 1e9 * sec / moves, "lanes_per_walker": lanes,
+            "roofline": _roof(48 * rate / 1e9, SMEM_SM_PEAK / 1e9, "GB/s",
+                              "48 B of shared-memory traffic per move against one SM's "
+                              "port; not meaningful for one serial walker")}
 
 
 def case_c1_batch(G, seed=11, walkers=4096, moves=20000, lpw=0):
@@ -178,10 +201,15 @@ def case_c3(G, seed=11, walkers=2048, moves=2048, lpw=0):
     lanes = _lanes(b, lpw, 256)
     sec = _time_run(b, moves, 512)
     b.close()
+    rate = walkers * moves / sec
+    flop = float(np.mean(2 * 15 * candidates([n for n, _, _ in inp], [Lb for _, Lb, _ in inp],
+                                              2 ** (1 / 6))))
     return {"workload": f"WCA, N in {{64,128,256,512}}, density U[0.6,0.9], {walkers} walkers, "
                         "SAMC t0=1e4, 500 bins over [0,500)",
-            "moves": walkers * moves, "moves_per_s": walkers * moves / sec,
-            "lanes_per_walker": lanes}
+            "moves": walkers * moves, "moves_per_s": rate, "lanes_per_walker": lanes,
+            "roofline": _roof(rate * flop / 1e12, FP32_PEAK / 1e12, "TFLOP/s",
+                              f"2 C x 15 FP32 FLOP per move, C = 27 N / n_c^3 - 1 per walker "
+                              f"(mean {flop:.0f} FLOP)")}
 
 
 def case_c5(G, seed=11, walkers=1024, moves=2048, lpw=0):
@@ -196,10 +224,15 @@ def case_c5(G, seed=11, walkers=1024, moves=2048, lpw=0):
     lanes = _lanes(b, lpw, 256)
     sec = _time_run(b, moves, 512)
     b.close()
+    rate = walkers * moves / sec
+    flop = float(np.mean(2 * 8 * candidates(1024, [Lb for Lb, _ in inp], 1.3)))
     return {"workload": f"hard-core square well lambda=1.3, N=1024, packing U[0.30,0.50], "
                         f"jittered FCC, WL on contact bins, {walkers} walkers",
-            "moves": walkers * moves, "moves_per_s": walkers * moves / sec,
-            "lanes_per_walker": lanes}
+            "moves": walkers * moves, "moves_per_s": rate, "lanes_per_walker": lanes,
+            "roofline": _roof(rate * flop / 1e12, FP64_PEAK / 1e12, "TFLOP/s",
+                              f"2 C x 8 FP64 FLOP per move (C = 27 N / n_c^3 - 1, mean {flop:.0f} "
+                              "FLOP) against the FP64 peak; the kernel decides most pairs with "
+                              "binary32 screens, so this counts the reference's work")}
 
 
 def case_grand(G, seed=11, walkers=4096, moves=4096, lpw=0):
@@ -315,7 +348,12 @@ def da_compare(G, rank=0, walkers=8192, moves=2048):
             "da_moves_per_s": (m2 - m1) / da_s, "da_accepted_per_s": (a2 - a1) / da_s,
             "da_vs_plain": ((m2 - m1) / da_s) / ((m1 - m0) / plain_s),
             "screened_fraction": screened, "surrogate_rmse": float(np.sqrt(loss)),
-            "train_s": train_s}
+            "train_s": train_s,
+            "roofline": _roof((m2 - m1) / da_s * 2 * n * 6208 / 1e12,
+                              float(peaks().get("bf16_tflops", 1900.0)), "TFLOP/s",
+                              f"stage 1: the MLP on all {n} descriptor rows, 2 x 6208 BF16 FLOP "
+                              "per row, against the measured bf16 peak (mma.sync m16n8k16, one "
+                              "walker per warp)")}
 
 
 def make_batch(G, n_walkers, seed=1, lpw=0):
