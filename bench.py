@@ -253,8 +253,14 @@ def case_grand(G, seed=11, walkers=4096, moves=4096, lpw=0):
     return out
 
 
+def case_da(G, seed=11, walkers=8192, moves=2048, **_):
+    """C4 shape: the plain and delayed-acceptance arms of da_compare, alone."""
+    return da_compare(G, 0, walkers, moves)
+
+
 CASES = {"C1": case_c1, "C1_batch": case_c1_batch, "C3": case_c3, "C5": case_c5,
          "grand": case_grand}
+ONLY = dict(CASES, DA=case_da)
 
 
 def cpu_cases(seed=11):
@@ -639,7 +645,7 @@ def run_case(args):
         kw["walkers"] = args.walkers
     if args.moves:
         kw["moves"] = args.moves
-    out = CASES[args.only](G, **kw)
+    out = ONLY[args.only](G, **kw)
     print(json.dumps({"case": args.only, **out}))
 
 
@@ -658,7 +664,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-da", action="store_true", help="skip the delayed-acceptance comparison")
     ap.add_argument("--no-other", action="store_true", help="skip the C1/C3/C5 measurements")
-    ap.add_argument("--only", choices=sorted(CASES),
+    ap.add_argument("--only", choices=sorted(ONLY),
                     help="time one other workload alone (with --walkers, --moves, --lpw) and "
                          "print its line; for profiling a small case")
     args = ap.parse_args()

@@ -1219,6 +1219,11 @@ int32_t sadmc_surrogate_train(sadmc_handle* h, int32_t steps, int32_t batch, flo
   double l = 0;
   CUDA_TRY(cudaMemcpyAsync(&l, h->sg_loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
+  {
+    unsigned int to = 0;
+    CUDA_TRY(sg_forward_timeouts(&to, h->stream));
+    if (to) return fail(SADMC_ERR_CUDA, "a tensor-core wait of the surrogate forward ran out");
+  }
   if (loss) *loss = l;
   return SADMC_OK;
 }
@@ -1238,6 +1243,11 @@ int32_t sadmc_surrogate_loss_grads(sadmc_handle* h, const float* pos, const floa
   CUDA_TRY(cudaMemcpyAsync(&l, h->sg_loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (grads) CUDA_TRY(cudaMemcpyAsync(grads, h->sg_grad, sizeof(float) * SG_NPARAM, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
+  {
+    unsigned int to = 0;
+    CUDA_TRY(sg_forward_timeouts(&to, h->stream));
+    if (to) return fail(SADMC_ERR_CUDA, "a tensor-core wait of the surrogate forward ran out");
+  }
   if (loss) *loss = l;
   return SADMC_OK;
 }
@@ -1299,6 +1309,11 @@ int32_t sadmc_surrogate_predict(sadmc_handle* h, const float* pos, int32_t confi
   std::vector<float> e(rows);
   CUDA_TRY(cudaMemcpyAsync(e.data(), sc.e, sizeof(float) * rows, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
+  {
+    unsigned int to = 0;
+    CUDA_TRY(sg_forward_timeouts(&to, h->stream));
+    if (to) return fail(SADMC_ERR_CUDA, "a tensor-core wait of the surrogate forward ran out");
+  }
   for (int c = 0; c < configs; ++c) {
     double s = 0;
     for (int i = 0; i < n; ++i) s += e[(size_t)c * n + i];

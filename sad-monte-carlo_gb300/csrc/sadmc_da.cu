@@ -7,9 +7,11 @@
 //   The descriptors change incrementally: atom i != a gains phi(|r_i - to|) - phi(|r_i - from|),
 //   the moved atom's row is rebuilt from the new distances; the MLP runs on all rows on the
 //   tensor cores.
-// Stage 2: the exact binary32 pair energy e2 (as in lj_move_kernel) decides with
-//   min(1, exp(ln w(E~) - ln w(e2))) through the shared flat-histogram bookkeeping, so the
-//   exact energy makes every final decision and, for a fixed ln w, detailed balance holds.
+// Stage 2: the exact binary32 pair energy e2 (as in lj_move_kernel) decides with the
+//   Christen-Fox ratio min(1, [pi(y) a1(y,x)] / [pi(x) a1(x,y)]), where the reverse
+//   screen a1(y,x) uses e2 - dS (the first stage's approximation depends on the state it
+//   starts from), through the shared flat-histogram bookkeeping: the exact energy makes
+//   every final decision and, for a fixed ln w, detailed balance holds.
 // A stage-1 rejection is a rejected move (it is histogrammed like any other).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -184,7 +186,20 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
       DS ux, uy, uz;
       float de = 0.f;
       const bool possible = lj.plan(a, d.g0, d.g1, d.g2, sc.h, sc.l, s.radius2, ux, uy, uz, de);
-      acc = fh.decide_de(possible, de, u_second, rs, true, lnw_til);
+      // Christen-Fox second stage for a state-dependent first stage: accept with
+      // min(1, [pi(y) a1(y,x)] / [pi(x) a1(x,y)]), pi = exp(-ln w(E)), where the first stage
+      // from x used E~ = E + dS and the reverse one from y would use e2 - dS:
+      //   ln a1(x,y) = min(0, ln w(E) - ln w(E~)),  ln a1(y,x) = min(0, ln w(e2) - ln w(e2 - dS)).
+      // decide_de accepts with min(1, exp(lnw_first - ln w(e2))), so
+      //   lnw_first = ln w(E) - ln a1(x,y) + ln a1(y,x).
+      // (A constant surrogate, dS = 0, gives ln w(E): the plain chain.)
+      double lnw_first = lnw_cur;
+      if (possible && fabsf(de) <= 3.0e38f) {
+        const double e2x = fh.c.E + (double)de;
+        const double back = fh.lnw_at(e2x) - fh.lnw_at(e2x - (double)des);
+        lnw_first = lnw_cur - (uphill1 ? lnw_cur - lnw_til : 0.0) + (back < 0.0 ? back : 0.0);
+      }
+      acc = fh.decide_de(possible, de, u_second, rs, true, lnw_first);
       if (acc) {
         lj.put(a, tx, ty, tz);
         for (int q = 0; q < APL; ++q) {

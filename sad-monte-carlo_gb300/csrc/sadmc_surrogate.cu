@@ -6,9 +6,10 @@
 //
 //   descriptor  G[i,k] = sum_{j != i} exp(-(r_ij - c_k)^2 / (2 w^2)), c_k = 0.8 + 2.2 k/31,
 //               w = 0.1 (binary32)
-//   forward     tensor cores: mma.sync m16n8k16, bf16 operands (G, W1, h1, W2), FP32
-//               accumulation; layer 1's accumulator fragments are re-packed in registers
-//               as layer 2's A fragments; the last layer (64 -> 1) and the SiLUs in FP32
+//   forward     fifth-generation tensor cores (tcgen05.mma, BF16 operands in shared memory,
+//               FP32 accumulators in tensor memory), 128-row tiles; the last layer
+//               (64 -> 1) and the SiLUs in FP32.  The delayed-acceptance move kernel runs
+//               the same network per walker on mma.sync fragments (sadmc_mma.cuh).
 //   backward    FP32 per-row deltas, then weight gradients as row reductions
 //   update      Adam with bias correction on FP32 master weights; bf16 copies refreshed
 #include <cuda_bf16.h>
@@ -19,6 +20,7 @@
 #include "sadmc_common.cuh"
 #include "sadmc_mma.cuh"
 #include "sadmc_surrogate.h"
+#include "sadmc_tc05.cuh"
 
 namespace sadmc {
 namespace dev {
@@ -53,95 +55,135 @@ __global__ void descriptor_kernel(const float* pos, int n, int rows, __nv_bfloat
   }
 }
 
-// Forward pass for 16-row tiles, one warp per tile.  Weights come from shared memory.
-// Writes per-row energies and, for training, z1 and z2 (pre-activations).
-__global__ void __launch_bounds__(128) forward_kernel(const __nv_bfloat16* gq, int rows,
-                                                      SgWeights wts, float* e_out, float* z1_out,
-                                                      float* z2_out) {
-  __shared__ uint32_t sW1[SG_H1 * SG_RBF / 2];   // W1^T as bf16 pairs: [n][k/2]
-  __shared__ uint32_t sW2[SG_H2 * SG_H1 / 2];    // W2^T: [n][k/2]
+// Forward pass on the fifth-generation tensor cores: one CTA of 4 warps per 128-row tile.
+// G (128 x 32), W1^T (64 x 32), h1 (128 x 64) and W2^T (64 x 64) sit in shared memory as
+// BF16 core matrices (K-major, no swizzle); thread 0 issues the tcgen05 MMAs of each
+// layer (M = 128, N = 64, K = 16 per instruction) into FP32 accumulators in tensor
+// memory (layer 1 in columns 0-63, layer 2 in 64-127) and commits them to an mbarrier;
+// each warp reads its 32 rows back with tcgen05.ld for the bias, SiLU and, after layer 2,
+// the 64 -> 1 output in FP32.  Writes per-row energies and, for training, z1 and z2.
+// A wait that runs out (it never should) sets *timeout and writes NaN energies.
+__global__ void __launch_bounds__(128, 1) forward_tc_kernel(const __nv_bfloat16* gq, int rows,
+                                                            SgWeights wts, float* e_out,
+                                                            float* z1_out, float* z2_out,
+                                                            unsigned int* timeout) {
+  constexpr int M = 128;
+  __shared__ __align__(1024) uint4 sA1[M * SG_RBF / 8];     // G tile, 4 core matrices along K
+  __shared__ __align__(1024) uint4 sB1[SG_H1 * SG_RBF / 8];  // W1^T
+  __shared__ __align__(1024) uint4 sA2[M * SG_H1 / 8];      // h1 tile, 8 core matrices along K
+  __shared__ __align__(1024) uint4 sB2[SG_H2 * SG_H1 / 8];  // W2^T
   __shared__ float sb1[SG_H1], sb2[SG_H2], sw3[SG_H2];
-  for (int k = threadIdx.x; k < SG_H1 * SG_RBF / 2; k += blockDim.x)
-    sW1[k] = reinterpret_cast<const uint32_t*>(wts.w1t)[k];
-  for (int k = threadIdx.x; k < SG_H2 * SG_H1 / 2; k += blockDim.x)
-    sW2[k] = reinterpret_cast<const uint32_t*>(wts.w2t)[k];
-  for (int k = threadIdx.x; k < SG_H1; k += blockDim.x) { sb1[k] = wts.b1[k]; sb2[k] = wts.b2[k]; sw3[k] = wts.w3[k]; }
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tbase;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row0 = blockIdx.x * M;
+  unsigned char* a1 = reinterpret_cast<unsigned char*>(sA1);
+  unsigned char* b1 = reinterpret_cast<unsigned char*>(sB1);
+  unsigned char* a2 = reinterpret_cast<unsigned char*>(sA2);
+  unsigned char* b2 = reinterpret_cast<unsigned char*>(sB2);
+  // operands into shared memory, 16-byte chunks = one core-matrix row
+  const uint4* G = reinterpret_cast<const uint4*>(gq);
+  for (int c = tid; c < M * (SG_RBF / 8); c += 128) {
+    const int r = c / (SG_RBF / 8), kg = c % (SG_RBF / 8);
+    const uint4 v = row0 + r < rows ? G[(size_t)(row0 + r) * (SG_RBF / 8) + kg] : make_uint4(0, 0, 0, 0);
+    *reinterpret_cast<uint4*>(a1 + tc05::core_offset(r, kg, SG_RBF / 8)) = v;
+  }
+  const uint4* W1 = reinterpret_cast<const uint4*>(wts.w1t);
+  for (int c = tid; c < SG_H1 * (SG_RBF / 8); c += 128) {
+    const int n = c / (SG_RBF / 8), kg = c % (SG_RBF / 8);
+    *reinterpret_cast<uint4*>(b1 + tc05::core_offset(n, kg, SG_RBF / 8)) = W1[c];
+  }
+  const uint4* W2 = reinterpret_cast<const uint4*>(wts.w2t);
+  for (int c = tid; c < SG_H2 * (SG_H1 / 8); c += 128) {
+    const int n = c / (SG_H1 / 8), kg = c % (SG_H1 / 8);
+    *reinterpret_cast<uint4*>(b2 + tc05::core_offset(n, kg, SG_H1 / 8)) = W2[c];
+  }
+  for (int k = tid; k < SG_H1; k += 128) { sb1[k] = wts.b1[k]; sb2[k] = wts.b2[k]; sw3[k] = wts.w3[k]; }
+  // 256 columns: the two 64-column accumulators with room to spare (two CTAs per SM)
+  if (warp == 0) tc05::tmem_alloc(&tbase, 256);
+  if (tid == 0) tc05::mbar_init(&mbar, 1);
+  tc05::fence_smem_async();
+  tc05::fence_before();
   __syncthreads();
-  const float b3 = wts.b3[0];
-  const int lane = threadIdx.x & 31;
-  const int tile = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int row0 = tile * 16;
-  if (row0 >= rows) return;
-  const int g = lane >> 2, t = lane & 3;
-  const int ra = row0 + g, rb = row0 + g + 8;
-  const bool va = ra < rows, vb = rb < rows;
-  // A fragments of G (16 x 32 = two k tiles)
-  uint32_t aG[2][4];
-  const uint32_t* G32 = reinterpret_cast<const uint32_t*>(gq);
+  tc05::fence_after();
+  const uint32_t tmem = tbase;
+  constexpr uint32_t idesc = tc05::idesc_bf16(M, SG_H1);
+  constexpr uint32_t kPolls = 1u << 24;
+  // layer 1: D1 = G W1 (two K = 16 steps, 2 core matrices = 256 bytes apart)
+  if (tid == 0) {
 #pragma unroll
-  for (int kt = 0; kt < 2; ++kt) {
-    aG[kt][0] = va ? G32[(size_t)ra * (SG_RBF / 2) + 8 * kt + t] : 0u;
-    aG[kt][1] = vb ? G32[(size_t)rb * (SG_RBF / 2) + 8 * kt + t] : 0u;
-    aG[kt][2] = va ? G32[(size_t)ra * (SG_RBF / 2) + 8 * kt + 4 + t] : 0u;
-    aG[kt][3] = vb ? G32[(size_t)rb * (SG_RBF / 2) + 8 * kt + 4 + t] : 0u;
+    for (int ks = 0; ks < SG_RBF / 16; ++ks)
+      tc05::mma_bf16(tmem, tc05::sdesc(tc05::smem_u32(a1) + 256 * ks, 128, 128 * (SG_RBF / 8)),
+                     tc05::sdesc(tc05::smem_u32(b1) + 256 * ks, 128, 128 * (SG_RBF / 8)), idesc, ks > 0);
+    tc05::commit(&mbar);
   }
-  // layer 1: 8 n tiles of 8
-  float h1[8][4];
+  bool ok = tc05::mbar_wait(&mbar, 0, kPolls);
+  tc05::fence_after();
+  const int r = warp * 32 + lane;  // this thread's row of the tile
+  const uint32_t lane_addr = (uint32_t)(warp * 32) << 16;
+  if (ok) {
+    // bias and SiLU of layer 1, h1 into shared memory as the layer-2 A operand
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int half = 0; half < 2; ++half) {
+      float acc[32];
+      tc05::ld32(tmem + lane_addr + 32 * half, acc);
 #pragma unroll
-    for (int kt = 0; kt < 2; ++kt) {
-      const int n = 8 * j + g;
-      mma16816(c, aG[kt], sW1[n * (SG_RBF / 2) + 8 * kt + t], sW1[n * (SG_RBF / 2) + 8 * kt + 4 + t]);
+      for (int q = 0; q < 4; ++q) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = 32 * half + 8 * q + 2 * u;
+          const float z0 = acc[8 * q + 2 * u] + sb1[j], zz1 = acc[8 * q + 2 * u + 1] + sb1[j + 1];
+          if (z1_out && row0 + r < rows) {
+            z1_out[(size_t)(row0 + r) * SG_H1 + j] = z0;
+            z1_out[(size_t)(row0 + r) * SG_H1 + j + 1] = zz1;
+          }
+          pk[u] = pack_bf16(silu32(z0), silu32(zz1));
+        }
+        *reinterpret_cast<uint4*>(a2 + tc05::core_offset(r, 4 * half + q, SG_H1 / 8)) =
+            make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
     }
-    const float bb0 = sb1[8 * j + 2 * t], bb1 = sb1[8 * j + 2 * t + 1];
-    const float z[4] = {c[0] + bb0, c[1] + bb1, c[2] + bb0, c[3] + bb1};
-    if (z1_out) {
-      if (va) { z1_out[(size_t)ra * SG_H1 + 8 * j + 2 * t] = z[0]; z1_out[(size_t)ra * SG_H1 + 8 * j + 2 * t + 1] = z[1]; }
-      if (vb) { z1_out[(size_t)rb * SG_H1 + 8 * j + 2 * t] = z[2]; z1_out[(size_t)rb * SG_H1 + 8 * j + 2 * t + 1] = z[3]; }
+  }
+  tc05::fence_smem_async();
+  tc05::fence_before();
+  __syncthreads();
+  tc05::fence_after();
+  // layer 2: D2 = h1 W2 (four K = 16 steps) into columns 64-127
+  if (tid == 0 && ok) {
+#pragma unroll
+    for (int ks = 0; ks < SG_H1 / 16; ++ks)
+      tc05::mma_bf16(tmem + SG_H1, tc05::sdesc(tc05::smem_u32(a2) + 256 * ks, 128, 128 * (SG_H1 / 8)),
+                     tc05::sdesc(tc05::smem_u32(b2) + 256 * ks, 128, 128 * (SG_H1 / 8)), idesc, ks > 0);
+    tc05::commit(&mbar);
+  }
+  // every thread saw the same layer-1 outcome only if the CTA agrees on it
+  ok = __syncthreads_and(ok);
+  if (ok) ok = tc05::mbar_wait(&mbar, 1, kPolls);
+  tc05::fence_after();
+  float e = 0.f;
+  if (ok) {
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float acc[32];
+      tc05::ld32(tmem + lane_addr + SG_H1 + 32 * half, acc);
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int j = 32 * half + q;
+        const float z = acc[q] + sb2[j];
+        if (z2_out && row0 + r < rows) z2_out[(size_t)(row0 + r) * SG_H2 + j] = z;
+        e += silu32(z) * sw3[j];
+      }
     }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) h1[j][q] = silu32(z[q]);
+    e += wts.b3[0];
+  } else {
+    e = __int_as_float(0x7fc00000);
+    if (tid == 0) atomicOr(timeout, 1u);
   }
-  // layer 2: A fragments from layer 1 accumulators (n tiles 2kt and 2kt+1 form k tile kt)
-  float h2[8][4];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    float c[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-      const uint32_t a[4] = {pack_bf16(h1[2 * kt][0], h1[2 * kt][1]), pack_bf16(h1[2 * kt][2], h1[2 * kt][3]),
-                             pack_bf16(h1[2 * kt + 1][0], h1[2 * kt + 1][1]),
-                             pack_bf16(h1[2 * kt + 1][2], h1[2 * kt + 1][3])};
-      const int n = 8 * j + g;
-      mma16816(c, a, sW2[n * (SG_H1 / 2) + 8 * kt + t], sW2[n * (SG_H1 / 2) + 8 * kt + 4 + t]);
-    }
-    const float bb0 = sb2[8 * j + 2 * t], bb1 = sb2[8 * j + 2 * t + 1];
-    const float z[4] = {c[0] + bb0, c[1] + bb1, c[2] + bb0, c[3] + bb1};
-    if (z2_out) {
-      if (va) { z2_out[(size_t)ra * SG_H2 + 8 * j + 2 * t] = z[0]; z2_out[(size_t)ra * SG_H2 + 8 * j + 2 * t + 1] = z[1]; }
-      if (vb) { z2_out[(size_t)rb * SG_H2 + 8 * j + 2 * t] = z[2]; z2_out[(size_t)rb * SG_H2 + 8 * j + 2 * t + 1] = z[3]; }
-    }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) h2[j][q] = silu32(z[q]);
-  }
-  // layer 3 (FP32): e = h2 . w3 + b3, reduced over the quad sharing a row
-  float ea = 0.f, eb = 0.f;
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const float w0 = sw3[8 * j + 2 * t], w1 = sw3[8 * j + 2 * t + 1];
-    ea += h2[j][0] * w0 + h2[j][1] * w1;
-    eb += h2[j][2] * w0 + h2[j][3] * w1;
-  }
-  ea += __shfl_xor_sync(0xffffffffu, ea, 1);
-  ea += __shfl_xor_sync(0xffffffffu, ea, 2);
-  eb += __shfl_xor_sync(0xffffffffu, eb, 1);
-  eb += __shfl_xor_sync(0xffffffffu, eb, 2);
-  if (t == 0) {
-    if (va) e_out[ra] = ea + b3;
-    if (vb) e_out[rb] = eb + b3;
-  }
+  if (row0 + r < rows) e_out[row0 + r] = e;
+  tc05::fence_before();
+  __syncthreads();
+  if (warp == 0) tc05::tmem_dealloc(tmem, 256);
 }
 
 // Per configuration: E_s = sum of its n row energies, residual against the target,
@@ -273,11 +315,29 @@ cudaError_t sg_descriptors(const float* pos, int n, int rows, __nv_bfloat16* gq,
   return cudaGetLastError();
 }
 
+namespace {
+// Set by forward_tc_kernel when a tensor-core wait ran out (its energies are NaN).
+__device__ unsigned int g_sg_tc_timeout;
+}  // namespace
+
 cudaError_t sg_forward(const __nv_bfloat16* gq, int rows, const SgWeights& w, float* e, float* z1,
                        float* z2, cudaStream_t st) {
-  const int tiles = (rows + 15) / 16;
-  dev::forward_kernel<<<(tiles + 3) / 4, 128, 0, st>>>(gq, rows, w, e, z1, z2);
+  unsigned int* flag = nullptr;
+  cudaError_t err = cudaGetSymbolAddress((void**)&flag, g_sg_tc_timeout);
+  if (err != cudaSuccess) return err;
+  dev::forward_tc_kernel<<<(rows + 127) / 128, 128, 0, st>>>(gq, rows, w, e, z1, z2, flag);
   return cudaGetLastError();
+}
+
+cudaError_t sg_forward_timeouts(unsigned int* count, cudaStream_t st) {
+  unsigned int zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbolAsync(count, g_sg_tc_timeout, sizeof(unsigned int), 0,
+                                            cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess && *count)
+    e = cudaMemcpyToSymbolAsync(g_sg_tc_timeout, &zero, sizeof(unsigned int), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
 }
 
 namespace {

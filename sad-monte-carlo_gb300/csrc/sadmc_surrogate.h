@@ -69,6 +69,9 @@ cudaError_t sg_descriptors(const float* pos, int n, int rows, __nv_bfloat16* gq,
                            cudaStream_t st);
 cudaError_t sg_forward(const __nv_bfloat16* gq, int rows, const SgWeights& w, float* e, float* z1,
                        float* z2, cudaStream_t st);
+// Tensor-core waits of sg_forward that ran out since the last call (then cleared);
+// synchronizes st.
+cudaError_t sg_forward_timeouts(unsigned int* count, cudaStream_t st);
 // One training step on `configs` configurations of n atoms (positions [configs][n][3],
 // binary32; target energies): loss into *loss_dev, gradients into grad; when step > 0
 // an Adam step with that step number updates the master weights and their bf16 copies.
