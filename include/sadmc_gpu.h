@@ -176,6 +176,10 @@ int32_t sadmc_status(sadmc_handle* h, uint32_t* per_walker_flags);
 int32_t sadmc_set_trace(sadmc_handle* h, uint64_t capacity);
 int32_t sadmc_read_trace(sadmc_handle* h, int32_t walker, double* e1, double* e2,
                          uint64_t* count);
+/* The surrogate energy change dS of each traced delayed-acceptance move (0 for plain
+ * moves); the proposed E of a move the first stage screened out is NaN.  No reference
+ * counterpart: replays sadmc_run_da's two-stage decisions through the FP64 oracle. */
+int32_t sadmc_read_trace_ds(sadmc_handle* h, int32_t walker, float* ds, uint64_t* count);
 
 /* Lanes per walker in use; sadmc_autotune times the candidates on a snapshot of the
  * batch (`moves` moves each), keeps the fastest and restores the snapshot. */

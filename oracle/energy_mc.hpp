@@ -111,6 +111,11 @@ struct EnergyMC {
   uint64_t override_base = 0;
   uint64_t override_mismatch = 0;
   double worst[4] = {0, 0, 0, 0};  // move, e2 given, e2 own, gross magnitude at the worst move
+  // Delayed-acceptance replay (with the overrides): da_ds[k] is the GPU surrogate's energy
+  // change dS of move k and da_u2(t) the second-stage uniform of move t; e2 is NaN when
+  // the first stage screened the move out (or it was impossible).
+  const float* da_ds = nullptr;
+  std::function<double(uint64_t)> da_u2;
 
   // EnergyMC::from_params, energy.rs:830-898 (descent loop at 840-851 uses the
   // descent stream with scale 0.05; at most `descent_limit` proposals).
@@ -230,13 +235,29 @@ struct EnergyMC {
     }
   }
 
-  bool reject_move(double e1, double e2, double u) {  // energy.rs:440-512
+  // ln w at energy e as the Metropolis test would read it, without growing the bins: the
+  // SAD extrapolations outside its window, 0 outside the allocated bins (a new bin's
+  // value).  The delayed-acceptance screen of the GPU kernel (Fh::lnw_at).
+  double lnw_at(double e) const {
+    if (method.kind == M_SAD) {
+      const double too_lo = method.too_lo, too_hi = method.too_hi;
+      if (e < too_lo) return bins.lnw[state_to_index(too_lo)] + (e - too_lo) / method.min_T;
+      if (e > too_hi) return bins.lnw[state_to_index(too_hi)];
+    }
+    if (e < bins.min || e >= bins.min + bins.width * (double)bins.lnw.size()) return 0.0;
+    return bins.lnw[state_to_index(e)];
+  }
+
+  // lnw1_given: the Metropolis test uses it in place of ln w(e1) (the second stage of a
+  // delayed-acceptance move).
+  bool reject_move(double e1, double e2, double u, const double* lnw1_given = nullptr) {  // energy.rs:440-512
     size_t i1 = state_to_index(e1), i2 = state_to_index(e2);
     switch (method.kind) {
       case M_SAD: {
         const double too_lo = method.too_lo, too_hi = method.too_hi, min_T = method.min_T;
         const auto& lnw = bins.lnw;
-        double lnw1 = e1 < too_lo ? lnw[state_to_index(too_lo)] + (e1 - too_lo) / min_T
+        double lnw1 = lnw1_given ? *lnw1_given
+                      : e1 < too_lo ? lnw[state_to_index(too_lo)] + (e1 - too_lo) / min_T
                       : e1 > too_hi ? lnw[state_to_index(too_hi)] : lnw[i1];
         double lnw2 = e2 < too_lo ? lnw[state_to_index(too_lo)] + (e2 - too_lo) / min_T
                       : e2 > too_hi ? lnw[state_to_index(too_hi)] : lnw[i2];
@@ -249,11 +270,11 @@ struct EnergyMC {
         return rejected;
       }
       case M_SAMC: {
-        double lnw1 = bins.lnw[i1], lnw2 = bins.lnw[i2];
+        double lnw1 = lnw1_given ? *lnw1_given : bins.lnw[i1], lnw2 = bins.lnw[i2];
         return lnw2 > lnw1 && u > std::exp(lnw1 - lnw2);
       }
       case M_WL: {
-        double lnw1 = bins.lnw[i1], lnw2 = bins.lnw[i2];
+        double lnw1 = lnw1_given ? *lnw1_given : bins.lnw[i1], lnw2 = bins.lnw[i2];
         bool rejected = lnw2 > lnw1 && u > std::exp(lnw1 - lnw2);
         if (!rejected && bins.histogram[i2] == 0 && method.lowest_hist > 0) method.wl_num_states += 1.0;
         return rejected;
@@ -403,7 +424,31 @@ struct EnergyMC {
     double recent_scale = std::sqrt(1.0 / (double)moves);
     acceptance_rate *= 1. - recent_scale;
     Draws d = draw(moves);
+    // delayed acceptance (sadmc_da.cu): stage 1 screens with E~ = E + dS
+    double lnw_first = 0.0;
+    bool use_first = false;
+    if (da_ds) {
+      const double ds = (double)da_ds[moves - 1 - override_base];
+      const double lnw_cur = lnw_at(e1), lnw_til = lnw_at(e1 + ds);
+      const bool uphill1 = lnw_til > lnw_cur;
+      if (uphill1 && d.u > std::exp(lnw_cur - lnw_til)) {  // screened out: a rejected move
+        if (e2_override[moves - 1 - override_base] == e2_override[moves - 1 - override_base])
+          ++override_mismatch;  // the GPU evaluated it
+        finish_move(e1);
+        return;
+      }
+      // stage 2 (Christen-Fox with the reverse screen from the proposed state); a certain
+      // first stage used no randomness, so the second reuses the move's uniform
+      const double ge2 = e2_override[moves - 1 - override_base];
+      if (ge2 == ge2) {
+        const double back = lnw_at(ge2) - lnw_at(ge2 - ds);
+        lnw_first = lnw_cur - (uphill1 ? lnw_cur - lnw_til : 0.0) + (back < 0.0 ? back : 0.0);
+        use_first = true;
+      }
+      if (uphill1) d.u = da_u2(moves);
+    }
     auto e2o = sys.plan_move(d, translation_scale);
+    if (da_ds && e2o && !use_first) ++override_mismatch;  // the GPU screened out or lost a possible move
     if (!e2o && e2_override && e2_override[moves - 1 - override_base] ==
                                    e2_override[moves - 1 - override_base])
       ++override_mismatch;
@@ -431,7 +476,7 @@ struct EnergyMC {
       if (has_min_allowed) oob = oob || (e2 < min_allowed && e2 < e1);
       if (!oob) {
         prepare_for_state(e2);
-        if (!reject_move(e1, e2, d.u)) {
+        if (!reject_move(e1, e2, d.u, use_first ? &lnw_first : nullptr)) {
           accepted_moves += 1;
           acceptance_rate += recent_scale;
           sys.confirm();
@@ -439,6 +484,12 @@ struct EnergyMC {
         }
       }
     }
+    finish_move(e1);
+  }
+
+  // The end of move_once (energy.rs:936-965): histogram, sums, extra data, update_weights
+  // and the max-entropy bookkeeping for the energy the move left.
+  void finish_move(double e1) {
     double energy = sys.energy();
     size_t i = state_to_index(energy);
     if (bins.histogram[i] == 0) bins.t_found[i] = moves;

@@ -61,6 +61,7 @@ def lib():
             "orc_destroy": (None, [P]),
             "orc_run": (None, [P, U64]),
             "orc_run_override": (D, [P, U64, P, P, P]),
+            "orc_run_override_da": (D, [P, U64, P, P, P, P]),
             "orc_energy": (D, [P]), "orc_compute_energy": (D, [P]),
             "orc_override_worst": (None, [P, P]),
             "orc_extra": (I64, [P, P, P]),
@@ -157,6 +158,16 @@ class Walker:
         e2 = np.ascontiguousarray(e2, dtype=np.float64)
         mm = ctypes.c_uint64(0)
         d = lib().orc_run_override(self.h, len(e2), _p(e1), _p(e2), ctypes.byref(mm))
+        return d, mm.value
+
+    def run_override_da(self, e1, e2, ds):
+        """Replay a traced delayed-acceptance run (e2 NaN where the first stage screened the
+        move out, ds the GPU surrogate's change); returns (max |e2 - own e2|, mismatches)."""
+        e1 = np.ascontiguousarray(e1, dtype=np.float64)
+        e2 = np.ascontiguousarray(e2, dtype=np.float64)
+        ds = np.ascontiguousarray(ds, dtype=np.float32)
+        mm = ctypes.c_uint64(0)
+        d = lib().orc_run_override_da(self.h, len(e2), _p(e1), _p(e2), _p(ds), ctypes.byref(mm))
         return d, mm.value
 
     def extra(self):

@@ -182,6 +182,35 @@ double orc_run_override(void* hv, uint64_t nmoves, const double* e1, const doubl
   });
 }
 
+// Replay of a traced delayed-acceptance run (sadmc_da.cu): as orc_run_override, with the
+// GPU surrogate's energy change ds[k] of each move; e2[k] is NaN for moves the first stage
+// screened out.  The oracle takes both stages' decisions itself from its own FP64 ln w.
+double orc_run_override_da(void* hv, uint64_t nmoves, const double* e1, const double* e2,
+                           const float* ds, uint64_t* mismatch) {
+  auto* h = (AnyMC*)hv;
+  const uint64_t seed = h->seed;
+  const uint32_t walker = h->walker;
+  return h->visit([&](auto& mc) {
+    mc.e1_override = e1;
+    mc.e2_override = e2;
+    mc.da_ds = ds;
+    mc.da_u2 = [seed, walker](uint64_t t) {  // counter word 2 = 4 of the move's counter
+      U4 U = philox4x32_10(U4{(uint32_t)t, (uint32_t)(t >> 32), 4u, (uint32_t)(seed >> 32)}, walker,
+                           (uint32_t)seed);
+      return u53(U.x, U.y);
+    };
+    mc.override_base = mc.moves;
+    mc.max_e2_discrepancy = 0.0;
+    mc.override_mismatch = 0;
+    for (uint64_t k = 0; k < nmoves; ++k) mc.move_once();
+    mc.e1_override = nullptr;
+    mc.e2_override = nullptr;
+    mc.da_ds = nullptr;
+    if (mismatch) *mismatch = mc.override_mismatch;
+    return mc.max_e2_discrepancy;
+  });
+}
+
 // The "pressure" BinCounts of the bins (empty unless the system collects it).
 int64_t orc_extra(void* hv, uint64_t* count, double* total) {
   return ((AnyMC*)hv)->visit([&](auto& mc) {

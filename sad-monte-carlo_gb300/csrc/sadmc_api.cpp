@@ -92,6 +92,7 @@ struct sadmc_handle {
   }
   double* d_tmp = nullptr;     // [W] + 2 scratch doubles
   TraceRec* d_trace = nullptr;
+  float* d_trace_ds = nullptr;  // dS of traced delayed-acceptance moves (0 for plain moves)
   uint64_t trace_cap = 0, trace_t0 = 0;
   uint64_t moves_done = 0;
   int pend_walker = -1;
@@ -220,6 +221,7 @@ struct sadmc_handle {
     m.trace = d_trace;
     m.trace_cap = trace_cap;
     m.trace_t0 = trace_t0;
+    m.trace_ds = d_trace_ds;
     m.resum_interval = resum();
     m.drift_tol = drift_tol();
     m.warps_per_block = wpb;
@@ -481,6 +483,7 @@ int32_t sadmc_destroy(sadmc_handle* h) {
   cudaFree(h->d_pos);
   cudaFree(h->d_spins);
   cudaFree(h->d_trace);
+  cudaFree(h->d_trace_ds);
   cudaFree(h->d_pos64); cudaFree(h->d_pos32); cudaFree(h->d_box); cudaFree(h->d_ncell);
   cudaFree(h->d_cell_of); cudaFree(h->d_cnt); cudaFree(h->d_atoms); cudaFree(h->d_build_status);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -930,12 +933,16 @@ int32_t sadmc_set_trace(sadmc_handle* h, uint64_t capacity) {
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
   h->drop_graphs();
   cudaFree(h->d_trace);
+  cudaFree(h->d_trace_ds);
   h->d_trace = nullptr;
+  h->d_trace_ds = nullptr;
   h->trace_cap = 0;
   if (capacity == 0) return SADMC_OK;
-  if (dalloc(&h->d_trace, (size_t)h->W * capacity) != cudaSuccess)
+  if (dalloc(&h->d_trace, (size_t)h->W * capacity) != cudaSuccess ||
+      dalloc(&h->d_trace_ds, (size_t)h->W * capacity) != cudaSuccess)
     return fail(SADMC_ERR_NOMEM, "trace allocation failed");
   CUDA_TRY(cudaMemsetAsync(h->d_trace, 0xff, sizeof(TraceRec) * (size_t)h->W * capacity, h->stream));
+  CUDA_TRY(cudaMemsetAsync(h->d_trace_ds, 0, sizeof(float) * (size_t)h->W * capacity, h->stream));
   h->trace_cap = capacity;
   h->trace_t0 = h->moves_done;
   return SADMC_OK;
@@ -955,6 +962,20 @@ int32_t sadmc_read_trace(sadmc_handle* h, int32_t walker, double* e1, double* e2
   for (uint64_t k = 0; k < n; ++k) {
     if (e1) e1[k] = r[k].e1;
     if (e2) e2[k] = r[k].e2;
+  }
+  if (count) *count = n;
+  return SADMC_OK;
+}
+
+int32_t sadmc_read_trace_ds(sadmc_handle* h, int32_t walker, float* ds, uint64_t* count) {
+  if (!h || walker < 0 || walker >= h->W) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->d_trace_ds) return fail(SADMC_ERR_STATE, "tracing disabled");
+  const uint64_t done = h->moves_done > h->trace_t0 ? h->moves_done - h->trace_t0 : 0;
+  const uint64_t n = std::min(done, h->trace_cap);
+  if (n && ds) {
+    CUDA_TRY(cudaMemcpyAsync(ds, h->d_trace_ds + (size_t)walker * h->trace_cap, n * sizeof(float),
+                             cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
   }
   if (count) *count = n;
   return SADMC_OK;
@@ -1282,8 +1303,7 @@ int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, 
     CUDA_TRY(cudaMalloc(&h->sg_stats, sizeof(uint64_t) * 2 * h->W));
     CUDA_TRY(cudaMemset(h->sg_stats, 0, sizeof(uint64_t) * 2 * h->W));
   }
-  MoveLaunch m = h->base_launch();
-  m.trace = nullptr;
+  MoveLaunch m = h->base_launch();  // traced like sadmc_run, with dS in the second record
   for (uint64_t left = moves; left > 0;) {
     m.n_moves = std::min<uint64_t>(left, 8192);
     CUDA_TRY(launch_lj_da(m, LjSys{h->d_pos, h->np, h->radius2()}, h->sg_weights(), refresh_interval,

@@ -169,7 +169,14 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
       if (i < n) part += sEn[i] - sE[i];
     }
     const float des = group_sum<32>(part, 0xffffffffu);
-    const double e_til = fh.c.E + (double)des;
+    const double e1 = fh.c.E;
+    const double e_til = e1 + (double)des;
+    if (m.trace && lane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
+      // (E before, proposed E: NaN when screened out or impossible) and dS
+      const size_t k = (size_t)w * m.trace_cap + (t - m.trace_t0 - 1);
+      m.trace[k] = TraceRec{e1, __longlong_as_double(0x7ff8000000000000ll)};
+      if (m.trace_ds) m.trace_ds[k] = des;
+    }
     const double lnw_cur = fh.lnw_current();
     const double lnw_til = fh.lnw_at(e_til);
     const bool uphill1 = dgt(lnw_til, lnw_cur);
@@ -199,6 +206,9 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
         const double back = fh.lnw_at(e2x) - fh.lnw_at(e2x - (double)des);
         lnw_first = lnw_cur - (uphill1 ? lnw_cur - lnw_til : 0.0) + (back < 0.0 ? back : 0.0);
       }
+      if (m.trace && lane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap)
+        m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)].e2 =
+            possible ? e1 + (double)de : __longlong_as_double(0x7ff8000000000000ll);
       acc = fh.decide_de(possible, de, u_second, rs, true, lnw_first);
       if (acc) {
         lj.put(a, tx, ty, tz);

@@ -18,6 +18,7 @@ struct MoveLaunch {
   TraceRec* trace;         // nullptr unless tracing
   uint64_t trace_cap;      // records per walker
   uint64_t trace_t0;       // move counter before the first traced move
+  float* trace_ds;         // with trace: the surrogate change dS of delayed-acceptance moves
   int resum_interval;      // FP64 re-sum period in moves (continuous systems), 0 = never
   double drift_tol;        // ST_DRIFT when |E_incremental - E_fp64| exceeds this
   int descent;             // 1: run the initial descent (energy.rs:840-851) instead

@@ -96,6 +96,7 @@ def lib():
         "sadmc_read_scalars": (I32, [P, I32, P]),
         "sadmc_counters": (I32, [P, P, P]), "sadmc_status": (I32, [P, P]),
         "sadmc_set_trace": (I32, [P, U64]), "sadmc_read_trace": (I32, [P, I32, P, P, P]),
+        "sadmc_read_trace_ds": (I32, [P, I32, P, P]),
         "sadmc_lanes_per_walker": (I32, [P]), "sadmc_autotune": (I32, [P, U64, P, P]),
         "sadmc_heat_capacity": (I32, [P, I32, P, P, I32, P]),
         "sadmc_checkpoint": (I32, [P, ctypes.c_char_p]),
@@ -317,6 +318,13 @@ class Batch:
         cnt = ctypes.c_uint64(0)
         _check(lib().sadmc_read_trace(self.h, w, _p(e1), _p(e2), ctypes.byref(cnt)))
         return e1[:cnt.value], e2[:cnt.value]
+
+    def trace_ds(self, w, capacity):
+        """dS of each traced delayed-acceptance move of walker w (0 for plain moves)."""
+        ds = np.zeros(capacity, np.float32)
+        cnt = ctypes.c_uint64(0)
+        _check(lib().sadmc_read_trace_ds(self.h, w, _p(ds), ctypes.byref(cnt)))
+        return ds[:cnt.value]
 
     def checkpoint(self, path):
         """Atomic binary checkpoint of the whole batch (write to path.tmp, rename)."""

@@ -6,7 +6,7 @@ before the exact evaluation while the sampled energies stay those of the plain c
 import numpy as np
 import pytest
 
-from helpers import BIN_KEYS, lj_configs
+from helpers import BIN_KEYS, assert_bins_equal, assert_scalars_equal, lj_configs
 
 pytestmark = pytest.mark.gpu
 
@@ -97,3 +97,46 @@ def test_trained_surrogate_keeps_the_distribution_at_fixed_weights(gpu, oracle, 
     pp = np.array([sum(h.get(k, 0) for h in hp) for k in keys], float)
     tv = 0.5 * np.abs(pd / pd.sum() - pp / pp.sum()).sum()
     assert tv < 0.05, tv
+
+
+@pytest.mark.parametrize("method", [0, 2])
+def test_da_trace_replay(gpu, oracle, method):
+    """A traced run (plain moves, surrogate training, then delayed-acceptance moves)
+    replayed by the FP64 oracle from the GPU's proposed energies and surrogate changes dS:
+    the oracle takes both stages' decisions itself (the screen from its own ln w, the
+    second stage with the reverse screen), so every screen, acceptance, bin and counter
+    must be the GPU's."""
+    n, W, R, seed, plain_moves, da_moves = 13, 8, 2.5, 6, 3000, 6000
+    confs = lj_configs(oracle, n, R, range(700, 700 + W))
+    kw = dict(method=method, min_T=0.1, energy_bin=0.1, max_allowed=0.0, target_rate=0.5,
+              translation_scale=0.1, seed=seed)
+    b = gpu.Batch(gpu.make_config(gpu.LJ, W, n, e_lo=-80, e_hi=1, lanes_per_walker=32, **kw),
+                  [(n, R, (0, 0, 0))] * W)
+    b.upload(confs)
+    b.initialize()
+    E0 = b.energies()
+    total = plain_moves + da_moves
+    b.set_trace(total)
+    b.surrogate_init(seed=2, ring_capacity=8192)
+    for _ in range(6):
+        b.run(plain_moves // 6)
+        b.surrogate_collect()
+    b.surrogate_train(200, batch=128, lr=2e-3, seed=4)
+    stats = b.run_da(da_moves)
+    screened = stats[:, 0].sum() / stats.sum()
+    assert 0.02 < screened < 0.95, screened
+    for w in range(W):
+        e1, e2 = b.trace(w, total)
+        ds = b.trace_ds(w, total)
+        assert len(e1) == total and len(ds) == total
+        assert not ds[:plain_moves].any()
+        ow = oracle.Walker(oracle.make_config(oracle.LJ, n, radius=R, walker=w, e0=float(E0[w]),
+                                              **kw), confs[w])
+        d1, m1 = ow.run_override(e1[:plain_moves], e2[:plain_moves])
+        d2, m2 = ow.run_override_da(e1[plain_moves:], e2[plain_moves:], ds[plain_moves:])
+        assert m1 == 0 and m2 == 0, (w, m1, m2)
+        assert max(d1, d2) < 2e-5, (w, d1, d2)
+        label = f"da method {method} walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
