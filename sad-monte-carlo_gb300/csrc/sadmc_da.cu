@@ -31,9 +31,12 @@ template <int APL>
 __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeights wts,
                                                     int refresh_interval, uint64_t* stats) {
   constexpr int NR = 32 * APL;  // descriptor rows (atoms, padded)
-  __shared__ float sG[NR][SG_RBF];                  // current descriptors (FP32)
-  __shared__ float sGf[NR][SG_RBF];                 // proposed descriptors (FP32)
-  __shared__ __nv_bfloat16 sGb[NR][SG_RBF];         // proposed descriptors (bf16, MLP input)
+  // Rows are padded by one 32-bit word so that the 32 lanes, each on its own row, hit 32
+  // different banks (the bf16 rows are 17 words: the MLP's fragment loads then meet at
+  // most 2-way conflicts).
+  __shared__ float sG[NR][SG_RBF + 1];              // current descriptors (FP32)
+  __shared__ float sGf[NR][SG_RBF + 1];             // proposed descriptors (FP32)
+  __shared__ __nv_bfloat16 sGb[NR][SG_RBF + 2];     // proposed descriptors (bf16, MLP input)
   __shared__ float sT[32][SG_RBF + 1];              // contributions to the moved atom's row
   __shared__ float sE[NR], sEn[NR];                 // per-atom surrogate energies
   __shared__ uint32_t sW1[SG_H1 * SG_RBF / 2], sW2[SG_H2 * SG_H1 / 2];
@@ -61,7 +64,8 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
   auto forward_rows = [&](float* dst) {
     for (int r0 = 0; r0 < n; r0 += 16) {
       float ea, eb;
-      mlp16(reinterpret_cast<const uint32_t*>(&sGb[r0][0]), sW1, sW2, sb1, sb2, sw3, b3, ea, eb);
+      mlp16<(SG_RBF + 2) / 2>(reinterpret_cast<const uint32_t*>(&sGb[r0][0]), sW1, sW2, sb1, sb2,
+                              sw3, b3, ea, eb);
       const int g = lane >> 2;
       if ((lane & 3) == 0) {
         if (r0 + g < NR) dst[r0 + g] = ea;

@@ -40,6 +40,7 @@ namespace dev {
 // in shared memory (32 bf16 = 16 words per row), weights in shared memory as in the
 // forward kernel.  Rows g and g+8 of the tile end in ea / eb (in the quad's lane t == 0
 // and the others alike).
+template <int RW>  // 32-bit words between consecutive rows of the tile
 __device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1,
                                       const uint32_t* sW2, const float* sb1, const float* sb2,
                                       const float* sw3, float b3, float& ea, float& eb) {
@@ -47,10 +48,10 @@ __device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1
   uint32_t aG[2][4];
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt) {
-    aG[kt][0] = gtile[g * 16 + 8 * kt + t];
-    aG[kt][1] = gtile[(g + 8) * 16 + 8 * kt + t];
-    aG[kt][2] = gtile[g * 16 + 8 * kt + 4 + t];
-    aG[kt][3] = gtile[(g + 8) * 16 + 8 * kt + 4 + t];
+    aG[kt][0] = gtile[g * RW + 8 * kt + t];
+    aG[kt][1] = gtile[(g + 8) * RW + 8 * kt + t];
+    aG[kt][2] = gtile[g * RW + 8 * kt + 4 + t];
+    aG[kt][3] = gtile[(g + 8) * RW + 8 * kt + 4 + t];
   }
   float h1[8][4];
 #pragma unroll
