@@ -30,6 +30,13 @@ def test_library_exports_every_declared_symbol():
     assert lib.sadmc_version() >= 1
 
 
+def test_rust_binding_covers_the_header():
+    """INTEGRATION.md's extern "C" blocks bind every declared entry point, and nothing else."""
+    text = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    bound = sorted(set(re.findall(r"pub fn (sadmc_\w+)\(", text)))
+    assert bound == declared_functions(), (set(declared_functions()) ^ set(bound))
+
+
 def test_no_oracle_in_product():
     """The product sources never include, link or load the oracle."""
     pkg = os.path.join(REPO, "sad-monte-carlo_gb300")
