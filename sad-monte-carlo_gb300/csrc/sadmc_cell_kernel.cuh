@@ -290,12 +290,23 @@ __global__ void __launch_bounds__(128, 1) cell_move_kernel(MoveLaunch m, CellSys
     int cn = 0, co = 0;
     bool overlap = false;
     float en = 0.0f, eo = 0.0f;
-    for (int k = glane; k < 54; k += LPW) {
-      if (k < 27)
+    if (KIND == SYS_SW) {
+      // the new position first: a hard-core overlap makes the move impossible, and then
+      // the old position's contacts are not needed
+      for (int k = glane; k < 27; k += LPW)
         CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, qt, a, wsqr, wsqr32, true, cn, overlap, en);
-      else
-        CellOps<LPW, KIND>::scan(cw, k - 27, ocx, ocy, ocz, qf, a, wsqr, wsqr32, false, co, overlap,
-                                 eo);
+      if (!__any_sync(gmask, overlap))
+        for (int k = glane; k < 27; k += LPW)
+          CellOps<LPW, KIND>::scan(cw, k, ocx, ocy, ocz, qf, a, wsqr, wsqr32, false, co, overlap,
+                                   eo);
+    } else {
+      for (int k = glane; k < 54; k += LPW) {
+        if (k < 27)
+          CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, qt, a, wsqr, wsqr32, true, cn, overlap, en);
+        else
+          CellOps<LPW, KIND>::scan(cw, k - 27, ocx, ocy, ocz, qf, a, wsqr, wsqr32, false, co,
+                                   overlap, eo);
+      }
     }
     p.new_c = cw.cell_index(nx, ny, nz);
     if (KIND == SYS_SW) {
