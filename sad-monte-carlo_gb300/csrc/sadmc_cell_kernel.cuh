@@ -176,56 +176,137 @@ __device__ __forceinline__ float ds_image_diff(float ph, float pl, float qh, flo
   return __fadd_rn(b, lo);
 }
 
+// The neighbour buckets of a lane group's queries, in shared memory: subcell, image
+// offset and the prefix of the bucket counts.  With the prefix every lane takes
+// candidates glane, glane + LPW, ... wherever they lie, so no lane waits for the fullest
+// bucket of its group.
+struct BucketScan {
+  int cell[54];
+  int pref[55];
+  signed char off[54][3];
+};
+
 template <int LPW, int KIND>
 struct CellOps {
-  // Sum over the 27 buckets around cell (cx,cy,cz) of query q (excluding atom `skip`).
-  // SW: counts contacts, sets *overlap; WCA: binary32 energy.
-  __device__ static void scan(const CellWalker& cw, int k0, int cx, int cy, int cz, const Query& q,
-                              int skip, double wsqr, float wsqr32, bool newq, int& contacts,
-                              bool& overlap, float& e32) {
-    // k0: the neighbour offset handled by this lane (0..26)
+  // Neighbour subcell k0 (0..26) of subcell (cx, cy, cz) and the reference's image
+  // offset: image = p - off * L.
+  __device__ static int bucket(const CellWalker& cw, int k0, int cx, int cy, int cz, int& ox,
+                               int& oy, int& oz) {
     const int dx = k0 / 9 - 1, dy = (k0 / 3) % 3 - 1, dz = k0 % 3 - 1;
     int ux = cx + dx, uy = cy + dy, uz = cz + dz;
-    int ox = 0, oy = 0, oz = 0;  // reference offset: image = p - off * L
+    ox = 0; oy = 0; oz = 0;
     if (ux < 0) { ux += cw.nc[0]; ox = 1; } else if (ux >= cw.nc[0]) { ux -= cw.nc[0]; ox = -1; }
     if (uy < 0) { uy += cw.nc[1]; oy = 1; } else if (uy >= cw.nc[1]) { uy -= cw.nc[1]; oy = -1; }
     if (uz < 0) { uz += cw.nc[2]; oz = 1; } else if (uz >= cw.nc[2]) { uz -= cw.nc[2]; oz = -1; }
-    const int c = cw.cell_index(ux, uy, uz);
+    return cw.cell_index(ux, uy, uz);
+  }
+
+  // One candidate j seen from query q through image offset (ox, oy, oz).  SW: counts a
+  // contact or sets *overlap (new position); WCA: binary32 pair energy into e32.
+  __device__ static void pair(const CellWalker& cw, int j, int ox, int oy, int oz, const Query& q,
+                              double wsqr, float wsqr32, bool newq, int& contacts, bool& overlap,
+                              float& e32) {
+    const float fx = (float)ox, fy = (float)oy, fz = (float)oz;
+    const float4 pj = cw.p32[KIND == SYS_WCA ? 2 * j : j];
+    const float ax = (pj.x - fx * cw.L32[0]) - q.hx, ay = (pj.y - fy * cw.L32[1]) - q.hy,
+                az = (pj.z - fz * cw.L32[2]) - q.hz;
+    const float d2 = ax * ax + ay * ay + az * az;
+    if (KIND == SYS_SW) {
+      bool near = fabsf(d2 - 1.0f) < 2e-4f || fabsf(d2 - wsqr32) < 2e-4f;
+      if (!near) {
+        if (d2 < 1.0f) { if (newq) overlap = true; else ++contacts; }
+        else if (d2 < wsqr32) ++contacts;
+      } else {
+        // the reference's FP64 expression (optsquare.rs:78-86)
+        const double bx = (cw.p[j] - (double)ox * cw.L[0]) - q.x;
+        const double by = (cw.p[cw.np + j] - (double)oy * cw.L[1]) - q.y;
+        const double bz = (cw.p[2 * cw.np + j] - (double)oz * cw.L[2]) - q.z;
+        const double e2 = bx * bx + by * by + bz * bz;
+        if (e2 < 1.0) { if (newq) overlap = true; else ++contacts; }
+        else if (e2 < wsqr) ++contacts;
+      }
+    } else if (d2 < wsqr32 + 1e-3f) {
+      // WCA: pairs whose high-part r^2 may lie inside the cutoff (the high parts are
+      // within 2^-24 |L| of each coordinate) are refined on the double-single positions
+      const float4 pl = cw.p32[2 * j + 1];
+      const float rx = ds_image_diff(pj.x, pl.x, q.hx, q.lx, fx, cw.L32[0], cw.Ll32[0]);
+      const float ry = ds_image_diff(pj.y, pl.y, q.hy, q.ly, fy, cw.L32[1], cw.Ll32[1]);
+      const float rz = ds_image_diff(pj.z, pl.z, q.hz, q.lz, fz, cw.L32[2], cw.Ll32[2]);
+      e32 += wca_v32(rx * rx + ry * ry + rz * rz, wsqr32);
+    }
+  }
+
+  // Sum over the candidates of one bucket k0 (0..26) around cell (cx,cy,cz) of query q
+  // (excluding atom `skip`); one lane per bucket.
+  __device__ static void scan(const CellWalker& cw, int k0, int cx, int cy, int cz, const Query& q,
+                              int skip, double wsqr, float wsqr32, bool newq, int& contacts,
+                              bool& overlap, float& e32) {
+    int ox, oy, oz;
+    const int c = bucket(cw, k0, cx, cy, cz, ox, oy, oz);
     const int m = min(cw.cnt[c], cw.bucket);
     const int* list = cw.atoms + (size_t)c * cw.bucket;
-    const float fx = (float)ox, fy = (float)oy, fz = (float)oz;
-    const float sx = fx * cw.L32[0], sy = fy * cw.L32[1], sz = fz * cw.L32[2];
-    // WCA: pairs whose high-part r^2 may lie inside the cutoff (the high parts are within
-    // 2^-24 |L| of each coordinate) are refined on the double-single positions
-    const float screen = wsqr32 + 1e-3f;
     for (int k = 0; k < m; ++k) {
       const int j = list[k];
-      if (j == skip) continue;
-      const float4 pj = cw.p32[KIND == SYS_WCA ? 2 * j : j];
-      const float ax = (pj.x - sx) - q.hx, ay = (pj.y - sy) - q.hy, az = (pj.z - sz) - q.hz;
-      const float d2 = ax * ax + ay * ay + az * az;
-      if (KIND == SYS_SW) {
-        bool near = fabsf(d2 - 1.0f) < 2e-4f || fabsf(d2 - wsqr32) < 2e-4f;
-        if (!near) {
-          if (d2 < 1.0f) { if (newq) overlap = true; else ++contacts; }
-          else if (d2 < wsqr32) ++contacts;
-        } else {
-          // the reference's FP64 expression (optsquare.rs:78-86)
-          const double bx = (cw.p[j] - (double)ox * cw.L[0]) - q.x;
-          const double by = (cw.p[cw.np + j] - (double)oy * cw.L[1]) - q.y;
-          const double bz = (cw.p[2 * cw.np + j] - (double)oz * cw.L[2]) - q.z;
-          const double e2 = bx * bx + by * by + bz * bz;
-          if (e2 < 1.0) { if (newq) overlap = true; else ++contacts; }
-          else if (e2 < wsqr) ++contacts;
-        }
-      } else if (d2 < screen) {
-        const float4 pl = cw.p32[2 * j + 1];
-        const float rx = ds_image_diff(pj.x, pl.x, q.hx, q.lx, fx, cw.L32[0], cw.Ll32[0]);
-        const float ry = ds_image_diff(pj.y, pl.y, q.hy, q.ly, fy, cw.L32[1], cw.Ll32[1]);
-        const float rz = ds_image_diff(pj.z, pl.z, q.hz, q.lz, fz, cw.L32[2], cw.Ll32[2]);
-        e32 += wca_v32(rx * rx + ry * ry + rz * rz, wsqr32);
-      }
+      if (j != skip) pair(cw, j, ox, oy, oz, q, wsqr, wsqr32, newq, contacts, overlap, e32);
     }
+  }
+
+  // The candidates of nq queries (1 or 2), 27 buckets each, spread evenly over the group:
+  // query 0's buckets around (c0x, c0y, c0z) are entries 0..26 of bs, query 1's around
+  // (c1x, c1y, c1z) entries 27..53.  Results go to each query's accumulators (SW:
+  // contacts and the overlap flag; WCA: energy).
+  __device__ static void scan_group(const CellWalker& cw, BucketScan& bs, int nq, int c0x, int c0y,
+                                    int c0z, int c1x, int c1y, int c1z, const Query& q0,
+                                    const Query& q1, bool new0, bool new1, int skip, double wsqr,
+                                    float wsqr32, int glane, unsigned gmask, int& cont0,
+                                    int& cont1, bool& overlap, float& e0, float& e1) {
+    const int nb = 27 * nq;
+    for (int k = glane; k < nb; k += LPW) {
+      const bool second = k >= 27;
+      int ox, oy, oz;
+      const int c = bucket(cw, second ? k - 27 : k, second ? c1x : c0x, second ? c1y : c0y,
+                           second ? c1z : c0z, ox, oy, oz);
+      bs.cell[k] = c;
+      bs.off[k][0] = (signed char)ox; bs.off[k][1] = (signed char)oy; bs.off[k][2] = (signed char)oz;
+      bs.pref[k + 1] = min(cw.cnt[c], cw.bucket);
+    }
+    if (LPW > 1) __syncwarp(gmask);
+    // prefix of the counts: each lane sums a contiguous chunk, then a scan over the group
+    constexpr int kMaxChunk = (54 + LPW - 1) / LPW;
+    const int chunk = (nb + LPW - 1) / LPW, e0i = glane * chunk;
+    int mine = 0;
+#pragma unroll
+    for (int i = 0; i < kMaxChunk; ++i)
+      if (i < chunk && e0i + i < nb) mine += bs.pref[e0i + i + 1];
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < LPW; o <<= 1) {
+      const int y = __shfl_up_sync(gmask, incl, o, LPW);
+      if (glane >= o) incl += y;
+    }
+    const int total = LPW > 1 ? __shfl_sync(gmask, incl, LPW - 1, LPW) : incl;
+    int run = incl - mine;
+#pragma unroll
+    for (int i = 0; i < kMaxChunk; ++i)
+      if (i < chunk && e0i + i < nb) {
+        run += bs.pref[e0i + i + 1];
+        bs.pref[e0i + i + 1] = run;
+      }
+    if (glane == 0) bs.pref[0] = 0;
+    if (LPW > 1) __syncwarp(gmask);
+    int k = 0;
+    for (int cnd = glane; cnd < total; cnd += LPW) {
+      while (bs.pref[k + 1] <= cnd) ++k;
+      const int j = cw.atoms[(size_t)bs.cell[k] * cw.bucket + (cnd - bs.pref[k])];
+      if (j == skip) continue;
+      const bool second = k >= 27;
+      int dc = 0;
+      float de = 0.0f;
+      pair(cw, j, bs.off[k][0], bs.off[k][1], bs.off[k][2], second ? q1 : q0, wsqr, wsqr32,
+           second ? new1 : new0, dc, overlap, de);
+      if (second) { cont1 += dc; e1 += de; } else { cont0 += dc; e0 += de; }
+    }
+    if (LPW > 1) __syncwarp(gmask);  // the group may reuse bs next
   }
 };
 
@@ -242,6 +323,7 @@ __global__ void __launch_bounds__(128, 1) cell_move_kernel(MoveLaunch m, CellSys
   if (!wr) w = m.n_walkers - 1;
   const unsigned gmask = group_mask<LPW>(group);
 
+  __shared__ BucketScan sbs[128 / LPW];
   Fh<LPW, FAM> fh;
   fh.load(m.cores, m.P, m.B, w, gmask, glane, wr);
   CellWalker cw;
@@ -288,25 +370,20 @@ __global__ void __launch_bounds__(128, 1) cell_move_kernel(MoveLaunch m, CellSys
     const Query qt = make_query<KIND == SYS_WCA>(p.tx, p.ty, p.tz);
     const Query qf = query_of<KIND == SYS_WCA>(cw, a);
     int cn = 0, co = 0;
-    bool overlap = false;
     float en = 0.0f, eo = 0.0f;
+    bool overlap = false;
+    BucketScan& bs = sbs[threadIdx.x / LPW];
     if (KIND == SYS_SW) {
       // the new position first: a hard-core overlap makes the move impossible, and then
       // the old position's contacts are not needed
-      for (int k = glane; k < 27; k += LPW)
-        CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, qt, a, wsqr, wsqr32, true, cn, overlap, en);
+      CellOps<LPW, KIND>::scan_group(cw, bs, 1, nx, ny, nz, 0, 0, 0, qt, qt, true, true, a, wsqr,
+                                     wsqr32, glane, gmask, cn, cn, overlap, en, en);
       if (!__any_sync(gmask, overlap))
-        for (int k = glane; k < 27; k += LPW)
-          CellOps<LPW, KIND>::scan(cw, k, ocx, ocy, ocz, qf, a, wsqr, wsqr32, false, co, overlap,
-                                   eo);
+        CellOps<LPW, KIND>::scan_group(cw, bs, 1, ocx, ocy, ocz, 0, 0, 0, qf, qf, false, false, a,
+                                       wsqr, wsqr32, glane, gmask, co, co, overlap, eo, eo);
     } else {
-      for (int k = glane; k < 54; k += LPW) {
-        if (k < 27)
-          CellOps<LPW, KIND>::scan(cw, k, nx, ny, nz, qt, a, wsqr, wsqr32, true, cn, overlap, en);
-        else
-          CellOps<LPW, KIND>::scan(cw, k - 27, ocx, ocy, ocz, qf, a, wsqr, wsqr32, false, co,
-                                   overlap, eo);
-      }
+      CellOps<LPW, KIND>::scan_group(cw, bs, 2, nx, ny, nz, ocx, ocy, ocz, qt, qf, true, false, a,
+                                     wsqr, wsqr32, glane, gmask, cn, co, overlap, en, eo);
     }
     p.new_c = cw.cell_index(nx, ny, nz);
     if (KIND == SYS_SW) {
