@@ -258,18 +258,19 @@ def case_da(G, seed=11, walkers=8192, moves=2048, **_):
     return da_compare(G, 0, walkers, moves)
 
 
-def case_grand_wca(G, seed=11, walkers=512, moves=2048, **_):
+def case_grand_wca(G, seed=11, walkers=512, moves=2048, lpw=0):
     """Grand-canonical WCA fluid, energy-number SAMC (wca.rs:307-323): walkers start empty
     in a periodic box of edge 6 and grow to at most 200 atoms (density up to 0.93)."""
     gb = G.GrandBatch(G.make_grand_config(walkers, 200, box=(6.0, 6.0, 6.0), method=G.SAMC,
                                           t0=1e4, energy_bin=1.0, max_allowed=400.0,
                                           translation_scale=0.1, addremove_probability=0.2,
-                                          e_lo=-1.0, e_hi=402.0, seed=seed))
+                                          e_lo=-1.0, e_hi=402.0, seed=seed, lanes_per_walker=lpw))
     sec = _time_run(gb, moves, 4096)
     out = {"workload": f"grand-canonical WCA fluid (box 6^3, N <= 200), energy-number SAMC "
-                       f"t0=1e4, {walkers} walkers, one warp per walker",
+                       f"t0=1e4, {walkers} walkers",
            "moves": walkers * moves, "moves_per_s": walkers * moves / sec,
-           "mean_N": float(np.mean([gb.scalars(w)["N"] for w in range(0, walkers, 64)]))}
+           "mean_N": float(np.mean([gb.scalars(w)["N"] for w in range(0, walkers, 64)])),
+           "lanes_per_walker": lpw or 32}
     gb.close()
     return out
 

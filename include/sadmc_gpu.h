@@ -289,8 +289,8 @@ typedef struct sadmc_grand_config {
   int32_t system;            /* SADMC_LJ or SADMC_WCA */
   double drift_tol;          /* 0 = 1e-2 */
   double box[3];             /* WCA: periodic box (at least 3 subcells of 2^(1/6) per axis) */
-  int32_t lanes_per_walker;  /* LJ: lanes of a warp per walker, 32/16/8/4 (at least 8 when
-                                max_N >= 32); 0 = 8.  The WCA fluid takes a warp per walker. */
+  int32_t lanes_per_walker;  /* lanes of a warp per walker.  LJ: 32/16/8/4 (at least 8 when
+                                max_N >= 32), 0 = 8.  WCA: 32/16/8, 0 = 32. */
 } sadmc_grand_config;
 int32_t sadmc_grand_create(const sadmc_grand_config* cfg, sadmc_grand** out);
 int32_t sadmc_grand_destroy(sadmc_grand* h);

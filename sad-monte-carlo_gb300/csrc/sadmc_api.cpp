@@ -1421,11 +1421,16 @@ int32_t sadmc_grand_create(const sadmc_grand_config* c, sadmc_grand** out) {
     if (!(l == 4 || l == 8 || l == 16 || l == 32) || np / l > 8)
       return fail(SADMC_ERR_INVALID, "lanes_per_walker: 32, 16, 8 or 4 (at least 8 when max_N >= 32)");
   }
+  if (wca && c->lanes_per_walker != 0) {
+    const int l = c->lanes_per_walker;
+    if (!(l == 8 || l == 16 || l == 32))
+      return fail(SADMC_ERR_INVALID, "lanes_per_walker of the WCA fluid: 32, 16 or 8");
+  }
   auto* h = new sadmc_grand();
   h->cfg = *c;
   h->W = c->n_walkers;
   h->np = wca ? (c->max_N + 31) / 32 * 32 : (c->max_N < 32 ? 32 : 64);
-  h->lanes = c->lanes_per_walker ? c->lanes_per_walker : 8;
+  h->lanes = c->lanes_per_walker ? c->lanes_per_walker : (wca ? 32 : 8);
   h->ncol = c->max_N + 1;
   for (int a = 0; a < 3; ++a) h->nc[a] = ncell[a];
   h->cell_cap = ncell[0] * ncell[1] * ncell[2];

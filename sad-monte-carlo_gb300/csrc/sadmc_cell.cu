@@ -108,14 +108,19 @@ __global__ void cell_energy_kernel(const WalkerCore* cores, CellSys s, int n_wal
 // wca.rs:307-323): translations (wca.rs:342-353), adds at a uniform point of the box
 // (add_atom_at, wca.rs:105-116; optcell.rs:126-130) and removals of a uniform atom
 // (remove_atom_number, wca.rs:151-163; optcell.rs:177-193: swap_remove, the last atom
-// takes the removed index).  One warp per walker over the subcell buckets.
+// takes the removed index).  LPW lanes per walker over the subcell buckets (32 by
+// default: a batch of a few hundred walkers needs the warps).
+template <int LPW>
 __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
-  const int lane = threadIdx.x & 31;
-  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  constexpr int WPW = 32 / LPW;
+  const int group = (threadIdx.x & 31) / LPW, glane = (threadIdx.x & 31) % LPW;
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * WPW + group;
+  // every collective below is over the walker's own group: a group past the last walker
+  // leaves without disturbing the others
   if (w >= m.n_walkers) return;
-  const unsigned full = 0xffffffffu;
-  GrandBook<32> bk;
-  bk.load(m, w, lane, full);
+  const unsigned gmask = group_mask<LPW>(group);
+  GrandBook<LPW> bk;
+  bk.load(m, w, glane, gmask);
   CellWalker cw;
   cw.np = m.np;
   cw.bucket = m.bucket;
@@ -145,9 +150,11 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
     bool ov = false;
     float e = 0.0f;
     const Query q = make_query<true>(qx, qy, qz);
-    for (int k = lane; k < 27; k += 32)
-      CellOps<32, SYS_WCA>::scan(cw, k, cx, cy, cz, q, skip, wsqr, wsqr32, true, cn, ov, e);
-    return group_sum<32>(e, full);
+    // one bucket per lane: the grand fluids are sparse (mostly empty subcells), where
+    // spreading the candidates over the group costs more than it saves
+    for (int k = glane; k < 27; k += LPW)
+      CellOps<LPW, SYS_WCA>::scan(cw, k, cx, cy, cz, q, skip, wsqr, wsqr32, true, cn, ov, e);
+    return group_sum<LPW>(e, gmask);
   };
   const double sc = m.translation_scale;
   Every resum;
@@ -205,7 +212,7 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
       N2 = N1 - 1;
     }
     const bool possible = kind_move >= 0 && fabsf(de) <= 3.0e38f;
-    if (m.trace && lane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
+    if (m.trace && glane == 0 && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap) {
       TraceRec r;
       r.e1 = E1;
       r.e2 = possible ? E1 + (double)de : __longlong_as_double(0x7ff8000000000000ll);
@@ -220,25 +227,25 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
           int* lo = cw.atoms + (size_t)oc * cw.bucket;
           const int mo = min(cw.cnt[oc], cw.bucket);
           int pos = -1;
-          for (int k = lane; k < mo; k += 32)
+          for (int k = glane; k < mo; k += LPW)
             if (lo[k] == which) pos = k;
 #pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            const int x = __shfl_xor_sync(full, pos, o);
+          for (int o = LPW / 2; o > 0; o >>= 1) {
+            const int x = __shfl_xor_sync(gmask, pos, o, LPW);
             pos = x > pos ? x : pos;
           }
-          __syncwarp(full);
-          if (lane == 0 && pos >= 0) {
+          __syncwarp(gmask);
+          if (glane == 0 && pos >= 0) {
             lo[pos] = lo[mo - 1];
             cw.cnt[oc] = mo - 1;
           }
-          __syncwarp(full);
+          __syncwarp(gmask);
         }
       }
       if (kind_move == 0 || kind_move == 1) {
         const int a = kind_move == 0 ? which : N1;
         const int oc = kind_move == 0 ? cw.cell_of[which] : -1;
-        if (lane == 0) {
+        if (glane == 0) {
           if (kind_move == 1 || new_c != oc) {
             const int cnt = cw.cnt[new_c];
             cw.atoms[(size_t)new_c * cw.bucket + cnt] = a;
@@ -254,15 +261,15 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
         int* ll = cw.atoms + (size_t)lc * cw.bucket;
         const int ml = min(cw.cnt[lc], cw.bucket);
         int pos = -1;
-        for (int k = lane; k < ml; k += 32)
+        for (int k = glane; k < ml; k += LPW)
           if (ll[k] == last) pos = k;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const int x = __shfl_xor_sync(full, pos, o);
+        for (int o = LPW / 2; o > 0; o >>= 1) {
+          const int x = __shfl_xor_sync(gmask, pos, o, LPW);
           pos = x > pos ? x : pos;
         }
-        __syncwarp(full);
-        if (lane == 0) {
+        __syncwarp(gmask);
+        if (glane == 0) {
           if (pos >= 0) ll[pos] = which;
           cw.cell_of[which] = lc;
           cw.p[which] = cw.p[last];
@@ -272,15 +279,15 @@ __global__ void __launch_bounds__(128) wca_grand_kernel(GrandLaunch m) {
           cw.p32[2 * which + 1] = cw.p32[2 * last + 1];
         }
       }
-      __syncwarp(full);
+      __syncwarp(gmask);
     }
     bk.finish(m, t, E1, N1);
     if (resum.tick()) {
       double e = 0.0;
       const int n = bk.c.N;
-      for (int i = lane; i < n; i += 32)
+      for (int i = glane; i < n; i += LPW)
         e += cw.pair_sum64(i, [&](double r2) { return wca_v64(r2, wsqr); });
-      bk.resummed(m, group_sum<32>(e, full) * 0.5);
+      bk.resummed(m, group_sum<LPW>(e, gmask) * 0.5);
     }
   }
   bk.store(m.cores, w);
@@ -313,7 +320,11 @@ cudaError_t launch_cell_energy(const WalkerCore* cores, const CellSys& s, int n_
 
 namespace sadmc {
 cudaError_t launch_wca_grand_move(const GrandLaunch& m, cudaStream_t st) {
-  dev::wca_grand_kernel<<<(m.n_walkers + 3) / 4, 128, 0, st>>>(m);
+  const int lpw = m.lanes == 8 || m.lanes == 16 ? m.lanes : 32;
+  const int warps = (m.n_walkers + (32 / lpw) - 1) / (32 / lpw);
+  if (lpw == 8) dev::wca_grand_kernel<8><<<(warps + 3) / 4, 128, 0, st>>>(m);
+  else if (lpw == 16) dev::wca_grand_kernel<16><<<(warps + 3) / 4, 128, 0, st>>>(m);
+  else dev::wca_grand_kernel<32><<<(warps + 3) / 4, 128, 0, st>>>(m);
   return cudaGetLastError();
 }
 }  // namespace sadmc

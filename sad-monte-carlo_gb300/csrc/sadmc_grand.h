@@ -47,7 +47,8 @@ struct GrandLaunch {
   float* pos;            // [walker][6][np] double-single positions
   int np, rows, ncol;    // ncol = N_cap + 1
   int n_walkers;
-  int lanes;             // LJ: lanes per walker (32, 16, 8 or 4; np / lanes atoms a lane)
+  int lanes;             // lanes per walker (LJ: 32, 16, 8 or 4, np / lanes atoms a lane;
+                         // WCA: 32, 16 or 8)
   uint64_t n_moves, seed;
   double width, inv_width, radius, radius2, t0, target_rate, translation_scale;
   double min_allowed, max_allowed;

@@ -469,7 +469,7 @@ def make_grand_config(n_walkers, max_N, radius=0.0, *, box=None, method=SAMC, t0
                       translation_scale=0.05, addremove_probability=0.05, e_lo=-200.0,
                       e_hi=50.0, seed=0, resum_interval=0, drift_tol=0.0, lanes_per_walker=0):
     """Energy-number walkers: the LJ cluster of `radius`, or (box given) the WCA fluid.
-    lanes_per_walker: LJ lanes per walker (32, 16, 8, 4; 0 = 8)."""
+    lanes_per_walker: lanes per walker (LJ: 32, 16, 8, 4, 0 = 8; WCA: 32, 16, 8, 0 = 32)."""
     c = GrandConfig()
     c.system = WCA if box is not None else LJ
     if box is not None:

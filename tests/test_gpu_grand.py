@@ -48,8 +48,8 @@ def test_grand_trace_replay(gpu, oracle, method, target, lanes, max_N):
         assert gs["energy"] == pytest.approx(ow.compute_energy(), abs=1e-3)
 
 
-@pytest.mark.parametrize("method", ["samc", "wl"])
-def test_grand_wca_trace_replay(gpu, oracle, method):
+@pytest.mark.parametrize("method,lanes", [("samc", 32), ("wl", 32), ("samc", 16), ("wl", 8)])
+def test_grand_wca_trace_replay(gpu, oracle, method, lanes):
     """The WCA fluid's grand moves (wca.rs:307-323): adds at a uniform point of the box,
     removals by swap_remove out of the subcell lists (optcell.rs:177-193)."""
     W, moves, max_N, L, seed = 6, 20000, 40, 4.5, 5
@@ -57,7 +57,7 @@ def test_grand_wca_trace_replay(gpu, oracle, method):
     common = dict(t0=1000.0, energy_bin=0.5, max_allowed=20.0, translation_scale=0.1,
                   addremove_probability=0.2, seed=seed)
     b = gpu.GrandBatch(gpu.make_grand_config(W, max_N, box=(L, L, L), method=m, e_lo=-1.0,
-                                             e_hi=25.0, **common))
+                                             e_hi=25.0, lanes_per_walker=lanes, **common))
     b.set_trace(moves)
     b.run(moves)
     for w in range(W):
