@@ -490,6 +490,7 @@ def run_reference(args):
         "data": "synthetic (seeded uniform-in-sphere LJ31 configurations)",
         "config": {"workload": WORKLOAD, "sample": f"{walkers} walkers x {moves} moves per step"},
         "cpu_baseline": {"value": value, "unit": "moves/s", "cores": threads, "kind": "port",
+                         "per_core": value / threads,
                          "sample": f"{walkers} C2 walkers x {moves} moves per step, FP64 C++ "
                                    "restatement of the reference (Rust toolchain absent)"},
         "e2e": {"value": value, "unit": "moves/s", "h2d_bytes_per_step": 0,
@@ -610,6 +611,7 @@ def run_gpu(args):
         threads = os.cpu_count() or 1
         v, va, sec, tm = cpu_sample(threads, walkers=256, moves=200000)
         cpu = {"value": v, "unit": "moves/s", "cores": threads, "kind": "port",
+               "per_core": v / threads, "accepted_moves_per_s": va,
                "sample": f"256 C2 walkers x 200000 moves ({tm} moves, {sec:.2f} s wall), FP64 "
                          "C++ restatement of the reference (Rust toolchain absent)"}
 
