@@ -106,6 +106,7 @@ struct sadmc_handle {
   float* sg_v = nullptr;
   __nv_bfloat16* sg_w1t = nullptr;              // bf16 copies for the tensor cores
   __nv_bfloat16* sg_w2t = nullptr;
+  __nv_bfloat16* sg_wc = nullptr;               // the same in tcgen05 shared-memory order
   float* sg_ring_pos = nullptr;                 // [cap][N][3] binary32
   float* sg_ring_e = nullptr;
   int sg_cap = 0, sg_head = 0, sg_count = 0, sg_step = 0;
@@ -117,14 +118,14 @@ struct sadmc_handle {
   int sg_batch_cap = 0;
   double* sg_loss = nullptr;
   uint64_t* sg_stats = nullptr;                 // [W][2] delayed-acceptance counters
-  SgWeights sg_weights() const { return SgWeights::from(sg_master, sg_w1t, sg_w2t); }
+  SgWeights sg_weights() const { return SgWeights::from(sg_master, sg_w1t, sg_w2t, sg_wc); }
   void free_surrogate() {
     cudaFree(sg_master); cudaFree(sg_grad); cudaFree(sg_m); cudaFree(sg_v); cudaFree(sg_w1t);
-    cudaFree(sg_w2t); cudaFree(sg_ring_pos); cudaFree(sg_ring_e); cudaFree(sg_scratch);
+    cudaFree(sg_w2t); cudaFree(sg_wc); cudaFree(sg_ring_pos); cudaFree(sg_ring_e); cudaFree(sg_scratch);
     cudaFree(sg_batch_pos); cudaFree(sg_batch_e); cudaFree(sg_idx); cudaFree(sg_loss); cudaFree(sg_stats);
     sg_stats = nullptr;
     sg_master = sg_grad = sg_m = sg_v = sg_ring_pos = sg_ring_e = sg_batch_pos = sg_batch_e = nullptr;
-    sg_w1t = sg_w2t = nullptr; sg_scratch = nullptr; sg_idx = nullptr; sg_loss = nullptr;
+    sg_w1t = sg_w2t = sg_wc = nullptr; sg_scratch = nullptr; sg_idx = nullptr; sg_loss = nullptr;
   }
   // scratch for `rows` rows and a gathered batch of `configs` configurations
   cudaError_t sg_reserve(size_t rows, int configs) {
@@ -1152,6 +1153,7 @@ int32_t sadmc_surrogate_init(sadmc_handle* h, uint64_t seed, int32_t ring_capaci
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_v, sizeof(float) * SG_NPARAM);
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_w1t, sizeof(__nv_bfloat16) * SG_RBF * SG_H1);
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_w2t, sizeof(__nv_bfloat16) * SG_H1 * SG_H2);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_wc, sizeof(__nv_bfloat16) * SG_WC_ELEMS);
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_ring_pos, sizeof(float) * 3 * (size_t)n * ring_capacity);
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_ring_e, sizeof(float) * ring_capacity);
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_loss, sizeof(double));

@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(128, 1) forward_tc_kernel(const __nv_bfloat16*
   __shared__ __align__(1024) uint4 sB2[SG_H2 * SG_H1 / 8];  // W2^T
   __shared__ float sb1[SG_H1], sb2[SG_H2], sw3[SG_H2];
   __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t wbar;  // the weights' bulk copies
   __shared__ uint32_t tbase;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row0 = blockIdx.x * M;
@@ -88,20 +89,18 @@ __global__ void __launch_bounds__(128, 1) forward_tc_kernel(const __nv_bfloat16*
     const uint4 v = row0 + r < rows ? G[(size_t)(row0 + r) * (SG_RBF / 8) + kg] : make_uint4(0, 0, 0, 0);
     *reinterpret_cast<uint4*>(a1 + tc05::core_offset(r, kg, SG_RBF / 8)) = v;
   }
-  const uint4* W1 = reinterpret_cast<const uint4*>(wts.w1t);
-  for (int c = tid; c < SG_H1 * (SG_RBF / 8); c += 128) {
-    const int n = c / (SG_RBF / 8), kg = c % (SG_RBF / 8);
-    *reinterpret_cast<uint4*>(b1 + tc05::core_offset(n, kg, SG_RBF / 8)) = W1[c];
-  }
-  const uint4* W2 = reinterpret_cast<const uint4*>(wts.w2t);
-  for (int c = tid; c < SG_H2 * (SG_H1 / 8); c += 128) {
-    const int n = c / (SG_H1 / 8), kg = c % (SG_H1 / 8);
-    *reinterpret_cast<uint4*>(b2 + tc05::core_offset(n, kg, SG_H1 / 8)) = W2[c];
-  }
   for (int k = tid; k < SG_H1; k += 128) { sb1[k] = wts.b1[k]; sb2[k] = wts.b2[k]; sw3[k] = wts.w3[k]; }
   // 256 columns: the two 64-column accumulators with room to spare (two CTAs per SM)
   if (warp == 0) tc05::tmem_alloc(&tbase, 256);
-  if (tid == 0) tc05::mbar_init(&mbar, 1);
+  constexpr uint32_t kW1Bytes = SG_H1 * SG_RBF * 2, kW2Bytes = SG_H2 * SG_H1 * 2;
+  if (tid == 0) {
+    tc05::mbar_init(&mbar, 1);
+    tc05::mbar_init(&wbar, 1);
+    // the weights come already in core-matrix order: two bulk copies by the copy engine
+    tc05::mbar_expect_tx(&wbar, kW1Bytes + kW2Bytes);
+    tc05::bulk_g2s(b1, wts.wc, kW1Bytes, &wbar);
+    tc05::bulk_g2s(b2, wts.wc + SG_H1 * SG_RBF, kW2Bytes, &wbar);
+  }
   tc05::fence_smem_async();
   tc05::fence_before();
   __syncthreads();
@@ -109,8 +108,10 @@ __global__ void __launch_bounds__(128, 1) forward_tc_kernel(const __nv_bfloat16*
   const uint32_t tmem = tbase;
   constexpr uint32_t idesc = tc05::idesc_bf16(M, SG_H1);
   constexpr uint32_t kPolls = 1u << 24;
-  // layer 1: D1 = G W1 (two K = 16 steps, 2 core matrices = 256 bytes apart)
-  if (tid == 0) {
+  // layer 1: D1 = G W1 (two K = 16 steps, 2 core matrices = 256 bytes apart), once the
+  // weights have landed
+  const bool wok = tid == 0 ? tc05::mbar_wait(&wbar, 0, kPolls) : true;
+  if (tid == 0 && wok) {
 #pragma unroll
     for (int ks = 0; ks < SG_RBF / 16; ++ks)
       tc05::mma_bf16(tmem, tc05::sdesc(tc05::smem_u32(a1) + 256 * ks, 128, 128 * (SG_RBF / 8)),
@@ -271,15 +272,20 @@ __global__ void adam_kernel(float* w, const float* grad, float* m, float* v, int
   w[p] -= lr * mh / (sqrtf(vh) + eps);
 }
 
-__global__ void refresh_bf16_kernel(const float* w, __nv_bfloat16* w1t, __nv_bfloat16* w2t) {
+__global__ void refresh_bf16_kernel(const float* w, __nv_bfloat16* w1t, __nv_bfloat16* w2t,
+                                    __nv_bfloat16* wc) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p < SG_RBF * SG_H1) {
     const int k = p / SG_H1, n = p % SG_H1;
-    w1t[n * SG_RBF + k] = __float2bfloat16_rn(w[SG_OFF_W1 + p]);
+    const __nv_bfloat16 v = __float2bfloat16_rn(w[SG_OFF_W1 + p]);
+    w1t[n * SG_RBF + k] = v;
+    wc[(tc05::core_offset(n, k / 8, SG_RBF / 8) + 2 * (k % 8)) / 2] = v;
   }
   if (p < SG_H1 * SG_H2) {
     const int k = p / SG_H2, n = p % SG_H2;
-    w2t[n * SG_H1 + k] = __float2bfloat16_rn(w[SG_OFF_W2 + p]);
+    const __nv_bfloat16 v = __float2bfloat16_rn(w[SG_OFF_W2 + p]);
+    w2t[n * SG_H1 + k] = v;
+    wc[SG_H1 * SG_RBF + (tc05::core_offset(n, k / 8, SG_H1 / 8) + 2 * (k % 8)) / 2] = v;
   }
 }
 
@@ -393,7 +399,7 @@ cudaError_t sg_train_step(const float* pos, const float* target, int configs, in
 }
 
 cudaError_t sg_refresh(const float* master, const SgWeights& w, cudaStream_t st) {
-  dev::refresh_bf16_kernel<<<(SG_H1 * SG_H2 + 127) / 128, 128, 0, st>>>(master, w.w1t, w.w2t);
+  dev::refresh_bf16_kernel<<<(SG_H1 * SG_H2 + 127) / 128, 128, 0, st>>>(master, w.w1t, w.w2t, w.wc);
   return cudaGetLastError();
 }
 

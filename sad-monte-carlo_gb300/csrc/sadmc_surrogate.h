@@ -14,6 +14,7 @@ constexpr int SG_OFF_B2 = SG_OFF_W2 + SG_H1 * SG_H2;
 constexpr int SG_OFF_W3 = SG_OFF_B2 + SG_H2;
 constexpr int SG_OFF_B3 = SG_OFF_W3 + SG_H2;
 constexpr int SG_NPARAM = SG_OFF_B3 + 1;
+constexpr int SG_WC_ELEMS = SG_H1 * SG_RBF + SG_H2 * SG_H1;
 
 struct SgWeights {
   const float* w2;       // master W2 [k][n] (FP32)
@@ -23,9 +24,13 @@ struct SgWeights {
   const float* b3;
   __nv_bfloat16* w1t;    // W1^T [n][k] bf16 (tensor-core B operand)
   __nv_bfloat16* w2t;    // W2^T [n][k] bf16
-  static SgWeights from(float* master, __nv_bfloat16* w1t, __nv_bfloat16* w2t) {
+  // W1^T then W2^T in the tcgen05 shared-memory order (8-row x 16-byte core matrices,
+  // K-major), SG_WC_ELEMS bf16: one bulk copy each lands them ready for the MMA
+  __nv_bfloat16* wc;
+  static SgWeights from(float* master, __nv_bfloat16* w1t, __nv_bfloat16* w2t,
+                        __nv_bfloat16* wc) {
     return SgWeights{master + SG_OFF_W2, master + SG_OFF_B1, master + SG_OFF_B2,
-                     master + SG_OFF_W3, master + SG_OFF_B3, w1t, w2t};
+                     master + SG_OFF_W3, master + SG_OFF_B3, w1t, w2t, wc};
   }
 };
 
