@@ -1306,10 +1306,12 @@ int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, 
     CUDA_TRY(cudaMemset(h->sg_stats, 0, sizeof(uint64_t) * 2 * h->W));
   }
   MoveLaunch m = h->base_launch();  // traced like sadmc_run, with dS in the second record
+  int max_atoms = 0;
+  for (const auto& g : h->geom) max_atoms = std::max(max_atoms, (int)g.n);
   for (uint64_t left = moves; left > 0;) {
     m.n_moves = std::min<uint64_t>(left, 8192);
-    CUDA_TRY(launch_lj_da(m, LjSys{h->d_pos, h->np, h->radius2()}, h->sg_weights(), refresh_interval,
-                          h->sg_stats, h->stream));
+    CUDA_TRY(launch_lj_da(m, LjSys{h->d_pos, h->np, h->radius2()}, h->sg_weights(), max_atoms,
+                          refresh_interval, h->sg_stats, h->stream));
     left -= m.n_moves;
   }
   h->moves_done += moves;

@@ -1,12 +1,13 @@
 // Delayed-acceptance moves for LJ clusters (Christen & Fox, "Markov chain Monte Carlo
 // using an approximation", J. Comput. Graph. Stat. 14, 2005), screened by the learned
-// surrogate of sadmc_surrogate.cu.  One walker per warp.
+// surrogate of sadmc_surrogate.cu.  One walker per warp, DA_WPB walkers per block sharing
+// one shared-memory copy of the weights.
 //
 // Stage 1: the proposal of lj.rs:365-374 is screened with the surrogate energy
 //   E~ = E + sum_i [e_s(G'_i) - e_s(G_i)], accepted with min(1, exp(ln w(E) - ln w(E~))).
 //   The descriptors change incrementally: atom i != a gains phi(|r_i - to|) - phi(|r_i - from|),
 //   the moved atom's row is rebuilt from the new distances; the MLP runs on all rows on the
-//   tensor cores.
+//   tensor cores (mma.sync, 16-row tiles; SiLU in its tanh form).
 // Stage 2: the exact binary32 pair energy e2 (as in lj_move_kernel) decides with the
 //   Christen-Fox ratio min(1, [pi(y) a1(y,x)] / [pi(x) a1(x,y)]), where the reverse
 //   screen a1(y,x) uses e2 - dS (the first stage's approximation depends on the state it
@@ -27,54 +28,103 @@
 namespace sadmc {
 namespace dev {
 
+// Shared memory of a block: the weights once, then one region per walker.
+constexpr int DA_WPB = 4;                                  // walkers (warps) per block
+constexpr int DA_W_WORDS = SG_H1 * SG_RBF / 2 + SG_H2 * SG_H1 / 2 + 3 * SG_H1;
+// Per walker, for R descriptor rows (the atoms rounded up to 16, the MLP's row tile):
+// current and proposed FP32 descriptors (rows padded by one word so that 32 lanes on 32
+// rows meet 32 banks), the proposed bf16 copy (17 words a row) and the per-atom energies.
+__host__ __device__ constexpr int da_rows(int n) { return (n + 15) & ~15; }
+__host__ __device__ constexpr int da_walker_words(int R) { return R * (2 * (SG_RBF + 1) + (SG_RBF + 2) / 2 + 2); }
+inline size_t da_smem_bytes(int R) {
+  return 4 * ((size_t)DA_W_WORDS + (size_t)DA_WPB * (size_t)da_walker_words(R));
+}
+
+// 2^x on the special-function unit (ex2.approx.ftz.f32, relative error about 2^-22)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Sum over the warp of v[l], left in lane l (a butterfly reduce-scatter: at each step a lane
+// keeps the half of its vector its partner sends it and adds the partner's copy of it).
+__device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32], int lane) {
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool up = (lane & s) != 0;
+#pragma unroll
+    for (int j = 0; j < s; ++j) {
+      const float send = up ? v[j] : v[j + s];
+      const float keep = up ? v[j + s] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+    }
+  }
+  return v[0];
+}
+
 template <int APL>
-__global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeights wts,
-                                                    int refresh_interval, uint64_t* stats) {
-  constexpr int NR = 32 * APL;  // descriptor rows (atoms, padded)
-  // Rows are padded by one 32-bit word so that the 32 lanes, each on its own row, hit 32
-  // different banks (the bf16 rows are 17 words: the MLP's fragment loads then meet at
-  // most 2-way conflicts).
-  __shared__ float sG[NR][SG_RBF + 1];              // current descriptors (FP32)
-  __shared__ float sGf[NR][SG_RBF + 1];             // proposed descriptors (FP32)
-  __shared__ __nv_bfloat16 sGb[NR][SG_RBF + 2];     // proposed descriptors (bf16, MLP input)
-  __shared__ float sT[32][SG_RBF + 1];              // contributions to the moved atom's row
-  __shared__ float sE[NR], sEn[NR];                 // per-atom surrogate energies
-  __shared__ uint32_t sW1[SG_H1 * SG_RBF / 2], sW2[SG_H2 * SG_H1 / 2];
-  __shared__ float sb1[SG_H1], sb2[SG_H2], sw3[SG_H2];
-  const int lane = threadIdx.x;
-  for (int k = lane; k < SG_H1 * SG_RBF / 2; k += 32) sW1[k] = reinterpret_cast<const uint32_t*>(wts.w1t)[k];
-  for (int k = lane; k < SG_H2 * SG_H1 / 2; k += 32) sW2[k] = reinterpret_cast<const uint32_t*>(wts.w2t)[k];
-  for (int k = lane; k < SG_H1; k += 32) { sb1[k] = wts.b1[k]; sb2[k] = wts.b2[k]; sw3[k] = wts.w3[k]; }
+__global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys s, SgWeights wts, int R,
+                                                             int refresh_interval, uint64_t* stats) {
+  constexpr int GW = SG_RBF + 1;        // FP32 descriptor row stride (words)
+  constexpr int BW = (SG_RBF + 2) / 2;  // bf16 descriptor row stride (words)
+  extern __shared__ __align__(16) uint32_t da_smem[];
+  uint32_t* sW1 = da_smem;
+  uint32_t* sW2 = sW1 + SG_H1 * SG_RBF / 2;
+  float* sb1 = reinterpret_cast<float*>(sW2 + SG_H2 * SG_H1 / 2);
+  float* sb2 = sb1 + SG_H1;
+  float* sw3 = sb2 + SG_H2;
+  for (int k = threadIdx.x; k < SG_H1 * SG_RBF / 2; k += blockDim.x)
+    sW1[k] = reinterpret_cast<const uint32_t*>(wts.w1t)[k];
+  for (int k = threadIdx.x; k < SG_H2 * SG_H1 / 2; k += blockDim.x)
+    sW2[k] = reinterpret_cast<const uint32_t*>(wts.w2t)[k];
+  for (int k = threadIdx.x; k < SG_H1; k += blockDim.x) { sb1[k] = wts.b1[k]; sb2[k] = wts.b2[k]; sw3[k] = wts.w3[k]; }
+  __syncthreads();
   const float b3 = wts.b3[0];
-  const int w = blockIdx.x;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int w = blockIdx.x * DA_WPB + wib;
   if (w >= m.n_walkers) return;
-  __syncwarp();
   Fh<32> fh;
   fh.load(m.cores, m.P, m.B, w, 0xffffffffu, lane, true);
   LjWalker<32, APL> lj;
   lj.glane = lane;
   lj.gmask = 0xffffffffu;
   lj.n = fh.c.n;
-  const int n = lj.n;
+  const int n = lj.n;  // <= R, the rows every walker region of the launch holds
+  float* sG = reinterpret_cast<float*>(da_smem + DA_W_WORDS + (size_t)wib * da_walker_words(R));
+  float* sGf = sG + R * GW;
+  uint32_t* sGbw = reinterpret_cast<uint32_t*>(sGf + R * GW);
+  __nv_bfloat16* sGb = reinterpret_cast<__nv_bfloat16*>(sGbw);
+  float* sE = reinterpret_cast<float*>(sGbw + R * BW);
+  float* sEn = sE + R;
   float* pw = s.pos + (size_t)w * 6 * (size_t)s.np;
   lj.load(pw, s.np);
   const float inv2w2 = 1.0f / (2.0f * 0.1f * 0.1f);
+  const float l2w = inv2w2 * 1.4426950408889634f;  // the same Gaussian in base 2
+  // high parts of the position of this lane's atom slot q (a runtime q without indexing the
+  // register arrays)
+  auto hi_of = [&](int q, float& xi, float& yi, float& zi) {
+    xi = lj.x[0].h; yi = lj.y[0].h; zi = lj.z[0].h;
+#pragma unroll
+    for (int k = 1; k < APL; ++k)
+      if (q == k) { xi = lj.x[k].h; yi = lj.y[k].h; zi = lj.z[k].h; }
+  };
 
   // surrogate energies of all rows from sGb -> dst
   auto forward_rows = [&](float* dst) {
     for (int r0 = 0; r0 < n; r0 += 16) {
       float ea, eb;
-      mlp16<(SG_RBF + 2) / 2>(reinterpret_cast<const uint32_t*>(&sGb[r0][0]), sW1, sW2, sb1, sb2,
-                              sw3, b3, ea, eb);
+      mlp16<BW>(sGbw + r0 * BW, sW1, sW2, sb1, sb2, sw3, b3, ea, eb);
       const int g = lane >> 2;
       if ((lane & 3) == 0) {
-        if (r0 + g < NR) dst[r0 + g] = ea;
-        if (r0 + g + 8 < NR) dst[r0 + g + 8] = eb;
+        dst[r0 + g] = ea;
+        dst[r0 + g + 8] = eb;
       }
     }
     __syncwarp();
   };
-  // full descriptors of the current configuration, their bf16 copy and energies
+  // full descriptors of the current configuration, their bf16 copy and energies (rows
+  // n..R-1 hold zeros)
   auto refresh = [&]() {
     for (int q = 0; q < APL; ++q) {
       float gacc[SG_RBF];
@@ -95,10 +145,12 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
           }
         }
       }
+      if (i < R) {
 #pragma unroll
-      for (int k = 0; k < SG_RBF; ++k) {
-        sG[i][k] = i < n ? gacc[k] : 0.f;
-        sGb[i][k] = __float2bfloat16_rn(i < n ? gacc[k] : 0.f);
+        for (int k = 0; k < SG_RBF; ++k) {
+          sG[i * GW + k] = i < n ? gacc[k] : 0.f;
+          sGb[i * 2 * BW + k] = __float2bfloat16_rn(i < n ? gacc[k] : 0.f);
+        }
       }
     }
     __syncwarp();
@@ -133,11 +185,15 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
     const DS tz = ds_add(fz, ds_scale(d.g2, sc.h, sc.l));
     // ---- stage 1: surrogate screen ----
     float part = 0.f;
+    float col[SG_RBF];  // this lane's atoms' contributions to the moved atom's row
+#pragma unroll
+    for (int k = 0; k < SG_RBF; ++k) col[k] = 0.f;
+#pragma unroll 1
     for (int q = 0; q < APL; ++q) {
       const int i = lane + 32 * q;
-      float contrib[SG_RBF];
       if (i < n && i != a) {
-        const float xi = lj.x[q].h, yi = lj.y[q].h, zi = lj.z[q].h;
+        float xi, yi, zi;
+        hi_of(q, xi, yi, zi);
         float dx = xi - fx.h, dy = yi - fy.h, dz = zi - fz.h;
         const float ro = sqrtf(dx * dx + dy * dy + dz * dz);
         dx = xi - tx.h; dy = yi - ty.h; dz = zi - tz.h;
@@ -145,27 +201,19 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
 #pragma unroll
         for (int k = 0; k < SG_RBF; ++k) {
           const float cn = rbf_centre(k);
-          const float pn = __expf(-(rn - cn) * (rn - cn) * inv2w2);
-          const float po = __expf(-(ro - cn) * (ro - cn) * inv2w2);
-          const float gnew = sG[i][k] + pn - po;
-          sGf[i][k] = gnew;
-          sGb[i][k] = __float2bfloat16_rn(gnew);
-          contrib[k] = pn;
+          const float pn = ex2_approx(-((rn - cn) * (rn - cn)) * l2w);
+          const float po = ex2_approx(-((ro - cn) * (ro - cn)) * l2w);
+          const float gnew = sG[i * GW + k] + pn - po;
+          sGf[i * GW + k] = gnew;
+          sGb[i * 2 * BW + k] = __float2bfloat16_rn(gnew);
+          col[k] += pn;
         }
-      } else {
-#pragma unroll
-        for (int k = 0; k < SG_RBF; ++k) contrib[k] = 0.f;
       }
-#pragma unroll
-      for (int k = 0; k < SG_RBF; ++k) sT[lane][k] = q == 0 ? contrib[k] : sT[lane][k] + contrib[k];
     }
-    __syncwarp();
-    {  // moved atom's row: column sums of sT
-      float ga = 0.f;
-      for (int r = 0; r < 32; ++r) ga += sT[r][lane];
-      sGf[a][lane] = ga;
-      sGb[a][lane] = __float2bfloat16_rn(ga);
-    }
+    // moved atom's row: lane k takes column k of the contributions
+    const float ga = warp_reduce_scatter32(col, lane);
+    sGf[a * GW + lane] = ga;
+    sGb[a * 2 * BW + lane] = __float2bfloat16_rn(ga);
     __syncwarp();
     forward_rows(sEn);
     for (int q = 0; q < APL; ++q) {
@@ -216,14 +264,16 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
       acc = fh.decide_de(possible, de, u_second, rs, true, lnw_first);
       if (acc) {
         lj.put(a, tx, ty, tz);
+#pragma unroll 1
         for (int q = 0; q < APL; ++q) {
           const int i = lane + 32 * q;
+          if (i < n && i != a) {
 #pragma unroll
-          for (int k = 0; k < SG_RBF; ++k) sG[i][k] = sGf[i][k];
-          sE[i] = sEn[i];
+            for (int k = 0; k < SG_RBF; ++k) sG[i * GW + k] = sGf[i * GW + k];
+          }
+          if (i < n) sE[i] = sEn[i];
         }
-        // the moved atom's row was written by lane k into column k
-        for (int k = 0; k < SG_RBF; ++k) sG[a][k] = sGf[a][k];
+        sG[a * GW + lane] = ga;  // the moved atom's row, column `lane`
         __syncwarp();
       }
     }
@@ -254,11 +304,26 @@ __global__ void __launch_bounds__(32) lj_da_kernel(MoveLaunch m, LjSys s, SgWeig
 
 }  // namespace dev
 
-cudaError_t launch_lj_da(const MoveLaunch& m, const LjSys& s, const SgWeights& w,
+cudaError_t launch_lj_da(const MoveLaunch& m, const LjSys& s, const SgWeights& w, int max_atoms,
                          int refresh_interval, uint64_t* stats, cudaStream_t st) {
-  if (s.np == 32) dev::lj_da_kernel<1><<<m.n_walkers, 32, 0, st>>>(m, s, w, refresh_interval, stats);
-  else if (s.np == 64) dev::lj_da_kernel<2><<<m.n_walkers, 32, 0, st>>>(m, s, w, refresh_interval, stats);
-  else return cudaErrorInvalidConfiguration;
+  if ((s.np != 32 && s.np != 64) || max_atoms < 2 || max_atoms > s.np) return cudaErrorInvalidConfiguration;
+  const int R = dev::da_rows(max_atoms);
+  static bool attr[64][2] = {};  // the limit (for R = np) is set once per device and shape
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return e;
+  const int shape = s.np == 32 ? 0 : 1;
+  if (device < 0 || device >= 64 || !attr[device][shape]) {
+    const int lim = (int)dev::da_smem_bytes(s.np);
+    e = shape == 0 ? cudaFuncSetAttribute(dev::lj_da_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)
+                   : cudaFuncSetAttribute(dev::lj_da_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (e != cudaSuccess) return e;
+    if (device >= 0 && device < 64) attr[device][shape] = true;
+  }
+  const size_t bytes = dev::da_smem_bytes(R);
+  const int blocks = (m.n_walkers + dev::DA_WPB - 1) / dev::DA_WPB;
+  if (shape == 0) dev::lj_da_kernel<1><<<blocks, 32 * dev::DA_WPB, bytes, st>>>(m, s, w, R, refresh_interval, stats);
+  else dev::lj_da_kernel<2><<<blocks, 32 * dev::DA_WPB, bytes, st>>>(m, s, w, R, refresh_interval, stats);
   return cudaGetLastError();
 }
 

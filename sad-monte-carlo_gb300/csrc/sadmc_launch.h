@@ -46,9 +46,10 @@ cudaError_t launch_lj_plan(WalkerCore* cores, const LjSys& s, int walker, int wh
                            cudaStream_t st);
 
 // Delayed-acceptance LJ moves screened by the surrogate (sadmc_da.cu); stats gets per
-// walker (stage-1 rejections, exact evaluations) added.  One warp per walker.
+// walker (stage-1 rejections, exact evaluations) added.  One warp per walker; max_atoms is
+// the largest cluster of the batch (it sizes each walker's shared-memory descriptors).
 struct SgWeights;
-cudaError_t launch_lj_da(const MoveLaunch& m, const LjSys& s, const SgWeights& w,
+cudaError_t launch_lj_da(const MoveLaunch& m, const LjSys& s, const SgWeights& w, int max_atoms,
                          int refresh_interval, uint64_t* stats, cudaStream_t st);
 
 // 2D Ising.  spins: [walker][L*L] int8, index i + j*L.

@@ -10,6 +10,16 @@ namespace dev {
 __device__ __forceinline__ float rbf_centre(int k) { return 0.8f + (2.2f / 31.0f) * (float)k; }
 
 __device__ __forceinline__ float silu32(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU as z/2 (1 + tanh(z/2)) on the hardware tanh (tanh.approx.f32, absolute error about
+// 2^-11): one special-function operation and an FMA in place of an exponential and an
+// IEEE division.  Used by the delayed-acceptance screen only, whose value decides no
+// move by itself (the exact energy makes every final decision).
+__device__ __forceinline__ float silu_fast(float z) {
+  const float h = 0.5f * z;
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return __fmaf_rn(h, t, h);
+}
 __device__ __forceinline__ float dsilu32(float z) {
   const float s = 1.0f / (1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
@@ -38,8 +48,8 @@ namespace dev {
 
 // Surrogate energies of 16 rows (one warp): A fragments of G from a row-major bf16 tile
 // in shared memory (32 bf16 = 16 words per row), weights in shared memory as in the
-// forward kernel.  Rows g and g+8 of the tile end in ea / eb (in the quad's lane t == 0
-// and the others alike).
+// forward kernel, SiLU in its tanh form (silu_fast).  Rows g and g+8 of the tile end in
+// ea / eb (in the quad's lane t == 0 and the others alike).
 template <int RW>  // 32-bit words between consecutive rows of the tile
 __device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1,
                                       const uint32_t* sW2, const float* sb1, const float* sb2,
@@ -61,8 +71,8 @@ __device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1
 #pragma unroll
     for (int kt = 0; kt < 2; ++kt) mma16816(c, aG[kt], sW1[n * 16 + 8 * kt + t], sW1[n * 16 + 8 * kt + 4 + t]);
     const float bb0 = sb1[8 * j + 2 * t], bb1 = sb1[8 * j + 2 * t + 1];
-    h1[j][0] = silu32(c[0] + bb0); h1[j][1] = silu32(c[1] + bb1);
-    h1[j][2] = silu32(c[2] + bb0); h1[j][3] = silu32(c[3] + bb1);
+    h1[j][0] = silu_fast(c[0] + bb0); h1[j][1] = silu_fast(c[1] + bb1);
+    h1[j][2] = silu_fast(c[2] + bb0); h1[j][3] = silu_fast(c[3] + bb1);
   }
   ea = 0.f;
   eb = 0.f;
@@ -79,8 +89,10 @@ __device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1
     }
     const float bb0 = sb2[8 * j + 2 * t], bb1 = sb2[8 * j + 2 * t + 1];
     const float w0 = sw3[8 * j + 2 * t], w1 = sw3[8 * j + 2 * t + 1];
-    ea += silu32(c[0] + bb0) * w0 + silu32(c[1] + bb1) * w1;
-    eb += silu32(c[2] + bb0) * w0 + silu32(c[3] + bb1) * w1;
+    ea = __fmaf_rn(silu_fast(c[0] + bb0), w0, ea);
+    ea = __fmaf_rn(silu_fast(c[1] + bb1), w1, ea);
+    eb = __fmaf_rn(silu_fast(c[2] + bb0), w0, eb);
+    eb = __fmaf_rn(silu_fast(c[3] + bb1), w1, eb);
   }
   ea += __shfl_xor_sync(0xffffffffu, ea, 1);
   ea += __shfl_xor_sync(0xffffffffu, ea, 2);
