@@ -31,11 +31,14 @@ namespace dev {
 // Shared memory of a block: the weights once, then one region per walker.
 constexpr int DA_WPB = 4;                                  // walkers (warps) per block
 constexpr int DA_W_WORDS = SG_H1 * SG_RBF / 2 + SG_H2 * SG_H1 / 2 + 3 * SG_H1;
-// Per walker, for R descriptor rows (the atoms rounded up to 16, the MLP's row tile):
-// current and proposed FP32 descriptors (rows padded by one word so that 32 lanes on 32
-// rows meet 32 banks), the proposed bf16 copy (17 words a row) and the per-atom energies.
+// Per walker, for R descriptor rows (the atoms rounded up to 16, the MLP's row tile): two
+// FP32 descriptor buffers, current and proposed, whose roles swap when a move is accepted
+// (rows of 36 words: 16-byte aligned for float4, and 8 lanes on 8 rows of one float4 phase
+// meet 32 different banks), the proposed bf16 copy (17 words a row) and two per-atom
+// energy buffers.
+constexpr int DA_GW = SG_RBF + 4;
 __host__ __device__ constexpr int da_rows(int n) { return (n + 15) & ~15; }
-__host__ __device__ constexpr int da_walker_words(int R) { return R * (2 * (SG_RBF + 1) + (SG_RBF + 2) / 2 + 2); }
+__host__ __device__ constexpr int da_walker_words(int R) { return R * (2 * DA_GW + (SG_RBF + 2) / 2 + 2); }
 inline size_t da_smem_bytes(int R) {
   return 4 * ((size_t)DA_W_WORDS + (size_t)DA_WPB * (size_t)da_walker_words(R));
 }
@@ -66,7 +69,7 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32], int lane)
 template <int APL>
 __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys s, SgWeights wts, int R,
                                                              int refresh_interval, uint64_t* stats) {
-  constexpr int GW = SG_RBF + 1;        // FP32 descriptor row stride (words)
+  constexpr int GW = DA_GW;             // FP32 descriptor row stride (words)
   constexpr int BW = (SG_RBF + 2) / 2;  // bf16 descriptor row stride (words)
   extern __shared__ __align__(16) uint32_t da_smem[];
   uint32_t* sW1 = da_smem;
@@ -92,11 +95,11 @@ __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys 
   lj.n = fh.c.n;
   const int n = lj.n;  // <= R, the rows every walker region of the launch holds
   float* sG = reinterpret_cast<float*>(da_smem + DA_W_WORDS + (size_t)wib * da_walker_words(R));
-  float* sGf = sG + R * GW;
+  float* sGf = sG + R * GW;  // sG: current descriptors, sGf: proposed (swapped on acceptance)
   uint32_t* sGbw = reinterpret_cast<uint32_t*>(sGf + R * GW);
   __nv_bfloat16* sGb = reinterpret_cast<__nv_bfloat16*>(sGbw);
   float* sE = reinterpret_cast<float*>(sGbw + R * BW);
-  float* sEn = sE + R;
+  float* sEn = sE + R;       // sE: current per-atom energies, sEn: proposed (swapped too)
   float* pw = s.pos + (size_t)w * 6 * (size_t)s.np;
   lj.load(pw, s.np);
   const float inv2w2 = 1.0f / (2.0f * 0.1f * 0.1f);
@@ -198,15 +201,24 @@ __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys 
         const float ro = sqrtf(dx * dx + dy * dy + dz * dz);
         dx = xi - tx.h; dy = yi - ty.h; dz = zi - tz.h;
         const float rn = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float4* gsrc = reinterpret_cast<const float4*>(sG + i * GW);
+        float4* gdst = reinterpret_cast<float4*>(sGf + i * GW);
 #pragma unroll
-        for (int k = 0; k < SG_RBF; ++k) {
-          const float cn = rbf_centre(k);
-          const float pn = ex2_approx(-((rn - cn) * (rn - cn)) * l2w);
-          const float po = ex2_approx(-((ro - cn) * (ro - cn)) * l2w);
-          const float gnew = sG[i * GW + k] + pn - po;
-          sGf[i * GW + k] = gnew;
-          sGb[i * 2 * BW + k] = __float2bfloat16_rn(gnew);
-          col[k] += pn;
+        for (int k4 = 0; k4 < SG_RBF / 4; ++k4) {
+          const float4 g = gsrc[k4];
+          float o[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int k = 4 * k4 + u;
+            const float cn = rbf_centre(k);
+            const float pn = ex2_approx(-((rn - cn) * (rn - cn)) * l2w);
+            const float po = ex2_approx(-((ro - cn) * (ro - cn)) * l2w);
+            o[u] = (u == 0 ? g.x : u == 1 ? g.y : u == 2 ? g.z : g.w) + pn - po;
+            col[k] += pn;
+          }
+          gdst[k4] = make_float4(o[0], o[1], o[2], o[3]);
+          sGbw[i * BW + 2 * k4] = pack_bf16(o[0], o[1]);
+          sGbw[i * BW + 2 * k4 + 1] = pack_bf16(o[2], o[3]);
         }
       }
     }
@@ -264,17 +276,10 @@ __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys 
       acc = fh.decide_de(possible, de, u_second, rs, true, lnw_first);
       if (acc) {
         lj.put(a, tx, ty, tz);
-#pragma unroll 1
-        for (int q = 0; q < APL; ++q) {
-          const int i = lane + 32 * q;
-          if (i < n && i != a) {
-#pragma unroll
-            for (int k = 0; k < SG_RBF; ++k) sG[i * GW + k] = sGf[i * GW + k];
-          }
-          if (i < n) sE[i] = sEn[i];
-        }
-        sG[a * GW + lane] = ga;  // the moved atom's row, column `lane`
-        __syncwarp();
+        // every row < n of the proposed buffers was rewritten by this move: they become
+        // the current ones
+        float* t0 = sG; sG = sGf; sGf = t0;
+        float* t1 = sE; sE = sEn; sEn = t1;
       }
     }
     fh.finish_move(acc);
