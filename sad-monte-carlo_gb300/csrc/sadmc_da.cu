@@ -30,13 +30,14 @@ namespace dev {
 
 // Shared memory of a block: the weights once, then one region per walker.
 constexpr int DA_WPB = 4;                                  // walkers (warps) per block
-constexpr int DA_W_WORDS = SG_H1 * SG_RBF / 2 + SG_H2 * SG_H1 / 2 + 3 * SG_H1;
+constexpr int DA_W_WORDS = SG_H1 * MLP_S1 + SG_H2 * MLP_S2 + 3 * SG_H1;  // mlp16's layout
 // Per walker, for R descriptor rows (the atoms rounded up to 16, the MLP's row tile): two
 // FP32 descriptor buffers, current and proposed, whose roles swap when a move is accepted
 // (rows of 36 words: 16-byte aligned for float4, and 8 lanes on 8 rows of one float4 phase
 // meet 32 different banks), the proposed bf16 copy (17 words a row) and two per-atom
 // energy buffers.
 constexpr int DA_GW = SG_RBF + 4;
+constexpr int DA_BW = (SG_RBF + 2) / 2;  // bf16 descriptor row stride (words)
 __host__ __device__ constexpr int da_rows(int n) { return (n + 15) & ~15; }
 __host__ __device__ constexpr int da_walker_words(int R) { return R * (2 * DA_GW + (SG_RBF + 2) / 2 + 2); }
 inline size_t da_smem_bytes(int R) {
@@ -66,6 +67,65 @@ __device__ __forceinline__ float warp_reduce_scatter32(float (&v)[32], int lane)
   return v[0];
 }
 
+// Stage-1 update of descriptor row i over columns [kb, kb + KPL): the proposed row, FP32 and
+// bf16, from the current one plus the new-position minus the old-position RBF terms (ro, rn:
+// the atom's old and new distances to the moved atom); the new-position terms are added to acc.
+template <int KPL>
+__device__ __forceinline__ void da_row_update(const float* sG, float* sGf, uint32_t* sGbw, int i, int kb,
+                                              float ro, float rn, float l2w, float (&acc)[KPL]) {
+  const float4* gsrc = reinterpret_cast<const float4*>(sG + i * DA_GW + kb);
+  float4* gdst = reinterpret_cast<float4*>(sGf + i * DA_GW + kb);
+#pragma unroll
+  for (int k4 = 0; k4 < KPL / 4; ++k4) {
+    const float4 g = gsrc[k4];
+    float o[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float cn = rbf_centre(kb + 4 * k4 + u);
+      const float pn = ex2_approx(-((rn - cn) * (rn - cn)) * l2w);
+      const float po = ex2_approx(-((ro - cn) * (ro - cn)) * l2w);
+      o[u] = (u == 0 ? g.x : u == 1 ? g.y : u == 2 ? g.z : g.w) + pn - po;
+      acc[4 * k4 + u] += pn;
+    }
+    gdst[k4] = make_float4(o[0], o[1], o[2], o[3]);
+    sGbw[i * DA_BW + kb / 2 + 2 * k4] = pack_bf16(o[0], o[1]);
+    sGbw[i * DA_BW + kb / 2 + 2 * k4 + 1] = pack_bf16(o[2], o[3]);
+  }
+}
+
+// Stage 1 for the second atom slot (atoms 32 ..) when it holds at most KPL atoms (KPL = 8:
+// N <= 40): 32 / KPL lanes share a row, KPL columns each, so that a few atoms there do not
+// leave most lanes idle.
+// Adds the rows' new-position terms to col (column k of this lane's share).
+template <int KPL, int APL>
+__device__ __forceinline__ void da_slot1_packed(const LjWalker<32, APL>& lj, int lane, int n, int a,
+                                                float fx, float fy, float fz, float tx, float ty,
+                                                float tz, const float* sG, float* sGf, uint32_t* sGbw,
+                                                float l2w, float (&col)[SG_RBF]) {
+  constexpr int P = SG_RBF / KPL;  // lanes per row
+  const int slot = lane / P, part = lane % P;
+  const float xi = __shfl_sync(0xffffffffu, lj.x[APL - 1].h, slot);
+  const float yi = __shfl_sync(0xffffffffu, lj.y[APL - 1].h, slot);
+  const float zi = __shfl_sync(0xffffffffu, lj.z[APL - 1].h, slot);
+  const int i = 32 + slot;
+  if (i < n && i != a) {
+    float dx = xi - fx, dy = yi - fy, dz = zi - fz;
+    const float ro = sqrtf(dx * dx + dy * dy + dz * dz);
+    dx = xi - tx; dy = yi - ty; dz = zi - tz;
+    const float rn = sqrtf(dx * dx + dy * dy + dz * dz);
+    float pk[KPL];
+#pragma unroll
+    for (int j = 0; j < KPL; ++j) pk[j] = 0.f;
+    da_row_update<KPL>(sG, sGf, sGbw, i, part * KPL, ro, rn, l2w, pk);
+#pragma unroll
+    for (int b = 0; b < P; ++b)
+      if (part == b) {
+#pragma unroll
+        for (int j = 0; j < KPL; ++j) col[b * KPL + j] += pk[j];
+      }
+  }
+}
+
 template <int APL>
 __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys s, SgWeights wts, int R,
                                                              int refresh_interval, uint64_t* stats) {
@@ -73,14 +133,14 @@ __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys 
   constexpr int BW = (SG_RBF + 2) / 2;  // bf16 descriptor row stride (words)
   extern __shared__ __align__(16) uint32_t da_smem[];
   uint32_t* sW1 = da_smem;
-  uint32_t* sW2 = sW1 + SG_H1 * SG_RBF / 2;
-  float* sb1 = reinterpret_cast<float*>(sW2 + SG_H2 * SG_H1 / 2);
+  uint32_t* sW2 = sW1 + SG_H1 * MLP_S1;
+  float* sb1 = reinterpret_cast<float*>(sW2 + SG_H2 * MLP_S2);
   float* sb2 = sb1 + SG_H1;
   float* sw3 = sb2 + SG_H2;
   for (int k = threadIdx.x; k < SG_H1 * SG_RBF / 2; k += blockDim.x)
-    sW1[k] = reinterpret_cast<const uint32_t*>(wts.w1t)[k];
+    sW1[mlp_wword(k / (SG_RBF / 2), k % (SG_RBF / 2), MLP_S1)] = reinterpret_cast<const uint32_t*>(wts.w1t)[k];
   for (int k = threadIdx.x; k < SG_H2 * SG_H1 / 2; k += blockDim.x)
-    sW2[k] = reinterpret_cast<const uint32_t*>(wts.w2t)[k];
+    sW2[mlp_wword(k / (SG_H1 / 2), k % (SG_H1 / 2), MLP_S2)] = reinterpret_cast<const uint32_t*>(wts.w2t)[k];
   for (int k = threadIdx.x; k < SG_H1; k += blockDim.x) { sb1[k] = wts.b1[k]; sb2[k] = wts.b2[k]; sw3[k] = wts.w3[k]; }
   __syncthreads();
   const float b3 = wts.b3[0];
@@ -117,7 +177,9 @@ __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys 
   auto forward_rows = [&](float* dst) {
     for (int r0 = 0; r0 < n; r0 += 16) {
       float ea, eb;
-      mlp16<BW>(sGbw + r0 * BW, sW1, sW2, sb1, sb2, sw3, b3, ea, eb);
+      mlp16<BW>(sGbw + r0 * BW, reinterpret_cast<const uint2*>(sW1), reinterpret_cast<const uint2*>(sW2),
+                reinterpret_cast<const float2*>(sb1), reinterpret_cast<const float2*>(sb2),
+                reinterpret_cast<const float2*>(sw3), b3, ea, eb);
       const int g = lane >> 2;
       if ((lane & 3) == 0) {
         dst[r0 + g] = ea;
@@ -191,8 +253,11 @@ __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys 
     float col[SG_RBF];  // this lane's atoms' contributions to the moved atom's row
 #pragma unroll
     for (int k = 0; k < SG_RBF; ++k) col[k] = 0.f;
+    // a lane per row for slot 0, and for slot 1 when it holds more than 8 atoms
+    const int m1 = n - 32;  // atoms in slot 1
+    const int full_slots = (APL > 1 && m1 > 8) ? 2 : 1;
 #pragma unroll 1
-    for (int q = 0; q < APL; ++q) {
+    for (int q = 0; q < full_slots; ++q) {
       const int i = lane + 32 * q;
       if (i < n && i != a) {
         float xi, yi, zi;
@@ -201,27 +266,11 @@ __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys 
         const float ro = sqrtf(dx * dx + dy * dy + dz * dz);
         dx = xi - tx.h; dy = yi - ty.h; dz = zi - tz.h;
         const float rn = sqrtf(dx * dx + dy * dy + dz * dz);
-        const float4* gsrc = reinterpret_cast<const float4*>(sG + i * GW);
-        float4* gdst = reinterpret_cast<float4*>(sGf + i * GW);
-#pragma unroll
-        for (int k4 = 0; k4 < SG_RBF / 4; ++k4) {
-          const float4 g = gsrc[k4];
-          float o[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int k = 4 * k4 + u;
-            const float cn = rbf_centre(k);
-            const float pn = ex2_approx(-((rn - cn) * (rn - cn)) * l2w);
-            const float po = ex2_approx(-((ro - cn) * (ro - cn)) * l2w);
-            o[u] = (u == 0 ? g.x : u == 1 ? g.y : u == 2 ? g.z : g.w) + pn - po;
-            col[k] += pn;
-          }
-          gdst[k4] = make_float4(o[0], o[1], o[2], o[3]);
-          sGbw[i * BW + 2 * k4] = pack_bf16(o[0], o[1]);
-          sGbw[i * BW + 2 * k4 + 1] = pack_bf16(o[2], o[3]);
-        }
+        da_row_update<SG_RBF>(sG, sGf, sGbw, i, 0, ro, rn, l2w, col);
       }
     }
+    if (APL > 1 && m1 > 0 && m1 <= 8)  // group-uniform: n is the walker's
+      da_slot1_packed<8, APL>(lj, lane, n, a, fx.h, fy.h, fz.h, tx.h, ty.h, tz.h, sG, sGf, sGbw, l2w, col);
     // moved atom's row: lane k takes column k of the contributions
     const float ga = warp_reduce_scatter32(col, lane);
     sGf[a * GW + lane] = ga;

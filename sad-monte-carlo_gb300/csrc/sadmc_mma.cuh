@@ -46,14 +46,24 @@ __device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32
 namespace sadmc {
 namespace dev {
 
+// Weight layout of mlp16 in shared memory: for output unit n, the two 32-bit words a lane t
+// of its quad passes to one m16n8k16 as B (K = 16 kt + 2t, 2t + 1 and 16 kt + 8 + 2t, +1) sit
+// side by side, so one 64-bit load fetches them.  Units are MLP_S1 (layer 1) and MLP_S2
+// (layer 2) words apart: the 8 units g of a load meet 32 different banks.
+constexpr int MLP_S1 = 24, MLP_S2 = 40;
+// Word index in that layout of word w (0 .. K/2 - 1) of unit n's row-major bf16 weights.
+__host__ __device__ constexpr int mlp_wword(int n, int w, int stride) {
+  return n * stride + (w >> 3) * 8 + 2 * (w & 3) + ((w >> 2) & 1);
+}
+
 // Surrogate energies of 16 rows (one warp): A fragments of G from a row-major bf16 tile
-// in shared memory (32 bf16 = 16 words per row), weights in shared memory as in the
-// forward kernel, SiLU in its tanh form (silu_fast).  Rows g and g+8 of the tile end in
-// ea / eb (in the quad's lane t == 0 and the others alike).
+// in shared memory (32 bf16 = 16 words per row), weights in the mlp_wword layout and biases
+// as float pairs in shared memory, SiLU in its tanh form (silu_fast).  Rows g and g+8 of
+// the tile end in ea / eb (in the quad's lane t == 0 and the others alike).
 template <int RW>  // 32-bit words between consecutive rows of the tile
-__device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1,
-                                      const uint32_t* sW2, const float* sb1, const float* sb2,
-                                      const float* sw3, float b3, float& ea, float& eb) {
+__device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint2* sW1, const uint2* sW2,
+                                      const float2* sb1, const float2* sb2, const float2* sw3,
+                                      float b3, float& ea, float& eb) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   uint32_t aG[2][4];
 #pragma unroll
@@ -69,10 +79,13 @@ __device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1
     float c[4] = {0.f, 0.f, 0.f, 0.f};
     const int n = 8 * j + g;
 #pragma unroll
-    for (int kt = 0; kt < 2; ++kt) mma16816(c, aG[kt], sW1[n * 16 + 8 * kt + t], sW1[n * 16 + 8 * kt + 4 + t]);
-    const float bb0 = sb1[8 * j + 2 * t], bb1 = sb1[8 * j + 2 * t + 1];
-    h1[j][0] = silu_fast(c[0] + bb0); h1[j][1] = silu_fast(c[1] + bb1);
-    h1[j][2] = silu_fast(c[2] + bb0); h1[j][3] = silu_fast(c[3] + bb1);
+    for (int kt = 0; kt < 2; ++kt) {
+      const uint2 b = sW1[(n * MLP_S1 + 8 * kt + 2 * t) >> 1];
+      mma16816(c, aG[kt], b.x, b.y);
+    }
+    const float2 bb = sb1[4 * j + t];
+    h1[j][0] = silu_fast(c[0] + bb.x); h1[j][1] = silu_fast(c[1] + bb.y);
+    h1[j][2] = silu_fast(c[2] + bb.x); h1[j][3] = silu_fast(c[3] + bb.y);
   }
   ea = 0.f;
   eb = 0.f;
@@ -85,14 +98,15 @@ __device__ __forceinline__ void mlp16(const uint32_t* gtile, const uint32_t* sW1
       const uint32_t a[4] = {pack_bf16(h1[2 * kt][0], h1[2 * kt][1]), pack_bf16(h1[2 * kt][2], h1[2 * kt][3]),
                              pack_bf16(h1[2 * kt + 1][0], h1[2 * kt + 1][1]),
                              pack_bf16(h1[2 * kt + 1][2], h1[2 * kt + 1][3])};
-      mma16816(c, a, sW2[n * 32 + 8 * kt + t], sW2[n * 32 + 8 * kt + 4 + t]);
+      const uint2 b = sW2[(n * MLP_S2 + 8 * kt + 2 * t) >> 1];
+      mma16816(c, a, b.x, b.y);
     }
-    const float bb0 = sb2[8 * j + 2 * t], bb1 = sb2[8 * j + 2 * t + 1];
-    const float w0 = sw3[8 * j + 2 * t], w1 = sw3[8 * j + 2 * t + 1];
-    ea = __fmaf_rn(silu_fast(c[0] + bb0), w0, ea);
-    ea = __fmaf_rn(silu_fast(c[1] + bb1), w1, ea);
-    eb = __fmaf_rn(silu_fast(c[2] + bb0), w0, eb);
-    eb = __fmaf_rn(silu_fast(c[3] + bb1), w1, eb);
+    const float2 bb = sb2[4 * j + t];
+    const float2 ww = sw3[4 * j + t];
+    ea = __fmaf_rn(silu_fast(c[0] + bb.x), ww.x, ea);
+    ea = __fmaf_rn(silu_fast(c[1] + bb.y), ww.y, ea);
+    eb = __fmaf_rn(silu_fast(c[2] + bb.x), ww.x, eb);
+    eb = __fmaf_rn(silu_fast(c[3] + bb.y), ww.y, eb);
   }
   ea += __shfl_xor_sync(0xffffffffu, ea, 1);
   ea += __shfl_xor_sync(0xffffffffu, ea, 2);

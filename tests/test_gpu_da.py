@@ -99,18 +99,24 @@ def test_trained_surrogate_keeps_the_distribution_at_fixed_weights(gpu, oracle, 
     assert tv < 0.05, tv
 
 
-@pytest.mark.parametrize("method", [0, 2])
-def test_da_trace_replay(gpu, oracle, method):
+# (atoms, sphere radius, lowest energy bin): one atom slot per lane (13); two slots with
+# the second one's few atoms spread over the lanes (38); two full slots (50)
+CLUSTERS = {13: (2.5, -80.0), 38: (3.5, -180.0), 50: (4.0, -250.0)}
+
+
+@pytest.mark.parametrize("method,n", [(0, 13), (2, 13), (0, 38)])
+def test_da_trace_replay(gpu, oracle, method, n):
     """A traced run (plain moves, surrogate training, then delayed-acceptance moves)
     replayed by the FP64 oracle from the GPU's proposed energies and surrogate changes dS:
     the oracle takes both stages' decisions itself (the screen from its own ln w, the
     second stage with the reverse screen), so every screen, acceptance, bin and counter
     must be the GPU's."""
-    n, W, R, seed, plain_moves, da_moves = 13, 8, 2.5, 6, 3000, 6000
+    W, seed, plain_moves, da_moves = 8, 6, 3000, 6000
+    R, e_lo = CLUSTERS[n]
     confs = lj_configs(oracle, n, R, range(700, 700 + W))
     kw = dict(method=method, min_T=0.1, energy_bin=0.1, max_allowed=0.0, target_rate=0.5,
               translation_scale=0.1, seed=seed)
-    b = gpu.Batch(gpu.make_config(gpu.LJ, W, n, e_lo=-80, e_hi=1, lanes_per_walker=32, **kw),
+    b = gpu.Batch(gpu.make_config(gpu.LJ, W, n, e_lo=e_lo, e_hi=1, lanes_per_walker=32, **kw),
                   [(n, R, (0, 0, 0))] * W)
     b.upload(confs)
     b.initialize()
@@ -136,7 +142,61 @@ def test_da_trace_replay(gpu, oracle, method):
         d2, m2 = ow.run_override_da(e1[plain_moves:], e2[plain_moves:], ds[plain_moves:])
         assert m1 == 0 and m2 == 0, (w, m1, m2)
         assert max(d1, d2) < 2e-5, (w, d1, d2)
-        label = f"da method {method} walker {w}"
+        label = f"da method {method} n {n} walker {w}"
         assert_bins_equal(b.bins(w), ow.bins(), label=label)
         assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
+
+
+@pytest.mark.parametrize("n", [38, 50])
+def test_da_screen_matches_the_mlp_statement(gpu, oracle, n):
+    """The screen's surrogate change dS of every accepted delayed-acceptance move against the
+    FP64 statement of the MLP (BF16 rounding emulated) on fresh descriptors of the
+    configurations before and after the move, which the oracle replays from the trace.  The
+    kernel keeps descriptors incrementally and per-atom energies of the current
+    configuration, so this checks every row and column of the incremental update, the moved
+    atom's row and the MLP on all row tiles: 38 atoms take the second atom slot's few rows
+    spread over the lanes, 50 atoms a lane per row.  Tolerance per move 0.02 (the tanh form
+    of SiLU, about 2^-11 per unit, and BF16 roundings it flips; observed below 0.005), and
+    the errors may not add up (their sum within 0.05)."""
+    import mlp_oracle as M
+    W, seed, plain_moves, da_moves = 2, 3, 2000, 1500
+    R, e_lo = CLUSTERS[n]
+    confs = lj_configs(oracle, n, R, range(900, 900 + W))
+    kw = dict(method=0, min_T=0.1, energy_bin=0.2, max_allowed=0.0, target_rate=0.5,
+              translation_scale=0.1, seed=seed)
+    b = gpu.Batch(gpu.make_config(gpu.LJ, W, n, e_lo=e_lo, e_hi=1, lanes_per_walker=32, **kw),
+                  [(n, R, (0, 0, 0))] * W)
+    b.upload(confs)
+    b.initialize()
+    E0 = b.energies()
+    total = plain_moves + da_moves
+    b.set_trace(total)
+    b.surrogate_init(seed=2, ring_capacity=8192)
+    for _ in range(4):
+        b.run(plain_moves // 4)
+        b.surrogate_collect()
+    b.surrogate_train(200, batch=128, lr=2e-3, seed=4)
+    p = gpu.unpack_params(b.surrogate_params())
+    es = lambda pos: float(M.forward(M.descriptors(pos), p, emulate_bf16=True)[0].sum())
+    x_before = [b.state(w) for w in range(W)]
+    b.run_da(da_moves, refresh_interval=1 << 30)  # one launch: descriptors built once
+    for w in range(W):
+        e1, e2 = b.trace(w, total)
+        ds = b.trace_ds(w, total).astype(np.float64)
+        ow = oracle.Walker(oracle.make_config(oracle.LJ, n, radius=R, walker=w, e0=float(E0[w]),
+                                              **kw), confs[w])
+        ow.run_override(e1[:plain_moves], e2[:plain_moves])
+        np.testing.assert_allclose(x_before[w], ow.state(), atol=1e-11)
+        err = []
+        for t in range(plain_moves, total):
+            x0 = ow.state().copy()
+            ow.run_override_da(e1[t:t + 1], e2[t:t + 1], ds[t:t + 1])
+            x1 = ow.state()
+            if np.any(x1 != x0):
+                err.append(ds[t] - (es(x1) - es(x0)))
+        err = np.array(err)
+        assert len(err) > da_moves // 10, len(err)
+        assert np.abs(err).max() < 0.02, (w, np.abs(err).max())
+        assert abs(err.sum()) < 0.05, (w, err.sum())
         np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
