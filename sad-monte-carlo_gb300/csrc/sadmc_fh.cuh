@@ -387,7 +387,7 @@ struct Fh {
     int g;
     if (e < c.cur_min) g = c.b_lo - 1;
     else if (e >= cur_max) g = c.b_hi + 1;
-    else g = gidx_exact(e);
+    else g = gidx(e);  // the FP32-estimate index, identical to gidx_exact's
     if (kind() == M_SAD) {
       if (e < c.too_lo) return ld_lnw(win_lo) + div_by(e - c.too_lo, c.min_T, inv_minT);
       if (e > c.too_hi) return ld_lnw(win_hi);
