@@ -19,7 +19,6 @@ import argparse
 import json
 import math
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -141,6 +140,13 @@ def _roof(achieved, peak, unit, note):
     return {"achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak, "note": note}
 
 
+def status_summary(b, ignore=0):
+    """Walkers whose device status word is set after a run, and the bits seen."""
+    st = b.status() & ~np.uint32(ignore)
+    bits = int(np.bitwise_or.reduce(st)) if len(st) else 0
+    return {"walkers_with_status": int((st != 0).sum()), "status_bits": bits}
+
+
 def candidates(n, L, r_cut):
     """C = 27 N / n_c^3 - 1 candidate partners of a query, n_c = floor(L / r_cut)."""
     nc = np.floor(np.asarray(L) / r_cut)
@@ -161,10 +167,12 @@ def case_c1(G, seed=11, moves=1_000_000, lpw=0, **_):
     b.initialize()
     lanes = _lanes(b, lpw, 20000)
     sec = _time_run(b, moves, 100_000)
+    flagged = int((b.status() != 0).sum())
     b.close()
     rate = moves / sec
     return {"workload": "Ising 32x32, plain SAD (min_T 0.2), 1 walker", "moves": moves,
             "moves_per_s": rate, "ns_per_move": 1e9 * sec / moves, "lanes_per_walker": lanes,
+            "walkers_with_status": flagged,
             "roofline": _roof(48 * rate / 1e9, SMEM_SM_PEAK / 1e9, "GB/s",
                               "48 B of shared-memory traffic per move against one SM's "
                               "port; not meaningful for one serial walker")}
@@ -182,10 +190,11 @@ def case_c1_batch(G, seed=11, walkers=4096, moves=20000, lpw=0):
     b.initialize()
     lanes = _lanes(b, lpw, 2000)
     sec = _time_run(b, moves, 4000)
+    flagged = int((b.status() != 0).sum())
     b.close()
     return {"workload": f"Ising 32x32, plain SAD (min_T 0.2), {walkers} independent walkers",
             "moves": walkers * moves, "moves_per_s": walkers * moves / sec,
-            "lanes_per_walker": lanes}
+            "lanes_per_walker": lanes, "walkers_with_status": flagged}
 
 
 def case_c3(G, seed=11, walkers=2048, moves=2048, lpw=0):
@@ -200,6 +209,7 @@ def case_c3(G, seed=11, walkers=2048, moves=2048, lpw=0):
     b.initialize()
     lanes = _lanes(b, lpw, 256)
     sec = _time_run(b, moves, 512)
+    flagged = status_summary(b)
     b.close()
     rate = walkers * moves / sec
     flop = float(np.mean(2 * 15 * candidates([n for n, _, _ in inp], [Lb for _, Lb, _ in inp],
@@ -207,6 +217,7 @@ def case_c3(G, seed=11, walkers=2048, moves=2048, lpw=0):
     return {"workload": f"WCA, N in {{64,128,256,512}}, density U[0.6,0.9], {walkers} walkers, "
                         "SAMC t0=1e4, 500 bins over [0,500)",
             "moves": walkers * moves, "moves_per_s": rate, "lanes_per_walker": lanes,
+            **flagged,
             "roofline": _roof(rate * flop / 1e12, FP32_PEAK / 1e12, "TFLOP/s",
                               f"2 C x 15 FP32 FLOP per move, C = 27 N / n_c^3 - 1 per walker "
                               f"(mean {flop:.0f} FLOP)")}
@@ -223,12 +234,14 @@ def case_c5(G, seed=11, walkers=1024, moves=2048, lpw=0):
     b.initialize()
     lanes = _lanes(b, lpw, 256)
     sec = _time_run(b, moves, 512)
+    flagged = status_summary(b)
     b.close()
     rate = walkers * moves / sec
     flop = float(np.mean(2 * 8 * candidates(1024, [Lb for Lb, _ in inp], 1.3)))
     return {"workload": f"hard-core square well lambda=1.3, N=1024, packing U[0.30,0.50], "
                         f"jittered FCC, WL on contact bins, {walkers} walkers",
             "moves": walkers * moves, "moves_per_s": rate, "lanes_per_walker": lanes,
+            **flagged,
             "roofline": _roof(rate * flop / 1e12, FP64_PEAK / 1e12, "TFLOP/s",
                               f"2 C x 8 FP64 FLOP per move (C = 27 N / n_c^3 - 1, mean {flop:.0f} "
                               "FLOP) against the FP64 peak; the kernel decides most pairs with "
@@ -436,17 +449,17 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def profile_value(key):
-    """A figure (`key: value` line) of the committed ncu summary of the move kernel."""
-    path = os.path.join(REPO, "profiles", "lj_move_kernel_lj31_4096w.md")
-    if not os.path.exists(path):
+def profile_value(key, kernel="lj_move_kernel_lj31_4096w"):
+    """A figure of the last ncu capture of a kernel (profiles/ncu_figures.json, written
+    from the capture that the summary of the same name describes), if present."""
+    try:
+        return json.load(open(os.path.join(REPO, "profiles", "ncu_figures.json")))[kernel].get(key)
+    except (OSError, ValueError, KeyError):
         return None
-    m = re.search(key + r":\s*([0-9.eE+]+)", open(path).read())
-    return float(m.group(1)) if m else None
 
 
 def profile_traffic():
-    """DRAM bytes per move-kernel launch from the committed ncu summary, if present."""
+    """DRAM bytes per move-kernel launch from the last ncu capture, if present."""
     return profile_value("traffic_bytes_per_launch")
 
 
@@ -634,7 +647,7 @@ def run_gpu(args):
                          "traffic": traffic,
                          "limiter": {"fp64_pipe_active": profile_value("fp64_pipe_active_frac"),
                                      "issue_active": profile_value("issue_active_frac"),
-                                     "source": "ncu, profiles/lj_move_kernel_lj31_4096w.md"},
+                                     "source": "ncu capture summarised in profiles/lj_move_kernel_lj31_4096w.md"},
                          "note": "30(N-1) FLOP/move algorithmic; peak = 152 SM x 128 FFMA x 2 x "
                                  "max SM clock (FP32 issue, not in MEASURED_PEAKS.json); the "
                                  "kernel is bound by the FP64 pipe and the latency of the per-move "

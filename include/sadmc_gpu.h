@@ -237,6 +237,27 @@ int32_t sadmc_surrogate_loss_grads_noalloc(sadmc_handle* h, const float* pos,
  * per walker the running totals (stage-1 rejections, exact evaluations). */
 int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, uint64_t* stats);
 
+/* Online training schedule of sadmc_run_online (no counterpart in the reference). */
+typedef struct sadmc_online {
+  uint64_t collect_interval;  /* moves between appends of every walker to the ring (0: never) */
+  uint64_t retrain_interval;  /* moves between training rounds (0: never) */
+  int32_t train_steps;        /* Adam steps per round */
+  int32_t batch;              /* ring configurations per step */
+  float lr;
+  int32_t pad;
+  uint64_t seed;              /* minibatch draws (hashed with the move count) */
+} sadmc_online;
+/* `moves` moves of every walker, plain (delayed = 0, as sadmc_run) or delayed-acceptance
+ * (delayed = 1, as sadmc_run_da), while the surrogate is trained online: every
+ * collect_interval moves each walker's configuration and exact energy join the training
+ * ring, every retrain_interval moves train_steps Adam steps run on minibatches drawn from
+ * it.  The schedule counts the handle's moves since sadmc_initialize, so consecutive calls
+ * continue it.  Everything runs on the device, stream-ordered, without host round trips;
+ * the call synchronises once at the end.  stats as for sadmc_run_da (delayed only).
+ * No counterpart in the reference (the learned part is this library's). */
+int32_t sadmc_run_online(sadmc_handle* h, uint64_t moves, int32_t delayed, int32_t refresh_interval,
+                         const sadmc_online* o, uint64_t* stats);
+
 /* Surrogate energies of caller configurations (host arrays). */
 int32_t sadmc_surrogate_predict(sadmc_handle* h, const float* pos, int32_t configs,
                                 float* energies);
@@ -260,6 +281,14 @@ int32_t sadmc_draws(int32_t system, uint32_t n, uint64_t seed, uint32_t walker, 
  * device (plotting/final_heat_capacity.py:79-88).  Host arrays. */
 int32_t sadmc_heat_capacity(const double* T, int32_t nT, const double* E, const double* S,
                             int32_t n, double* C);
+
+/* Heat capacity of every walker from its own bins, FP64 on the device: C[w * nT + t] =
+ * heat_capacity(T[t], E, S) (plotting/final_heat_capacity.py:79-88) over the walker's
+ * visited bins, with S the entropy estimate plotting/parse-binning.py:136-160 forms from
+ * ln w (SAD: extended below too_lo with slope 1/min_T and above too_hi flat, both
+ * corrected by ln(hist / mean hist over the window); Wang-Landau production: plus ln of
+ * the production histogram).  Host arrays; C has n_walkers * nT entries. */
+int32_t sadmc_walker_heat_capacity(sadmc_handle* h, const double* T, int32_t nT, double* C);
 
 /* ---- Grand-canonical systems with the energy-number method ------------------------
  * EnergyNumberMC<S> (src/mc/energy_number.rs) for the LJ cluster (GrandSystem of

@@ -97,8 +97,22 @@ struct EnergyMC {
   std::vector<uint64_t> round_trips;
   double max_S = 0;
   size_t max_S_index = 0;
-  // random source and diagnostics
+  // random source and diagnostics.  The move loop takes its draws straight from the
+  // Philox stream (seed, walker) of the system kind (no indirect call in the timed loop);
+  // `draw`, when set, replaces it (tests that inject their own stream).
   std::function<Draws(uint64_t)> draw;
+  bool philox_ising = false;
+  uint64_t philox_seed = 0;
+  uint32_t philox_walker = 0, philox_n = 0;
+  bool philox_set = false;
+  Draws next_draws(uint64_t t) const {
+    if (philox_set) return philox_ising ? draws_ising(philox_seed, philox_walker, t, philox_n, 0)
+                                        : draws_continuous(philox_seed, philox_walker, t, philox_n, 0);
+    return draw(t);
+  }
+  void use_philox(uint64_t seed, uint32_t walker, uint32_t n, bool ising) {
+    philox_seed = seed; philox_walker = walker; philox_n = n; philox_ising = ising; philox_set = true;
+  }
   uint64_t verify_failures = 0;
   bool nan_gamma = false;
   // Trace replay: when set, move k starts from the caller's energy e1[k] (the GPU's
@@ -423,7 +437,7 @@ struct EnergyMC {
     double e1 = sys.energy();
     double recent_scale = std::sqrt(1.0 / (double)moves);
     acceptance_rate *= 1. - recent_scale;
-    Draws d = draw(moves);
+    Draws d = next_draws(moves);
     // delayed acceptance (sadmc_da.cu): stage 1 screens with E~ = E + dS
     double lnw_first = 0.0;
     bool use_first = false;

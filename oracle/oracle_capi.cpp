@@ -123,6 +123,7 @@ void* orc_create(const orc_config* c, const double* state) {
     h->ising->init(std::move(s), p, [seed, walker, L](uint64_t t, uint32_t stream) {
       return draws_ising(seed, walker, t, L, stream);
     }, dl);
+    h->ising->use_philox(seed, walker, L, true);
   } else {
     uint32_t n = (uint32_t)c->n;
     auto src = [seed, walker, n](uint64_t t, uint32_t stream) {
@@ -137,18 +138,21 @@ void* orc_create(const orc_config* c, const double* state) {
       s.E = s.compute_energy();
       h->lj.reset(new EnergyMC<Lj>());
       h->lj->init(std::move(s), p, src, dl);
+      h->lj->use_philox(seed, walker, n, false);
     } else if (c->system == 2) {
       Wca s;
       s.cell = make_cell(c->box, wca_r_cutoff(), state, c->n);
       s.E = s.compute_energy();
       h->wca.reset(new EnergyMC<Wca>());
       h->wca->init(std::move(s), p, src, dl);
+      h->wca->use_philox(seed, walker, n, false);
     } else {
       SquareWell s;
       s.cell = make_cell(c->box, c->well_width, state, c->n);
       s.E = s.compute_energy();
       h->sw.reset(new EnergyMC<SquareWell>());
       h->sw->init(std::move(s), p, src, dl);
+      h->sw->use_philox(seed, walker, n, false);
     }
   }
   return h;

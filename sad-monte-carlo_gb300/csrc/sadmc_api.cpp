@@ -114,18 +114,19 @@ struct sadmc_handle {
   size_t sg_scratch_rows = 0;
   float* sg_batch_pos = nullptr;                // gathered minibatch
   float* sg_batch_e = nullptr;
-  int* sg_idx = nullptr;
   int sg_batch_cap = 0;
   double* sg_loss = nullptr;
+  unsigned int* sg_flag = nullptr;              // the timeout flag, read and cleared
   uint64_t* sg_stats = nullptr;                 // [W][2] delayed-acceptance counters
   SgWeights sg_weights() const { return SgWeights::from(sg_master, sg_w1t, sg_w2t, sg_wc); }
+  SgAdam sg_adam(int step, float lr) const { return SgAdam{sg_master, sg_m, sg_v, step, lr}; }
   void free_surrogate() {
     cudaFree(sg_master); cudaFree(sg_grad); cudaFree(sg_m); cudaFree(sg_v); cudaFree(sg_w1t);
     cudaFree(sg_w2t); cudaFree(sg_wc); cudaFree(sg_ring_pos); cudaFree(sg_ring_e); cudaFree(sg_scratch);
-    cudaFree(sg_batch_pos); cudaFree(sg_batch_e); cudaFree(sg_idx); cudaFree(sg_loss); cudaFree(sg_stats);
+    cudaFree(sg_batch_pos); cudaFree(sg_batch_e); cudaFree(sg_loss); cudaFree(sg_flag); cudaFree(sg_stats);
     sg_stats = nullptr;
     sg_master = sg_grad = sg_m = sg_v = sg_ring_pos = sg_ring_e = sg_batch_pos = sg_batch_e = nullptr;
-    sg_w1t = sg_w2t = sg_wc = nullptr; sg_scratch = nullptr; sg_idx = nullptr; sg_loss = nullptr;
+    sg_w1t = sg_w2t = sg_wc = nullptr; sg_scratch = nullptr; sg_loss = nullptr; sg_flag = nullptr;
   }
   // scratch for `rows` rows and a gathered batch of `configs` configurations
   cudaError_t sg_reserve(size_t rows, int configs) {
@@ -137,11 +138,10 @@ struct sadmc_handle {
       sg_scratch_rows = e == cudaSuccess ? rows : 0;
     }
     if (e == cudaSuccess && configs > sg_batch_cap) {
-      cudaFree(sg_batch_pos); cudaFree(sg_batch_e); cudaFree(sg_idx);
-      sg_batch_pos = nullptr; sg_batch_e = nullptr; sg_idx = nullptr;
+      cudaFree(sg_batch_pos); cudaFree(sg_batch_e);
+      sg_batch_pos = nullptr; sg_batch_e = nullptr;
       e = cudaMalloc(&sg_batch_pos, sizeof(float) * 3 * (size_t)configs * geom[0].n);
       if (e == cudaSuccess) e = cudaMalloc(&sg_batch_e, sizeof(float) * configs);
-      if (e == cudaSuccess) e = cudaMalloc(&sg_idx, sizeof(int) * configs);
       sg_batch_cap = e == cudaSuccess ? configs : 0;
     }
     return e;
@@ -1144,6 +1144,8 @@ int32_t sadmc_surrogate_init(sadmc_handle* h, uint64_t seed, int32_t ring_capaci
   if (h->cfg.system != SADMC_LJ) return fail(SADMC_ERR_INVALID, "the surrogate is for LJ clusters");
   for (int w = 1; w < h->W; ++w)
     if (h->geom[w].n != h->geom[0].n) return fail(SADMC_ERR_INVALID, "surrogate needs walkers of equal N");
+  if (h->geom[0].n > SG_MAX_ATOMS)
+    return fail(SADMC_ERR_INVALID, "the surrogate supports clusters of up to " + std::to_string(SG_MAX_ATOMS) + " atoms");
   if (ring_capacity <= 0) return fail(SADMC_ERR_INVALID, "ring_capacity must be positive");
   h->free_surrogate();
   const int n = h->geom[0].n;
@@ -1157,6 +1159,7 @@ int32_t sadmc_surrogate_init(sadmc_handle* h, uint64_t seed, int32_t ring_capaci
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_ring_pos, sizeof(float) * 3 * (size_t)n * ring_capacity);
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_ring_e, sizeof(float) * ring_capacity);
   if (e == cudaSuccess) e = cudaMalloc(&h->sg_loss, sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->sg_flag, sizeof(unsigned int));
   if (e != cudaSuccess) { h->free_surrogate(); return fail(SADMC_ERR_NOMEM, "surrogate allocation failed"); }
   // N(0, 1/fan_in) weights, zero biases (a splitmix/Box-Muller host generator)
   std::vector<float> p(SG_NPARAM, 0.0f);
@@ -1181,6 +1184,7 @@ int32_t sadmc_surrogate_init(sadmc_handle* h, uint64_t seed, int32_t ring_capaci
 int32_t sadmc_surrogate_set_params(sadmc_handle* h, const float* params) {
   if (!h || !params) return fail(SADMC_ERR_INVALID, "null argument");
   if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
   CUDA_TRY(cudaMemcpy(h->sg_master, params, sizeof(float) * SG_NPARAM, cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemset(h->sg_m, 0, sizeof(float) * SG_NPARAM));
   CUDA_TRY(cudaMemset(h->sg_v, 0, sizeof(float) * SG_NPARAM));
@@ -1198,21 +1202,60 @@ int32_t sadmc_surrogate_get_params(sadmc_handle* h, float* params) {
   return SADMC_OK;
 }
 
+namespace {
+
+// Append every walker's configuration and energy to the training ring (stream-ordered,
+// no host synchronisation: the energies are read from the walker state on the device).
+cudaError_t sg_collect_async(sadmc_handle* h) {
+  const int take = std::min(h->W, h->sg_cap);
+  cudaError_t e = sg_collect(h->d_pos, h->np, h->geom[0].n, h->d_cores, take, h->sg_ring_pos, h->sg_ring_e,
+                             h->sg_cap, h->sg_head, h->stream);
+  if (e == cudaSuccess) {
+    h->sg_head = (h->sg_head + take) % h->sg_cap;
+    h->sg_count = std::min(h->sg_cap, h->sg_count + take);
+  }
+  return e;
+}
+
+// `steps` Adam steps on minibatches of `batch` ring configurations (stream-ordered).
+cudaError_t sg_train_async(sadmc_handle* h, int steps, int batch, float lr, uint64_t seed) {
+  const int n = h->geom[0].n;
+  cudaError_t e = h->sg_reserve((size_t)batch * n, batch);
+  if (e != cudaSuccess) return e;
+  const SgScratch sc = SgScratch::carve(h->sg_scratch, (size_t)batch * n);
+  unsigned int* flag = nullptr;
+  e = sg_timeout_flag(&flag);
+  for (int it = 0; it < steps && e == cudaSuccess; ++it) {
+    e = sg_gather(h->sg_ring_pos, h->sg_ring_e, n, h->sg_count, seed, (uint64_t)it, batch, h->sg_batch_pos,
+                  h->sg_batch_e, h->stream);
+    h->sg_step += 1;
+    if (e == cudaSuccess)
+      e = sg_train_step(h->sg_batch_pos, h->sg_batch_e, batch, n, h->sg_weights(), h->sg_grad,
+                        h->sg_adam(h->sg_step, lr), sc, h->sg_loss, flag, h->stream);
+  }
+  return e;
+}
+
+// Synchronise the handle's stream and report (then clear) a tensor-core wait that ran out.
+int32_t sg_check_timeouts(sadmc_handle* h) {
+  unsigned int* flag = nullptr;
+  CUDA_TRY(sg_timeout_flag(&flag));
+  CUDA_TRY(sg_take_flag(flag, h->sg_flag, h->stream));
+  unsigned int to = 0;
+  CUDA_TRY(cudaMemcpyAsync(&to, h->sg_flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (to) return fail(SADMC_ERR_CUDA, "a tensor-core wait of the surrogate ran out");
+  return SADMC_OK;
+}
+
+}  // namespace
+
 int32_t sadmc_surrogate_collect(sadmc_handle* h, int32_t* ring_count) {
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
   if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
   if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
-  int32_t r = h->pull_cores();
-  if (r) return r;
-  std::vector<double> E(h->W);
-  for (int w = 0; w < h->W; ++w) E[w] = h->h_cores[w].E;
-  CUDA_TRY(cudaMemcpyAsync(h->d_tmp, E.data(), sizeof(double) * h->W, cudaMemcpyHostToDevice, h->stream));
-  const int take = std::min(h->W, h->sg_cap);
-  CUDA_TRY(sg_collect(h->d_pos, h->np, h->geom[0].n, h->d_tmp, take, h->sg_ring_pos, h->sg_ring_e,
-                      h->sg_cap, h->sg_head, h->stream));
+  CUDA_TRY(sg_collect_async(h));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
-  h->sg_head = (h->sg_head + take) % h->sg_cap;
-  h->sg_count = std::min(h->sg_cap, h->sg_count + take);
   if (ring_count) *ring_count = h->sg_count;
   return SADMC_OK;
 }
@@ -1223,30 +1266,11 @@ int32_t sadmc_surrogate_train(sadmc_handle* h, int32_t steps, int32_t batch, flo
   if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
   if (h->sg_count == 0) return fail(SADMC_ERR_STATE, "the training ring is empty");
   if (steps <= 0 || batch <= 0) return fail(SADMC_ERR_INVALID, "steps and batch must be positive");
-  const int n = h->geom[0].n;
-  CUDA_TRY(h->sg_reserve((size_t)batch * n, batch));
-  const SgScratch sc = SgScratch::carve(h->sg_scratch, (size_t)batch * n);
-  std::vector<int> idx(batch);
-  uint64_t s = seed ^ 0xD1B54A32D192ED03ull;
-  for (int it = 0; it < steps; ++it) {
-    for (int b = 0; b < batch; ++b) {
-      s = s * 6364136223846793005ull + 1442695040888963407ull;
-      idx[b] = (int)((s >> 33) % (uint64_t)h->sg_count);
-    }
-    CUDA_TRY(cudaMemcpyAsync(h->sg_idx, idx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, h->stream));
-    CUDA_TRY(sg_gather(h->sg_ring_pos, h->sg_ring_e, n, h->sg_idx, batch, h->sg_batch_pos, h->sg_batch_e, h->stream));
-    h->sg_step += 1;
-    CUDA_TRY(sg_train_step(h->sg_batch_pos, h->sg_batch_e, batch, n, h->sg_weights(), h->sg_master,
-                           h->sg_grad, h->sg_m, h->sg_v, h->sg_step, lr, sc, h->sg_loss, h->stream));
-  }
+  CUDA_TRY(sg_train_async(h, steps, batch, lr, seed));
   double l = 0;
   CUDA_TRY(cudaMemcpyAsync(&l, h->sg_loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
-  {
-    unsigned int to = 0;
-    CUDA_TRY(sg_forward_timeouts(&to, h->stream));
-    if (to) return fail(SADMC_ERR_CUDA, "a tensor-core wait of the surrogate forward ran out");
-  }
+  int32_t r = sg_check_timeouts(h);
+  if (r) return r;
   if (loss) *loss = l;
   return SADMC_OK;
 }
@@ -1258,19 +1282,17 @@ int32_t sadmc_surrogate_loss_grads(sadmc_handle* h, const float* pos, const floa
   const int n = h->geom[0].n;
   CUDA_TRY(h->sg_reserve((size_t)configs * n, configs));
   const SgScratch sc = SgScratch::carve(h->sg_scratch, (size_t)configs * n);
+  unsigned int* flag = nullptr;
+  CUDA_TRY(sg_timeout_flag(&flag));
   CUDA_TRY(cudaMemcpyAsync(h->sg_batch_pos, pos, sizeof(float) * 3 * (size_t)configs * n, cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(cudaMemcpyAsync(h->sg_batch_e, target, sizeof(float) * configs, cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(sg_train_step(h->sg_batch_pos, h->sg_batch_e, configs, n, h->sg_weights(), h->sg_master,
-                         h->sg_grad, h->sg_m, h->sg_v, 0, 0.0f, sc, h->sg_loss, h->stream));
+  CUDA_TRY(sg_train_step(h->sg_batch_pos, h->sg_batch_e, configs, n, h->sg_weights(), h->sg_grad,
+                         h->sg_adam(0, 0.0f), sc, h->sg_loss, flag, h->stream));
   double l = 0;
   CUDA_TRY(cudaMemcpyAsync(&l, h->sg_loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (grads) CUDA_TRY(cudaMemcpyAsync(grads, h->sg_grad, sizeof(float) * SG_NPARAM, cudaMemcpyDeviceToHost, h->stream));
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
-  {
-    unsigned int to = 0;
-    CUDA_TRY(sg_forward_timeouts(&to, h->stream));
-    if (to) return fail(SADMC_ERR_CUDA, "a tensor-core wait of the surrogate forward ran out");
-  }
+  int32_t r = sg_check_timeouts(h);
+  if (r) return r;
   if (loss) *loss = l;
   return SADMC_OK;
 }
@@ -1289,13 +1311,31 @@ int32_t sadmc_surrogate_loss_grads_noalloc(sadmc_handle* h, const float* pos, co
   CUDA_TRY(sg_static_scratch(&base));
   const SgScratch sc = SgScratch::carve(base, rows);
   const cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
-  // step 0: loss (zeroed first) and gradients only, no optimizer state touched
-  CUDA_TRY(sg_train_step(pos, target, configs, h->geom[0].n, h->sg_weights(), h->sg_master,
-                         grads, nullptr, nullptr, 0, 0.0f, sc, loss, st));
+  // gradients only, no optimizer state touched; no timeout flag: a tensor-core wait that
+  // ran out leaves NaN in the loss and the gradients, the only signal of this path
+  CUDA_TRY(sg_train_step(pos, target, configs, h->geom[0].n, h->sg_weights(), grads, h->sg_adam(0, 0.0f),
+                         sc, loss, nullptr, st));
   return SADMC_OK;
 }
 
-int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, uint64_t* stats) {
+namespace {
+
+// `moves` delayed-acceptance moves of every walker, in launches of at most 8192.
+cudaError_t launch_da_chunks(sadmc_handle* h, uint64_t moves, int32_t refresh_interval) {
+  MoveLaunch m = h->base_launch();  // traced like sadmc_run, with dS in the second record
+  int max_atoms = 0;
+  for (const auto& g : h->geom) max_atoms = std::max(max_atoms, (int)g.n);
+  cudaError_t e = cudaSuccess;
+  for (uint64_t left = moves; left > 0 && e == cudaSuccess;) {
+    m.n_moves = std::min<uint64_t>(left, 8192);
+    e = launch_lj_da(m, LjSys{h->d_pos, h->np, h->radius2()}, h->sg_weights(), max_atoms, refresh_interval,
+                     h->sg_stats, h->stream);
+    left -= m.n_moves;
+  }
+  return e;
+}
+
+int32_t da_checks(sadmc_handle* h) {
   if (!h) return fail(SADMC_ERR_INVALID, "null handle");
   if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
   if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
@@ -1305,19 +1345,52 @@ int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, 
     CUDA_TRY(cudaMalloc(&h->sg_stats, sizeof(uint64_t) * 2 * h->W));
     CUDA_TRY(cudaMemset(h->sg_stats, 0, sizeof(uint64_t) * 2 * h->W));
   }
-  MoveLaunch m = h->base_launch();  // traced like sadmc_run, with dS in the second record
-  int max_atoms = 0;
-  for (const auto& g : h->geom) max_atoms = std::max(max_atoms, (int)g.n);
-  for (uint64_t left = moves; left > 0;) {
-    m.n_moves = std::min<uint64_t>(left, 8192);
-    CUDA_TRY(launch_lj_da(m, LjSys{h->d_pos, h->np, h->radius2()}, h->sg_weights(), max_atoms,
-                          refresh_interval, h->sg_stats, h->stream));
-    left -= m.n_moves;
-  }
+  return SADMC_OK;
+}
+
+}  // namespace
+
+int32_t sadmc_run_da(sadmc_handle* h, uint64_t moves, int32_t refresh_interval, uint64_t* stats) {
+  int32_t r = da_checks(h);
+  if (r) return r;
+  CUDA_TRY(launch_da_chunks(h, moves, refresh_interval));
   h->moves_done += moves;
   if (stats) CUDA_TRY(cudaMemcpyAsync(stats, h->sg_stats, sizeof(uint64_t) * 2 * h->W, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   return SADMC_OK;
+}
+
+int32_t sadmc_run_online(sadmc_handle* h, uint64_t moves, int32_t delayed, int32_t refresh_interval,
+                         const sadmc_online* o, uint64_t* stats) {
+  if (!h || !o) return fail(SADMC_ERR_INVALID, "null argument");
+  if (!h->sg_master) return fail(SADMC_ERR_STATE, "call sadmc_surrogate_init first");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  if (o->retrain_interval && (o->train_steps <= 0 || o->batch <= 0))
+    return fail(SADMC_ERR_INVALID, "train_steps and batch must be positive");
+  if (delayed) {
+    int32_t r = da_checks(h);
+    if (r) return r;
+  }
+  // the schedule counts this handle's moves since initialize, so consecutive calls
+  // continue it
+  const uint64_t t0 = h->moves_done;
+  auto next_event = [](uint64_t t, uint64_t every) -> uint64_t {
+    return every ? (t / every + 1) * every : ~0ull;
+  };
+  for (uint64_t t = t0; t < t0 + moves;) {
+    const uint64_t stop = std::min({t0 + moves, next_event(t, o->collect_interval), next_event(t, o->retrain_interval)});
+    const uint64_t seg = stop - t;
+    if (delayed) CUDA_TRY(launch_da_chunks(h, seg, refresh_interval));
+    else CUDA_TRY(launch_chunks(h, seg, h->stream));
+    t = stop;
+    h->moves_done = t;
+    if (o->collect_interval && t % o->collect_interval == 0) CUDA_TRY(sg_collect_async(h));
+    if (o->retrain_interval && t % o->retrain_interval == 0 && h->sg_count > 0)
+      CUDA_TRY(sg_train_async(h, o->train_steps, o->batch, o->lr, o->seed ^ (t * 0x9E3779B97F4A7C15ull)));
+  }
+  if (stats && delayed)
+    CUDA_TRY(cudaMemcpyAsync(stats, h->sg_stats, sizeof(uint64_t) * 2 * h->W, cudaMemcpyDeviceToHost, h->stream));
+  return sg_check_timeouts(h);
 }
 
 int32_t sadmc_surrogate_predict(sadmc_handle* h, const float* pos, int32_t configs, float* energies) {
@@ -1327,17 +1400,15 @@ int32_t sadmc_surrogate_predict(sadmc_handle* h, const float* pos, int32_t confi
   const size_t rows = (size_t)configs * n;
   CUDA_TRY(h->sg_reserve(rows, configs));
   const SgScratch sc = SgScratch::carve(h->sg_scratch, rows);
+  unsigned int* flag = nullptr;
+  CUDA_TRY(sg_timeout_flag(&flag));
   CUDA_TRY(cudaMemcpyAsync(h->sg_batch_pos, pos, sizeof(float) * 3 * rows, cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(sg_descriptors(h->sg_batch_pos, n, (int)rows, sc.gq, nullptr, h->stream));
-  CUDA_TRY(sg_forward(sc.gq, (int)rows, h->sg_weights(), sc.e, nullptr, nullptr, h->stream));
+  CUDA_TRY(sg_forward(sc.gq, (int)rows, h->sg_weights(), sc.e, flag, h->stream));
   std::vector<float> e(rows);
   CUDA_TRY(cudaMemcpyAsync(e.data(), sc.e, sizeof(float) * rows, cudaMemcpyDeviceToHost, h->stream));
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
-  {
-    unsigned int to = 0;
-    CUDA_TRY(sg_forward_timeouts(&to, h->stream));
-    if (to) return fail(SADMC_ERR_CUDA, "a tensor-core wait of the surrogate forward ran out");
-  }
+  int32_t r = sg_check_timeouts(h);
+  if (r) return r;
   for (int c = 0; c < configs; ++c) {
     double s = 0;
     for (int i = 0; i < n; ++i) s += e[(size_t)c * n + i];
@@ -1377,6 +1448,23 @@ int32_t sadmc_check_numerics(uint64_t n, uint64_t seed, uint64_t* mismatches, do
   if (e == cudaSuccess && first) e = cudaMemcpy(first, df, sizeof(double) * 2, cudaMemcpyDeviceToHost);
   cudaFree(d);
   cudaFree(df);
+  if (e != cudaSuccess) return fail(SADMC_ERR_CUDA, cudaGetErrorString(e));
+  return SADMC_OK;
+}
+
+int32_t sadmc_walker_heat_capacity(sadmc_handle* h, const double* T, int32_t nT, double* C) {
+  if (!h || !T || !C || nT <= 0) return fail(SADMC_ERR_INVALID, "bad argument");
+  if (!h->initialized) return fail(SADMC_ERR_STATE, "initialize first");
+  double *dT = nullptr, *dC = nullptr;
+  cudaError_t e = cudaMalloc(&dT, sizeof(double) * nT);
+  if (e == cudaSuccess) e = cudaMalloc(&dC, sizeof(double) * (size_t)nT * h->W);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dT, T, sizeof(double) * nT, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = launch_walker_cv(h->d_cores, h->planes, h->nb, h->width, h->W, dT, nT, dC, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(C, dC, sizeof(double) * (size_t)nT * h->W, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(dT);
+  cudaFree(dC);
   if (e != cudaSuccess) return fail(SADMC_ERR_CUDA, cudaGetErrorString(e));
   return SADMC_OK;
 }

@@ -17,6 +17,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "sadmc_common.cuh"
 #include "sadmc_fh.cuh"
 #include "sadmc_launch.h"
@@ -362,17 +364,19 @@ cudaError_t launch_lj_da(const MoveLaunch& m, const LjSys& s, const SgWeights& w
                          int refresh_interval, uint64_t* stats, cudaStream_t st) {
   if ((s.np != 32 && s.np != 64) || max_atoms < 2 || max_atoms > s.np) return cudaErrorInvalidConfiguration;
   const int R = dev::da_rows(max_atoms);
-  static bool attr[64][2] = {};  // the limit (for R = np) is set once per device and shape
+  // The limit (for R = np) is set once per device and shape.  Host threads launching on
+  // one device may race to set it; setting it twice is harmless, and the flags are atomic.
+  static std::atomic<bool> attr[64][2] = {};
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return e;
   const int shape = s.np == 32 ? 0 : 1;
-  if (device < 0 || device >= 64 || !attr[device][shape]) {
+  if (device < 0 || device >= 64 || !attr[device][shape].load(std::memory_order_acquire)) {
     const int lim = (int)dev::da_smem_bytes(s.np);
     e = shape == 0 ? cudaFuncSetAttribute(dev::lj_da_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)
                    : cudaFuncSetAttribute(dev::lj_da_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e != cudaSuccess) return e;
-    if (device >= 0 && device < 64) attr[device][shape] = true;
+    if (device >= 0 && device < 64) attr[device][shape].store(true, std::memory_order_release);
   }
   const size_t bytes = dev::da_smem_bytes(R);
   const int blocks = (m.n_walkers + dev::DA_WPB - 1) / dev::DA_WPB;

@@ -90,6 +90,9 @@ cudaError_t launch_init_planes(const WalkerCore* cores, BinPlanes B, int nbins, 
 
 // Heat capacity C(T) = (<E^2> - <E>^2)/T^2 from (E_k, S_k) with max-shifted weights,
 // FP64 (plotting/final_heat_capacity.py:79-88).  One block per temperature.
+// Per-walker heat capacity C[w][t] from the bin planes (FP64).
+cudaError_t launch_walker_cv(const WalkerCore* cores, const BinPlanes& B, int nbins, double width,
+                             int n_walkers, const double* T, int nT, double* C, cudaStream_t st);
 cudaError_t launch_heat_capacity(const double* T, int nT, const double* E, const double* S,
                                  int n, double* C, cudaStream_t st);
 

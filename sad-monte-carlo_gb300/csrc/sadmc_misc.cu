@@ -90,7 +90,125 @@ __global__ void heat_capacity_kernel(const double* T, const double* E, const dou
   if (threadIdx.x == 0) C[blockIdx.x] = red[0] / (t * t);
 }
 
+
+// Block-wide reductions of walker_cv_kernel (256 threads).
+__device__ __forceinline__ double block_max(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Entropy estimate of bin g of one walker, the treatment of plotting/parse-binning.py:
+// 136-160 (restated in export.excess_entropy): ln w inside SAD's [too_lo, too_hi]; below
+// it ln w(too_lo) + (E - too_lo)/min_T + ln(hist / mean hist over the window), above it
+// ln w(too_hi) + ln(hist / mean hist); a Wang-Landau production run adds ln of its
+// production histogram.  -inf for a bin never visited.
+struct WalkerEntropy {
+  const WalkerCore* c;
+  const double* lnw;
+  const uint64_t* hist;
+  const uint64_t* wlh;
+  double width;
+  int i_lo, i_hi;
+  double mean_hist;
+  bool sad, wl_prod;
+  __device__ double E(int g) const { return c->cur_min + ((double)(g - c->b_lo) + 0.5) * width; }
+  __device__ double S(int g) const {
+    const uint64_t h = hist[g];
+    if (h == 0) return -1.0 / 0.0;
+    const double e = E(g);
+    if (sad) {
+      if (e < c->too_lo) return lnw[i_lo] + (e - c->too_lo) / c->min_T + log((double)h / mean_hist);
+      if (e > c->too_hi) return lnw[i_hi] + log((double)h / mean_hist);
+      return lnw[g];
+    }
+    if (wl_prod) {
+      const int k = c->wl_lo + (g - c->b_lo);
+      const uint64_t p = (k >= c->wl_lo && k <= c->wl_hi) ? wlh[k] : 0;
+      return p > 0 ? lnw[g] + log((double)p) : lnw[g];
+    }
+    return lnw[g];
+  }
+};
+
+// C[w][t] = heat_capacity(T[t], E, S) of walker w (plotting/final_heat_capacity.py:79-88)
+// over its allocated bins, FP64, one block per walker.
+__global__ void walker_cv_kernel(const WalkerCore* cores, BinPlanes B, int nbins, double width,
+                                 const double* T, int nT, double* C) {
+  __shared__ double red[256];
+  const int w = blockIdx.x;
+  const WalkerCore* c = &cores[w];
+  const size_t off = (size_t)w * (size_t)nbins;
+  WalkerEntropy we;
+  we.c = c;
+  we.lnw = B.lnw + off;
+  we.hist = B.hist + off;
+  we.wlh = B.wl_hist + off;
+  we.width = width;
+  we.sad = c->kind == M_SAD;
+  we.wl_prod = (c->kind == M_WL || c->kind == M_INV_T_WL) && c->has_min_gamma && c->gamma == 0.0;
+  we.i_lo = we.i_hi = c->b_lo;
+  we.mean_hist = 1.0;
+  if (we.sad) {
+    // the window edges are bin centres: the nearest bin of each
+    int lo = c->b_lo + (int)floor((c->too_lo - c->cur_min) / width);
+    int hi = c->b_lo + (int)floor((c->too_hi - c->cur_min) / width);
+    lo = max(c->b_lo, min(c->b_hi, lo));
+    hi = max(c->b_lo, min(c->b_hi, hi));
+    we.i_lo = lo;
+    we.i_hi = hi;
+    double hs = 0.0;
+    for (int g = lo + threadIdx.x; g <= hi; g += blockDim.x) hs += (double)we.hist[g];
+    we.mean_hist = block_sum(hs, red) / (double)(hi - lo + 1);
+  }
+  for (int t = 0; t < nT; ++t) {
+    const double tt = T[t];
+    double mx = -1.0 / 0.0;
+    for (int g = c->b_lo + threadIdx.x; g <= c->b_hi; g += blockDim.x) mx = fmax(mx, we.S(g) - we.E(g) / tt);
+    mx = block_max(mx, red);
+    double z = 0.0, ez = 0.0;
+    for (int g = c->b_lo + threadIdx.x; g <= c->b_hi; g += blockDim.x) {
+      const double p = exp(we.S(g) - we.E(g) / tt - mx);
+      z += p;
+      ez += we.E(g) * p;
+    }
+    z = block_sum(z, red);
+    const double U = block_sum(ez, red) / z;
+    double cc = 0.0;
+    for (int g = c->b_lo + threadIdx.x; g <= c->b_hi; g += blockDim.x) {
+      const double de = we.E(g) - U;
+      cc += de * de * exp(we.S(g) - we.E(g) / tt - mx) / z;
+    }
+    cc = block_sum(cc, red);
+    if (threadIdx.x == 0) C[(size_t)w * nT + t] = cc / (tt * tt);
+  }
+}
+
 }  // namespace dev
+
+cudaError_t launch_walker_cv(const WalkerCore* cores, const BinPlanes& B, int nbins, double width,
+                             int n_walkers, const double* T, int nT, double* C, cudaStream_t st) {
+  if (nT <= 0 || n_walkers <= 0) return cudaSuccess;
+  dev::walker_cv_kernel<<<n_walkers, 256, 0, st>>>(cores, B, nbins, width, T, nT, C);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_init_planes(const WalkerCore* cores, BinPlanes B, int nbins, int n_walkers,
                                cudaStream_t st) {

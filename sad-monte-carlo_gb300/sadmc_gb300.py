@@ -60,6 +60,13 @@ class Geometry(ctypes.Structure):
                 ("box", ctypes.c_double * 3)]
 
 
+class Online(ctypes.Structure):
+    """sadmc_online: the online training schedule of run_online."""
+    _fields_ = [("collect_interval", ctypes.c_uint64), ("retrain_interval", ctypes.c_uint64),
+                ("train_steps", ctypes.c_int32), ("batch", ctypes.c_int32),
+                ("lr", ctypes.c_float), ("pad", ctypes.c_int32), ("seed", ctypes.c_uint64)]
+
+
 class Proposal(ctypes.Structure):
     _fields_ = [("which", ctypes.c_int32), ("j", ctypes.c_int32), ("g", ctypes.c_double * 3),
                 ("scale", ctypes.c_double)]
@@ -119,6 +126,8 @@ def lib():
         "sadmc_grand_translation_counts": (I32, [P, I32, P, P]),
         "sadmc_surrogate_predict": (I32, [P, P, I32, P]),
         "sadmc_run_da": (I32, [P, U64, I32, P]),
+        "sadmc_run_online": (I32, [P, U64, I32, I32, P, P]),
+        "sadmc_walker_heat_capacity": (I32, [P, P, I32, P]),
         "sadmc_draws": (I32, [I32, ctypes.c_uint32, U64, ctypes.c_uint32, U64, I32, ctypes.c_uint32,
                               P, P, P]),
     }
@@ -392,10 +401,30 @@ class Batch:
         _check(lib().sadmc_run_da(self.h, int(moves), refresh_interval, _p(st)))
         return st.reshape(-1, 2)
 
+    def run_online(self, moves, delayed, collect_interval=0, retrain_interval=0, train_steps=0,
+                   batch=256, lr=1e-3, seed=0, refresh_interval=2048):
+        """Plain (delayed=False) or delayed-acceptance moves while the surrogate trains
+        online on the device (sadmc_run_online); returns the delayed-acceptance counters
+        (stage-1 rejections, exact evaluations) per walker, or None for plain moves."""
+        o = Online(int(collect_interval), int(retrain_interval), int(train_steps), int(batch),
+                   float(lr), 0, int(seed))
+        st = np.zeros(2 * self.W, np.uint64)
+        _check(lib().sadmc_run_online(self.h, int(moves), int(bool(delayed)), int(refresh_interval),
+                                      ctypes.byref(o), _p(st)))
+        return st.reshape(-1, 2) if delayed else None
+
     def surrogate_predict(self, pos):
         pos = np.ascontiguousarray(pos, np.float32)
         out = np.zeros(pos.shape[0], np.float32)
         _check(lib().sadmc_surrogate_predict(self.h, _p(pos), pos.shape[0], _p(out)))
+        return out
+
+    def heat_capacities(self, T):
+        """Per-walker heat capacity C[w, t] from each walker's own bins, FP64 on the device
+        (sadmc_walker_heat_capacity)."""
+        T = np.ascontiguousarray(T, np.float64)
+        out = np.zeros((self.W, len(T)))
+        _check(lib().sadmc_walker_heat_capacity(self.h, _p(T), len(T), _p(out)))
         return out
 
     def lanes_per_walker(self):

@@ -31,8 +31,9 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_rust_binding_covers_the_header():
-    """INTEGRATION.md's extern "C" blocks bind every declared entry point, and nothing else."""
-    text = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    """The Rust binding's extern "C" blocks bind every declared entry point, and nothing
+    else."""
+    text = open(os.path.join(REPO, "include", "sadmc_gpu.rs")).read()
     bound = sorted(set(re.findall(r"pub fn (sadmc_\w+)\(", text)))
     assert bound == declared_functions(), (set(declared_functions()) ^ set(bound))
 

@@ -171,3 +171,65 @@ def test_square_well_initial_descent_bit_exact(gpu, oracle):
         assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
         np.testing.assert_array_equal(b.state(w), ow.state())
     assert not b.status().any()
+
+
+@pytest.mark.parametrize("lpw", [32, 16])
+def test_square_well_c5_shape_bit_exact(gpu, oracle, lpw):
+    """The hard-sphere workload's own shape: N = 1024 square-well atoms (lambda 1.3) at
+    packing fractions 0.30 and 0.50 (9 and 7 subcells per axis) and between, Wang-Landau
+    on contact bins, a few thousand moves; bins, scalars and configurations bit-identical
+    to the oracle's (optsquare.rs:74-95, 273-322)."""
+    n, moves, seed = 1024, 3000, 11
+    ws = sw_walkers(oracle, n, [0.30, 0.50, 0.40, 0.45], 60)
+    ncs = [int(np.floor(box[0] / 1.3)) for _, box in ws]
+    assert ncs[0] == 9 and ncs[1] == 7, ncs
+    cfg = gpu.make_config(gpu.SW, len(ws), n, method=2, e_lo=-6.0 * n - 2, e_hi=2.0, well_width=1.3,
+                          seed=seed, translation_scale=0.05, lanes_per_walker=lpw)
+    b = gpu.Batch(cfg, [(n, 0.0, box) for _, box in ws])
+    b.upload([p for p, _ in ws])
+    E0 = b.compute_energies()
+    b.initialize()
+    b.run(moves)
+    for w, (pos, box) in enumerate(ws):
+        ow = oracle.Walker(oracle.make_config(oracle.SW, n, box=box, well_width=1.3, method=2, seed=seed,
+                                              walker=w, translation_scale=0.05), pos)
+        assert ow.energy() == E0[w]
+        ow.run(moves)
+        label = f"sw C5 shape lpw{lpw} walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_array_equal(b.state(w), ow.state())
+    np.testing.assert_array_equal(b.energies(), b.compute_energies())
+    assert not b.status().any()
+
+
+def test_wca_c3_shape_trace_replay(gpu, oracle):
+    """The uneven WCA workload's largest walkers: N = 512 at density 0.6 (8 subcells per
+    axis) and N = 256 at 0.9 (5), beside N = 512 at 0.75 and N = 256 at 0.6, SAMC, traced
+    and replayed by the FP64 oracle (wca.rs:119-140)."""
+    specs = [(512, 0.6), (256, 0.9), (512, 0.75), (256, 0.6)]
+    moves, seed, w_bin = 4000, 21, 0.5
+    confs = [wca_config(n, rho, 70 + k) for k, (n, rho) in enumerate(specs)]
+    assert int(np.floor(confs[0][1][0] / 2 ** (1 / 6))) == 8
+    cfg = gpu.make_config(gpu.WCA, len(specs), 512, method=1, t0=1e4, energy_bin=w_bin, e_lo=-2 * w_bin,
+                          e_hi=4100.0, max_allowed=4000.0, translation_scale=0.1, seed=seed,
+                          lanes_per_walker=16, resum_interval=1500)
+    b = gpu.Batch(cfg, [(n, 0.0, box) for (n, _), (_, box) in zip(specs, confs)])
+    b.upload([p for p, _ in confs])
+    b.initialize()
+    E0 = b.energies()
+    b.set_trace(moves)
+    b.run(moves)
+    for w, ((n, rho), (pos, box)) in enumerate(zip(specs, confs)):
+        e1, e2 = b.trace(w, moves)
+        ow = oracle.Walker(oracle.make_config(oracle.WCA, n, box=box, method=1, t0=1e4,
+                                              energy_bin=w_bin, max_allowed=4000.0,
+                                              translation_scale=0.1, seed=seed, walker=w,
+                                              e0=float(E0[w])), pos)
+        disc, mismatch = ow.run_override(e1, e2)
+        assert mismatch == 0 and disc < 5e-6, (w, mismatch, disc)
+        label = f"wca C3 shape walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-12)
+    assert not (b.status() & ~np.uint32(gpu.ST_DESCENT_FAILED)).any()

@@ -200,3 +200,45 @@ def test_da_screen_matches_the_mlp_statement(gpu, oracle, n):
         assert np.abs(err).max() < 0.02, (w, np.abs(err).max())
         assert abs(err.sum()) < 0.05, (w, err.sum())
         np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
+
+
+def test_da_trace_replay_at_c4_launch_geometry(gpu, oracle):
+    """Delayed acceptance at the LJ38 workload's own launch geometry (8192 walkers, R = 3.5,
+    SAD min_T 0.05, bins of 0.2): plain moves with online collection, training, then
+    delayed-acceptance moves with online retraining, all traced; walkers from the first,
+    middle and last blocks are replayed through the FP64 oracle, which takes both stages'
+    decisions itself."""
+    n, W, R, seed = 38, 8192, 3.5, 8
+    plain_moves, da_moves = 1500, 3000
+    confs = lj_configs(oracle, n, R, range(5000, 5000 + W))
+    kw = dict(method=0, min_T=0.05, energy_bin=0.2, max_allowed=0.0, target_rate=0.5,
+              translation_scale=0.1, seed=seed)
+    b = gpu.Batch(gpu.make_config(gpu.LJ, W, n, e_lo=-180.0, e_hi=1.0, lanes_per_walker=32, **kw),
+                  [(n, R, (0, 0, 0))] * W)
+    b.upload(confs)
+    b.initialize()
+    E0 = b.energies()
+    total = plain_moves + da_moves
+    b.set_trace(total)
+    b.surrogate_init(seed=2, ring_capacity=1 << 15)
+    b.run_online(plain_moves, False, collect_interval=500, retrain_interval=1500, train_steps=100,
+                 batch=256, lr=2e-3, seed=4)
+    stats = b.run_online(da_moves, True, collect_interval=1000, retrain_interval=1500, train_steps=20,
+                         batch=256, lr=1e-3, seed=5)
+    screened = stats[:, 0].sum() / stats.sum()
+    assert 0.02 < screened < 0.95, screened
+    for w in (0, 1, 3, 4, 4096, 4099, 8188, 8191):
+        e1, e2 = b.trace(w, total)
+        ds = b.trace_ds(w, total)
+        assert not ds[:plain_moves].any()
+        ow = oracle.Walker(oracle.make_config(oracle.LJ, n, radius=R, walker=w, e0=float(E0[w]), **kw),
+                           confs[w])
+        d1, m1 = ow.run_override(e1[:plain_moves], e2[:plain_moves])
+        d2, m2 = ow.run_override_da(e1[plain_moves:], e2[plain_moves:], ds[plain_moves:])
+        assert m1 == 0 and m2 == 0, (w, m1, m2)
+        assert max(d1, d2) < 2e-5, (w, d1, d2)
+        label = f"da C4 launch walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
+    assert not b.status().any()

@@ -114,3 +114,35 @@ def test_heat_capacity_gpu_vs_oracle(gpu, oracle):
     T = np.linspace(0.05, 0.5, 64)
     np.testing.assert_allclose(gpu.heat_capacity(T, E, S), oracle.heat_capacity(T, E, S),
                                rtol=1e-10)
+
+
+def test_lj_c2_launch_geometry_trace_replay(gpu, oracle):
+    """The headline workload's own launch: 4096 LJ31 walkers (R = 2.5, SAD min_T 0.2, 1000
+    bins of 0.134 over [-134, 0], max_allowed_energy 0, step 0.1 adapted to 50 %) at its
+    default shape, one run traced; walkers from the first, middle and last warps and blocks
+    are replayed through the FP64 oracle: every decision and bin must be the GPU's."""
+    n, W, radius, seed, moves = 31, 4096, 2.5, 17, 3000
+    width = 0.134
+    confs = lj_configs(oracle, n, radius, range(2000, 2000 + W))
+    cfg = gpu.make_config(gpu.LJ, W, n, method=0, min_T=0.2, energy_bin=width, max_allowed=0.0,
+                          e_lo=-134.0 - 2 * width, e_hi=2 * width, target_rate=0.5,
+                          translation_scale=0.1, seed=seed, lanes_per_walker=8)
+    b = gpu.Batch(cfg, [(n, radius, (0, 0, 0))] * W)
+    b.upload(confs)
+    b.initialize()
+    E0 = b.energies()
+    b.set_trace(moves)
+    b.run(moves)
+    for w in (0, 1, 3, 4, 127, 2048, 2051, 4092, 4095):
+        e1, e2 = b.trace(w, moves)
+        ow = oracle.Walker(oracle.make_config(oracle.LJ, n, radius=radius, method=0, min_T=0.2,
+                                              energy_bin=width, max_allowed=0.0, target_rate=0.5,
+                                              translation_scale=0.1, seed=seed, walker=w,
+                                              e0=float(E0[w])), confs[w])
+        disc, mismatch = ow.run_override(e1, e2)
+        assert mismatch == 0 and disc < REPLAY_REL, (w, mismatch, disc)
+        label = f"C2 launch walker {w}"
+        assert_bins_equal(b.bins(w), ow.bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
+        np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
+    assert not b.status().any()
