@@ -49,6 +49,28 @@ def assert_scalars_equal(gs, os_, keys=None, label=""):
         assert gs[k] == os_[k], f"{label} scalar {k}: gpu {gs[k]!r} oracle {os_[k]!r}"
 
 
+def sphere_configs(n, radius, count, seed, dmin=0.8):
+    """`count` LJ-cluster configurations for large batches: atoms uniform in the sphere,
+    each redrawn while closer than dmin to an earlier one (the rule of the LJ workloads),
+    from one seeded numpy generator.  Far quicker than the oracle's initialiser, which
+    follows the reference's (lj.rs:126-204) at about 0.3 s per configuration."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        pts = np.empty((n, 3))
+        k = 0
+        while k < n:
+            p = rng.uniform(-radius, radius, 3)
+            if p @ p >= radius * radius:
+                continue
+            if k and np.min(((pts[:k] - p) ** 2).sum(axis=1)) < dmin * dmin:
+                continue
+            pts[k] = p
+            k += 1
+        out.append(pts)
+    return out
+
+
 def lj_configs(oracle, n, radius, seeds):
     out = []
     for s in seeds:

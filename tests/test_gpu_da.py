@@ -6,7 +6,7 @@ before the exact evaluation while the sampled energies stay those of the plain c
 import numpy as np
 import pytest
 
-from helpers import BIN_KEYS, assert_bins_equal, assert_scalars_equal, lj_configs
+from helpers import BIN_KEYS, assert_bins_equal, assert_scalars_equal, lj_configs, sphere_configs
 
 pytestmark = pytest.mark.gpu
 
@@ -210,7 +210,7 @@ def test_da_trace_replay_at_c4_launch_geometry(gpu, oracle):
     decisions itself."""
     n, W, R, seed = 38, 8192, 3.5, 8
     plain_moves, da_moves = 1500, 3000
-    confs = lj_configs(oracle, n, R, range(5000, 5000 + W))
+    confs = sphere_configs(n, R, W, seed=5000)
     kw = dict(method=0, min_T=0.05, energy_bin=0.2, max_allowed=0.0, target_rate=0.5,
               translation_scale=0.1, seed=seed)
     b = gpu.Batch(gpu.make_config(gpu.LJ, W, n, e_lo=-180.0, e_hi=1.0, lanes_per_walker=32, **kw),

@@ -8,7 +8,7 @@ flat-histogram decision and bin must be bit-identical.
 import numpy as np
 import pytest
 
-from helpers import assert_bins_equal, assert_scalars_equal, lj_configs
+from helpers import assert_bins_equal, assert_scalars_equal, lj_configs, sphere_configs
 
 pytestmark = pytest.mark.gpu
 
@@ -123,7 +123,7 @@ def test_lj_c2_launch_geometry_trace_replay(gpu, oracle):
     are replayed through the FP64 oracle: every decision and bin must be the GPU's."""
     n, W, radius, seed, moves = 31, 4096, 2.5, 17, 3000
     width = 0.134
-    confs = lj_configs(oracle, n, radius, range(2000, 2000 + W))
+    confs = sphere_configs(n, radius, W, seed=2000)
     cfg = gpu.make_config(gpu.LJ, W, n, method=0, min_T=0.2, energy_bin=width, max_allowed=0.0,
                           e_lo=-134.0 - 2 * width, e_hi=2 * width, target_rate=0.5,
                           translation_scale=0.1, seed=seed, lanes_per_walker=8)

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import cv_oracle as CV
-from helpers import lj_configs
+from helpers import sphere_configs
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "lj31_cv_reference.json")
@@ -26,7 +26,7 @@ def c2_batch(gpu, oracle, W, seed, lpw=0):
                           e_lo=-134.0 - 2 * width, e_hi=2 * width, target_rate=0.5,
                           translation_scale=0.1, seed=seed, lanes_per_walker=lpw)
     b = gpu.Batch(cfg, [(31, 2.5, (0, 0, 0))] * W)
-    b.upload(lj_configs(oracle, 31, 2.5, range(3000, 3000 + W)))
+    b.upload(sphere_configs(31, 2.5, W, seed=3000 + seed))
     b.initialize()
     return b
 

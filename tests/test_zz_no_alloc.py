@@ -5,7 +5,7 @@ is accepted in full and a request one row above it is refused before anything la
 import numpy as np
 import pytest
 
-from helpers import lj_configs
+from helpers import sphere_configs
 
 pytestmark = pytest.mark.gpu
 
@@ -13,7 +13,7 @@ MAX_ROWS = 4096
 
 
 def _batch(gpu, oracle, n, W, R, seed=0):
-    confs = lj_configs(oracle, n, R, range(300, 300 + W))
+    confs = sphere_configs(n, R, W, seed=300 + n)
     cfg = gpu.make_config(gpu.LJ, W, n, energy_bin=0.134, max_allowed=0.0, e_lo=-180, e_hi=1,
                           target_rate=0.5, translation_scale=0.1, seed=seed)
     b = gpu.Batch(cfg, [(n, R, (0, 0, 0))] * W)
