@@ -266,9 +266,14 @@ def case_grand(G, seed=11, walkers=4096, moves=4096, lpw=0):
     return out
 
 
-def case_da(G, seed=11, walkers=8192, moves=2048, **_):
+def case_da(G, seed=11, walkers=8192, moves=100_000, **_):
     """C4 shape: the plain and delayed-acceptance arms of da_compare, alone."""
     return da_compare(G, 0, walkers, moves)
+
+
+def case_north_star(G, seed=31, walkers=512, moves=1_000_000, **_):
+    """Plain against delayed acceptance at equal heat-capacity error (the benchmark spec), alone."""
+    return north_star(G, walkers=walkers, warm=moves, seed=seed)
 
 
 def case_grand_wca(G, seed=11, walkers=512, moves=2048, lpw=0):
@@ -290,7 +295,7 @@ def case_grand_wca(G, seed=11, walkers=512, moves=2048, lpw=0):
 
 CASES = {"C1": case_c1, "C1_batch": case_c1_batch, "C3": case_c3, "C5": case_c5,
          "grand": case_grand, "grand_wca": case_grand_wca}
-ONLY = dict(CASES, DA=case_da)
+ONLY = dict(CASES, DA=case_da, NORTH_STAR=case_north_star)
 
 
 def cpu_cases(seed=11):
@@ -337,59 +342,168 @@ def other_configs(G, seed=11, cpu=True):
     return out
 
 
-def da_compare(G, rank=0, walkers=8192, moves=2048):
-    """C4 shape: LJ38 (R=3.5), SAD; the surrogate is trained on configurations the walkers
-    visit, then plain and delayed-acceptance moves are timed on the same batch state."""
-    import ctypes
-    import torch
-    n, R = 38, 3.5
-    rng = np.random.default_rng(77 + rank)
-    confs = []
-    for _ in range(walkers):  # uniform in the sphere with sequential 0.8 rejection
-        pts = []
-        while len(pts) < n:
+def sphere_configs(n, R, count, seed):
+    """Uniform in the sphere with sequential rejection of pairs closer than 0.8."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        pts = np.empty((n, 3))
+        k = 0
+        while k < n:
             p = rng.uniform(-R, R, 3)
-            if p @ p >= R * R or (pts and np.min(np.sum((np.array(pts) - p) ** 2, axis=1)) < 0.64):
+            if p @ p >= R * R or (k and np.min(((pts[:k] - p) ** 2).sum(axis=1)) < 0.64):
                 continue
-            pts.append(p)
-        confs.append(np.array(pts))
+            pts[k] = p
+            k += 1
+        out.append(pts)
+    return out
+
+
+def _timed(f):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = f()
+    torch.cuda.synchronize()
+    return r, time.perf_counter() - t0
+
+
+def da_compare(G, rank=0, walkers=8192, moves=100_000):
+    """C4 shape: LJ38 (R = 3.5), SAD min_T 0.05, bins of 0.2, 8192 walkers.  The surrogate
+    is trained online on configurations the walkers' own SAD run visits (a ring of 1e6,
+    every walker collected every 4000 moves, retrained every 2e4 moves of the warm-up),
+    then the plain arm (at its autotuned shape) and the delayed-acceptance arm (retrained
+    every 5e4 moves, inside its timed region) each run `moves` moves per walker."""
+    n, R = 38, 3.5
     cfg = G.make_config(G.LJ, walkers, n, method=G.SAD, min_T=0.05, energy_bin=0.2,
                         max_allowed=0.0, e_lo=-180.0, e_hi=1.0, target_rate=0.5,
-                        translation_scale=0.1, seed=21 + rank, lanes_per_walker=32)
+                        translation_scale=0.1, seed=21 + rank)
     b = G.Batch(cfg, [(n, R, (0, 0, 0))] * walkers)
-    b.upload(confs)
+    b.upload(sphere_configs(n, R, walkers, 77 + rank))
     b.initialize()
-    b.surrogate_init(seed=3, ring_capacity=1 << 16)
-    for _ in range(8):
-        b.run(1024)
-        b.surrogate_collect()
-    t0 = time.perf_counter()
-    loss = b.surrogate_train(800, batch=512, lr=2e-3, seed=5)
-    train_s = time.perf_counter() - t0
-    torch.cuda.synchronize()
+    b.surrogate_init(seed=3, ring_capacity=1_000_000)
+    _, warm_s = _timed(lambda: b.run_online(40_000, False, collect_interval=4000, retrain_interval=20_000,
+                                            train_steps=400, batch=512, lr=2e-3, seed=5))
+    _, train_s = _timed(lambda: b.surrogate_train(200, batch=512, lr=1e-3, seed=6))
+    loss = b.surrogate_train(1, batch=4096, lr=0.0, seed=7)
+    b.autotune(2048)
     m0, a0 = b.counters()
-    t0 = time.perf_counter()
-    b.run(moves)
-    plain_s = time.perf_counter() - t0
+    _, plain_s = _timed(lambda: b.run(moves))
     m1, a1 = b.counters()
-    t0 = time.perf_counter()
-    st = b.run_da(moves)
-    da_s = time.perf_counter() - t0
+    st0 = b.run_da(0)
+    st, da_s = _timed(lambda: b.run_online(moves, True, collect_interval=10_000, retrain_interval=50_000,
+                                           train_steps=100, batch=512, lr=1e-3, seed=8))
     m2, a2 = b.counters()
+    flagged = status_summary(b)
+    lanes = b.lanes_per_walker()
     b.close()
+    st = st.astype(np.float64) - st0.astype(np.float64)
     screened = float(st[:, 0].sum()) / float(st.sum())
-    return {"workload": f"C4 shape: LJ{n} (R={R}), SAD, {walkers} walkers, {moves} moves/walker each arm, "
-                        "one walker per warp in both arms",
+    exact = float(st[:, 1].sum()) / float(m2 - m1)
+    return {"workload": f"C4 shape: LJ{n} (R={R}), SAD min_T 0.05, bins of 0.2, {walkers} walkers, "
+                        f"{moves} moves/walker per arm",
             "plain_moves_per_s": (m1 - m0) / plain_s, "plain_accepted_per_s": (a1 - a0) / plain_s,
+            "plain_lanes_per_walker": lanes,
             "da_moves_per_s": (m2 - m1) / da_s, "da_accepted_per_s": (a2 - a1) / da_s,
             "da_vs_plain": ((m2 - m1) / da_s) / ((m1 - m0) / plain_s),
-            "screened_fraction": screened, "surrogate_rmse": float(np.sqrt(loss)),
-            "train_s": train_s,
+            "da_accepted_vs_plain": ((a2 - a1) / da_s) / ((a1 - a0) / plain_s),
+            "screened_fraction": screened, "exact_evaluations_per_move": exact,
+            "surrogate_rmse": float(np.sqrt(loss)),
+            "train_us_per_step": 1e6 * train_s / 200, "train_batch_rows": 512 * n,
+            "warmup_s": warm_s, **flagged,
+            "online": "ring 1e6 configurations; warm-up collects every 4000 moves and retrains every "
+                      "20000 (400 Adam steps of 512); the DA arm collects every 10000 and retrains "
+                      "every 50000 moves (100 steps) inside its timed region",
             "roofline": _roof((m2 - m1) / da_s * 2 * n * 6208 / 1e12,
                               float(peaks().get("bf16_tflops", 1900.0)), "TFLOP/s",
                               f"stage 1: the MLP on all {n} descriptor rows, 2 x 6208 BF16 FLOP "
                               "per row, against the measured bf16 peak (mma.sync m16n8k16, one "
                               "walker per warp)")}
+
+
+CV_T = np.array([0.25, 0.28, 0.30, 0.33, 0.36])
+
+
+def lj31_reference_cv(T=CV_T):
+    """Mean of the reference's Rc = 2.5 LJ31 curves (RESTMC and t-REM) at T, from the
+    committed fixture of the reference's CSV files."""
+    import cv as CVM
+    g = json.load(open(os.path.join(REPO, "tests", "golden", "lj31_cv_reference.json")))
+    return CVM.interp_reference(T, [(g["curves"][k]["T"], g["curves"][k]["Cv"]) for k in ("RESTMC", "t-REM")])
+
+
+def north_star(G, walkers=512, warm=1_000_000, seconds=20.0, seed=31):
+    """Plain against delayed-acceptance moves at equal heat-capacity error, on the LJ31
+    workload's configuration (R = 2.5, SAD min_T 0.2, bins of 0.134), whose heat capacity
+    the reference holds (its Rc = 2.5 curves, RESTMC and t-REM, T = 0.25-0.36).  Both arms
+    continue from one checkpoint after a shared warm-up in which the surrogate trains
+    online on the walkers' own configurations; each arm runs for `seconds` of wall time in
+    segments, and after each segment every walker's Cv is rebuilt on the device from its
+    own bins.  The error is that of the walker-median Cv curve against the reference
+    (max over T of the relative error).  The comparison is the time each arm needs to
+    reach the error both reach (the larger of the two final errors)."""
+    import tempfile
+    import cv as CVM
+    ref = lj31_reference_cv()
+    width = 0.134
+    cfg = G.make_config(G.LJ, walkers, 31, method=G.SAD, min_T=0.2, energy_bin=width, max_allowed=0.0,
+                        e_lo=-134.0 - 2 * width, e_hi=2 * width, target_rate=0.5,
+                        translation_scale=0.1, seed=seed)
+    b = G.Batch(cfg, [(31, 2.5, (0, 0, 0))] * walkers)
+    b.upload(sphere_configs(31, 2.5, walkers, 900 + seed))
+    b.initialize()
+    b.surrogate_init(seed=4, ring_capacity=1 << 18)
+    b.run_online(warm, False, collect_interval=warm // 10, retrain_interval=warm // 5, train_steps=300,
+                 batch=512, lr=2e-3, seed=9)
+    path = os.path.join(tempfile.gettempdir(), f"sadmc_north_star_{os.getpid()}.ck")
+    b.checkpoint(path)
+    plain = G.Batch.resume(path)
+    os.remove(path)
+
+    def arm(step, seg):
+        rows, t, m_start, a_start = [], 0.0, *b_counters(step)
+        while t < seconds:
+            _, dt = _timed(lambda: step["run"](seg))
+            t += dt
+            m, a = b_counters(step)
+            e = CVM.cv_error(step["batch"].heat_capacities(CV_T), ref)
+            rows.append({"t": t, "moves_per_walker": (m - m_start) / walkers, "accepted": a - a_start,
+                         "err": e["max_rel_of_median"], "median_walker_err": e["median_max_rel"]})
+        return rows
+
+    def b_counters(step):
+        return step["batch"].counters()
+
+    p_rows = arm({"batch": plain, "run": lambda k: plain.run(k)}, 1_000_000)
+    d_rows = arm({"batch": b, "run": lambda k: b.run_online(k, True, collect_interval=100_000,
+                                                             retrain_interval=100_000, train_steps=100,
+                                                             batch=512, lr=1e-3, seed=10)}, 200_000)
+    eps = max(p_rows[-1]["err"], d_rows[-1]["err"])
+    tp = CVM.time_to_error([r["t"] for r in p_rows], [r["err"] for r in p_rows], eps)
+    td = CVM.time_to_error([r["t"] for r in d_rows], [r["err"] for r in d_rows], eps)
+    flagged = {"plain": status_summary(plain), "da": status_summary(b)}
+    plain.close()
+    b.close()
+
+    def summary(rows):
+        t = rows[-1]["t"]
+        return {"seconds": t, "moves_per_s": rows[-1]["moves_per_walker"] * walkers / t,
+                "accepted_moves_per_s": rows[-1]["accepted"] / t, "cv_error": rows[-1]["err"],
+                "median_walker_cv_error": rows[-1]["median_walker_err"],
+                "curve": [(round(r["t"], 2), round(r["moves_per_walker"]), round(r["err"], 4)) for r in rows]}
+    out = {"workload": f"LJ31 (R=2.5), SAD min_T 0.2, bins of 0.134, {walkers} walkers, {warm} shared "
+                       f"warm-up moves/walker with online training, then {seconds:g} s per arm",
+           "cv_reference": "mean of the reference's Rc = 2.5 curves (RESTMC, t-REM) at T = "
+                           + ", ".join(f"{t:g}" for t in CV_T),
+           "cv_error_metric": "max over T of |median-walker Cv - reference| / reference",
+           "plain": summary(p_rows), "da": summary(d_rows), "equal_cv_error": eps,
+           "plain_seconds_to_equal_error": tp, "da_seconds_to_equal_error": td,
+           "da_speedup_at_equal_cv_error": (tp / td) if (tp and td) else None,
+           "status": flagged}
+    out["da_wins"] = bool(out["da_speedup_at_equal_cv_error"] and out["da_speedup_at_equal_cv_error"] > 1.0)
+    for k in ("plain", "da"):
+        out[k]["accepted_moves_per_s_at_equal_cv_error"] = out[k]["accepted_moves_per_s"]
+    return out
 
 
 def make_batch(G, n_walkers, seed=1, lpw=0):
@@ -614,7 +728,7 @@ def run_gpu(args):
 
     da = None
     if not args.no_da and world == 1:
-        da = da_compare(G, rank)
+        da = {"c4_shape": da_compare(G, rank), "equal_cv_error": north_star(G)}
     others = None
     if not args.no_other and rank == 0:
         others = other_configs(G, cpu=not args.no_cpu)

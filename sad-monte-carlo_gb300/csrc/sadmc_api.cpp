@@ -51,8 +51,8 @@ int pad_atoms(int n) {
 
 bool valid_lpw_lj(int lpw, int np) {
   switch (np) {
-    case 32: return lpw == 32 || lpw == 16 || lpw == 8 || lpw == 4;
-    case 64: return lpw == 32 || lpw == 16 || lpw == 8;
+    case 32: return lpw == 32 || lpw == 16 || lpw == 8 || lpw == 4 || lpw == 2 || lpw == 1;
+    case 64: return lpw == 32 || lpw == 16 || lpw == 8 || lpw == 2 || lpw == 1;
     default: return lpw == 32;
   }
 }
@@ -98,7 +98,7 @@ struct sadmc_handle {
   int pend_walker = -1;
   sadmc_proposal pend{};
   std::vector<WalkerCore> h_cores;
-  int wpb = 4;                                  // warps per block
+  int wpb = 0;                                  // warps per block (0: the kernel's own default)
   // learned surrogate (LJ)
   float* sg_master = nullptr;                   // FP32 parameters
   float* sg_grad = nullptr;
@@ -184,7 +184,13 @@ struct sadmc_handle {
   }
   cudaError_t launch_move(const MoveLaunch& m) {
     switch (cfg.system) {
-      case SADMC_LJ: return launch_lj_move(m, LjSys{d_pos, np, 0.0 + radius2()}, lpw, stream);
+      case SADMC_LJ:
+        // one or two lanes per walker: the shared-memory kernel for moves; the initial
+        // descent runs on the register kernel (8 lanes per walker) either way
+        if (lj_lane_shape(lpw, np))
+          return m.descent ? launch_lj_move(m, LjSys{d_pos, np, 0.0 + radius2()}, 8, stream)
+                           : launch_lj_lane(m, LjSys{d_pos, np, 0.0 + radius2()}, lpw, stream);
+        return launch_lj_move(m, LjSys{d_pos, np, 0.0 + radius2()}, lpw, stream);
       case SADMC_ISING: return launch_ising_move(m, IsingSys{d_spins, L}, lpw, stream);
       case SADMC_SW:
       case SADMC_WCA: return launch_cell_move(m, cell_sys(), lpw, stream);
@@ -294,8 +300,8 @@ std::vector<int> lpw_candidates(const sadmc_handle* h) {
   switch (h->cfg.system) {
     case SADMC_ISING: return {1, 32};
     case SADMC_LJ:
-      if (h->np == 32) return {4, 8, 16, 32};
-      if (h->np == 64) return {8, 16, 32};
+      if (h->np == 32) return {1, 2, 4, 8, 16, 32};
+      if (h->np == 64) return {1, 2, 8, 16, 32};
       return {32};
     default: return {4, 8, 16, 32};
   }

@@ -77,6 +77,14 @@ __device__ __forceinline__ double f2d(float f) {
                                ((unsigned long long)(b & 0x7fffffu) << 29);
   return __longlong_as_double((long long)d);
 }
+// (double)x for an integer x < 2^53 (exact), by integer instructions: the FP64 pipe, the
+// scarce one on GB300, also runs the integer-to-double conversion.
+__device__ __forceinline__ double u2d(uint64_t x) {
+  if (x == 0) return 0.0;
+  const int e = 63 - __clzll((long long)x);  // x in [2^e, 2^(e+1)), e <= 52
+  const uint64_t m = x << (52 - e);           // leading 1 at bit 52
+  return __longlong_as_double((long long)(((uint64_t)(e + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull)));
+}
 // a / b, correctly rounded, for a divisor b whose correctly rounded reciprocal y = 1/b is
 // known: q = a y, r = a - b q (exact, one FMA), a / b = RN(q + r y) (P. Markstein,
 // IBM J. Res. Dev. 34(1), 1990).  Finite normal operands and quotient.
@@ -148,6 +156,8 @@ struct Fh {
   // tF and num_states they were taken for
   double inv_minT, inv_tF, inv_ns;
   uint64_t inv_tF_of, inv_ns_of;
+  double tF_d, ns_d;    // (double) tF and num_states for the values above
+  bool g_zero;          // latest_param * tF * num_states == 0 (SAD gamma is 0), per refresh
   bool inverted;        // too_lo > too_hi (never true for SAD; kept exact)
 
   // ---- index helpers ---------------------------------------------------------------
@@ -256,6 +266,8 @@ struct Fh {
     inv_wf = (float)inv_width;
     inv_minT = 1.0 / c.min_T;
     inv_tF_of = 0; inv_ns_of = 0; inv_tF = inv_ns = 0.0;
+    tF_d = ns_d = 0.0;
+    g_zero = true;
   }
   __device__ void store(WalkerCore* cores, int w) {
     if (c.kind != M_DESCENT) flush_cur();
@@ -266,14 +278,15 @@ struct Fh {
   __device__ double gamma_at(uint64_t t) const {
     switch (kind()) {
       case M_SAD: {
-        double p = c.latest_param, tF = (double)c.tF, ns = (double)c.num_states;
-        if (p * tF * ns == 0.0) return 0.0;
-        double td = (double)t;
-        const double t_tF = div_by(td, tF, inv_tF);  // inv_tF, inv_ns refreshed by gamma()
-        return (p + t_tF) / (p + div_by(td, ns, inv_ns) * t_tF);
+        // tF_d, ns_d, their reciprocals and g_zero are refreshed by gamma() for the
+        // current parameters; the expression is compute_gamma's
+        if (g_zero) return 0.0;
+        const double p = c.latest_param, td = u2d(t);
+        const double t_tF = div_by(td, tF_d, inv_tF);
+        return (p + t_tF) / (p + div_by(td, ns_d, inv_ns) * t_tF);
       }
       case M_SAMC: {
-        double td = (double)t;
+        const double td = u2d(t);
         return td > c.t0 ? c.t0 / td : 1.0;
       }
       case M_WL:
@@ -302,8 +315,9 @@ struct Fh {
     }
     if (SADMC_RARE(!((gb_ok >> qc) & 1u))) {
       if (kind() == M_SAD) {
-        if (c.tF != inv_tF_of) { inv_tF = 1.0 / (double)c.tF; inv_tF_of = c.tF; }
-        if (c.num_states != inv_ns_of) { inv_ns = 1.0 / (double)c.num_states; inv_ns_of = c.num_states; }
+        if (c.tF != inv_tF_of) { tF_d = u2d(c.tF); inv_tF = 1.0 / tF_d; inv_tF_of = c.tF; }
+        if (c.num_states != inv_ns_of) { ns_d = u2d(c.num_states); inv_ns = 1.0 / ns_d; inv_ns_of = c.num_states; }
+        g_zero = c.latest_param * tF_d * ns_d == 0.0;
       }
       const uint64_t t0 = c.moves - (uint64_t)off;
       if (off == 0 || LPW == 32) {
@@ -434,10 +448,12 @@ struct Fh {
     if (!possible || !(fabsf(de) <= 3.0e38f)) return true;
     const float e2f = Ef + de;
     const float tol = (fabsf(Ef) + fabsf(e2f)) * 2.5e-7f + 1e-30f;
-    auto exact = [&]() -> double {
-      if (!have) { e2 = c.E + f2d(de); have = true; }
-      return e2;
-    };
+    // The FP64 e2 is formed here, once and by every walker of the warp alike: taken at
+    // each place that needs it, the walkers' different places each cost the warp an FP64
+    // instruction of their own.
+    e2 = c.E + f2d(de);
+    have = true;
+    auto exact = [&]() -> double { return e2; };
     // e2 > T (T's binary32 copy Tf within |T| 2^-23)
     auto gt = [&](float Tf, double T) -> bool {
       const float m = tol + fabsf(Tf) * 2.5e-7f;
@@ -467,15 +483,14 @@ struct Fh {
       if (!prepare(exact())) { c.status |= ST_BIN_RANGE; return true; }
       if (grew_front) reindex_after_growth();
     }
-    // state_to_index
-    if (have) {
-      i2 = gidx(e2);
-    } else {
+    // state_to_index, from the binary32 estimate unless it lies within its error bound
+    // of a bin edge
+    {
       const float q = (e2f - cminf) * inv_wf;
       const int qi = __float2int_rd(q);
       const float fr = q - (float)qi;
       const float m = (tol + fabsf(cminf) * 2.5e-7f) * inv_wf + fabsf(q) * 2.5e-7f + 1e-6f;
-      i2 = (fr > m && fr < 1.0f - m) ? qi + c.b_lo : gidx(exact());
+      i2 = (fr > m && fr < 1.0f - m) ? qi + c.b_lo : gidx(e2);
     }
     if (SADMC_RARE(i2 < c.b_lo || i2 > c.b_hi)) {
       c.status |= ST_BIN_RANGE;
@@ -494,7 +509,7 @@ struct Fh {
         if (SADMC_RARE(!rejected && hist2 == 0)) {  // energy.rs:466-483
           exact();
           if (e2 < c.too_hi && e2 > c.too_lo) {
-            c.latest_param = (c.too_hi - c.too_lo) / c.min_T;
+            c.latest_param = div_by(c.too_hi - c.too_lo, c.min_T, inv_minT);
             c.num_states += 1;
             c.tL = c.moves;
             gb_ok = 0;
@@ -577,7 +592,7 @@ struct Fh {
             else st_lnw(j, 0.0);
           }
         }
-        c.latest_param = (energy - c.too_lo) / c.min_T;
+        c.latest_param = div_by(energy - c.too_lo, c.min_T, inv_minT);
         c.tL = c.moves;
         c.too_hi = center(cur);
         inverted = c.too_lo > c.too_hi;
@@ -605,7 +620,7 @@ struct Fh {
             }
           }
         }
-        c.latest_param = (c.too_hi - energy) / c.min_T;
+        c.latest_param = div_by(c.too_hi - energy, c.min_T, inv_minT);
         c.tL = c.moves;
         c.too_lo = center(cur);
         inverted = c.too_lo > c.too_hi;

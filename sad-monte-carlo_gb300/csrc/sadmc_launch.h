@@ -36,6 +36,10 @@ struct LjSys {
   double radius2;
 };
 cudaError_t launch_lj_move(const MoveLaunch& m, const LjSys& s, int lpw, cudaStream_t st);
+// The shared-memory LJ move kernel with one or two lanes per walker (sadmc_lj_lane.cu),
+// for 32- and 64-atom planes; it runs moves only (no descent).
+bool lj_lane_shape(int lpw, int np);
+cudaError_t launch_lj_lane(const MoveLaunch& m, const LjSys& s, int lpw, cudaStream_t st);
 cudaError_t launch_lj_energy(const WalkerCore* cores, const LjSys& s, int n_walkers, double* out,
                              cudaStream_t st);
 // Injected proposal for one walker (the plan_move parity hook): out[0] = e2 (FP64 sum of

@@ -29,7 +29,8 @@ def make_batch(gpu, n, W, radius, moves_bins, method=0, seed=3, target_rate=0.5,
     return gpu.Batch(cfg, [(n, radius, (0, 0, 0))] * W), cfg
 
 
-@pytest.mark.parametrize("n,lpw", [(13, 8), (31, 8), (31, 4), (31, 32), (38, 8), (38, 16)])
+@pytest.mark.parametrize("n,lpw", [(13, 8), (31, 8), (31, 4), (31, 32), (38, 8), (38, 16), (13, 1),
+                                   (31, 1), (31, 2), (38, 1), (38, 2)])
 def test_lj_trace_replay(gpu, oracle, n, lpw):
     W, moves, radius, seed = 12, 6000, 2.5 if n < 35 else 3.5, 5
     confs = lj_configs(oracle, n, radius, range(100, 100 + W))
@@ -116,7 +117,8 @@ def test_heat_capacity_gpu_vs_oracle(gpu, oracle):
                                rtol=1e-10)
 
 
-def test_lj_c2_launch_geometry_trace_replay(gpu, oracle):
+@pytest.mark.parametrize("lpw", [8, 1])
+def test_lj_c2_launch_geometry_trace_replay(gpu, oracle, lpw):
     """The headline workload's own launch: 4096 LJ31 walkers (R = 2.5, SAD min_T 0.2, 1000
     bins of 0.134 over [-134, 0], max_allowed_energy 0, step 0.1 adapted to 50 %) at its
     default shape, one run traced; walkers from the first, middle and last warps and blocks
@@ -126,7 +128,7 @@ def test_lj_c2_launch_geometry_trace_replay(gpu, oracle):
     confs = sphere_configs(n, radius, W, seed=2000)
     cfg = gpu.make_config(gpu.LJ, W, n, method=0, min_T=0.2, energy_bin=width, max_allowed=0.0,
                           e_lo=-134.0 - 2 * width, e_hi=2 * width, target_rate=0.5,
-                          translation_scale=0.1, seed=seed, lanes_per_walker=8)
+                          translation_scale=0.1, seed=seed, lanes_per_walker=lpw)
     b = gpu.Batch(cfg, [(n, radius, (0, 0, 0))] * W)
     b.upload(confs)
     b.initialize()
@@ -141,7 +143,7 @@ def test_lj_c2_launch_geometry_trace_replay(gpu, oracle):
                                               e0=float(E0[w])), confs[w])
         disc, mismatch = ow.run_override(e1, e2)
         assert mismatch == 0 and disc < REPLAY_REL, (w, mismatch, disc)
-        label = f"C2 launch walker {w}"
+        label = f"C2 launch lpw{lpw} walker {w}"
         assert_bins_equal(b.bins(w), ow.bins(), label=label)
         assert_scalars_equal(b.scalars(w), ow.scalars(), label=label)
         np.testing.assert_allclose(b.state(w), ow.state(), atol=1e-11)
