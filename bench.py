@@ -157,7 +157,10 @@ C3_METHOD = dict(t0=1e4, energy_bin=1.0, max_allowed=500.0, translation_scale=0.
 C5_METHOD = dict(well_width=1.3, translation_scale=0.05)
 
 
-def case_c1(G, seed=11, moves=1_000_000, lpw=0, **_):
+O_FLAGS = "g++ -O3 -ffp-contract=off -mcpu=native (Arm host; -march=native on x86)"
+
+
+def case_c1(G, seed=11, moves=10_000_000, lpw=0, **_):
     """C1: plain SAD, Ising 32x32, one walker, bins of 4 over [-2N, 2N]."""
     L, spins = c1_inputs(seed)
     b = G.Batch(G.make_config(G.ISING, 1, L, method=G.SAD, min_T=0.2, e_lo=-2.0 * L * L - 8,
@@ -310,20 +313,20 @@ def cpu_cases(seed=11):
     L, spins = c1_inputs(seed)
     moves = 2_000_000
     cfg = O.make_config(O.ISING, L, method=O.M_SAD, min_T=0.2, seed=seed, walker=0)
-    sec, tm, _ = O.bench([cfg], [spins], moves, 1)
+    sec, tm, _ = O.bench([cfg], [spins], moves, 1, native=True)
     out["C1"] = {"moves_per_s": tm / sec, "threads": 1, "sample": f"1 walker x {moves} moves"}
     w3, m3 = 256, 8000
     inp = c3_inputs(seed, w3)
     cfgs = [O.make_config(O.WCA, n, box=(Lb, Lb, Lb), method=O.M_SAMC, seed=seed, walker=w,
                           **C3_METHOD) for w, (n, Lb, _) in enumerate(inp)]
-    sec, tm, _ = O.bench(cfgs, [p for _, _, p in inp], m3, threads)
+    sec, tm, _ = O.bench(cfgs, [p for _, _, p in inp], m3, threads, native=True)
     out["C3"] = {"moves_per_s": tm / sec, "threads": threads,
                  "sample": f"first {w3} walkers x {m3} moves"}
     w5, m5 = 128, 8000
     inp = c5_inputs(seed, w5)
     cfgs = [O.make_config(O.SW, 1024, box=(Lb, Lb, Lb), method=O.M_WL, seed=seed, walker=w,
                           **C5_METHOD) for w, (Lb, _) in enumerate(inp)]
-    sec, tm, _ = O.bench(cfgs, [p for _, p in inp], m5, threads)
+    sec, tm, _ = O.bench(cfgs, [p for _, p in inp], m5, threads, native=True)
     out["C5"] = {"moves_per_s": tm / sec, "threads": threads,
                  "sample": f"first {w5} walkers x {m5} moves"}
     return out
@@ -593,7 +596,7 @@ def cpu_sample(threads, walkers=128, moves=100000, seed=7):
     cfgs = [O.make_config(O.LJ, N_ATOMS, radius=RADIUS, method=O.M_SAD, min_T=0.2,
                           energy_bin=WIDTH, max_allowed=0.0, target_rate=0.5,
                           translation_scale=0.1, seed=seed, walker=w) for w in range(walkers)]
-    sec, tm, ta = O.bench(cfgs, [c.reshape(-1) for c in confs], moves, threads)
+    sec, tm, ta = O.bench(cfgs, [c.reshape(-1) for c in confs], moves, threads, native=True)
     return tm / sec, ta / sec, sec, tm
 
 
@@ -619,7 +622,8 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": "moves/s", "cores": threads, "kind": "port",
                          "per_core": value / threads,
                          "sample": f"{walkers} C2 walkers x {moves} moves per step, FP64 C++ "
-                                   "restatement of the reference (Rust toolchain absent)"},
+                                   "restatement of the reference (Rust toolchain absent), built "
+                                   f"{O_FLAGS}"},
         "e2e": {"value": value, "unit": "moves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -740,7 +744,7 @@ def run_gpu(args):
         cpu = {"value": v, "unit": "moves/s", "cores": threads, "kind": "port",
                "per_core": v / threads, "accepted_moves_per_s": va,
                "sample": f"256 C2 walkers x 200000 moves ({tm} moves, {sec:.2f} s wall), FP64 "
-                         "C++ restatement of the reference (Rust toolchain absent)"}
+                         f"C++ restatement of the reference (Rust toolchain absent), built {O_FLAGS}"}
 
     if rank == 0:
         line = {

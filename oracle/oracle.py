@@ -45,15 +45,20 @@ def build():
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
 
 
-_lib = None
+_libs = {}
+# the timed CPU baseline: the same sources built for the host's own cores (oracle/Makefile)
+NATIVE_FLAGS = "g++ -O3 -ffp-contract=off -mcpu=native (Arm) / -march=native (x86)"
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(_LIB_PATH):
+def lib(native=False):
+    """The oracle library; native=True loads the host-tuned build of the same sources,
+    which the CPU baseline times (its results are the checker's)."""
+    key = bool(native)
+    if key not in _libs:
+        path = _LIB_PATH.replace(".so", "_native.so") if native else _LIB_PATH
+        if not os.path.exists(path):
             build()
-        L = ctypes.CDLL(_LIB_PATH)
+        L = ctypes.CDLL(path)
         P, D, U64, I32, U32, I64 = (ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64,
                                     ctypes.c_int32, ctypes.c_uint32, ctypes.c_int64)
         sig = {
@@ -101,8 +106,8 @@ def lib():
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
-        _lib = L
-    return _lib
+        _libs[key] = L
+    return _libs[key]
 
 
 def _p(a):
@@ -415,13 +420,13 @@ def selftest_cell(walker):
     return lib().orc_selftest_cell(walker.h)
 
 
-def bench(cfgs, states, moves, threads):
+def bench(cfgs, states, moves, threads, native=False):
     """Time `moves` moves of each walker on `threads` host threads; returns
-    (seconds, total_moves, total_accepted)."""
+    (seconds, total_moves, total_accepted).  native: the host-tuned build."""
     n = len(cfgs)
     arr = (Config * n)(*cfgs)
     keep = [np.ascontiguousarray(s, np.float64) for s in states]
     ptrs = (ctypes.c_void_p * n)(*[k.ctypes.data for k in keep])
     tm, ta = ctypes.c_uint64(0), ctypes.c_uint64(0)
-    sec = lib().orc_bench(arr, ptrs, n, int(moves), threads, ctypes.byref(tm), ctypes.byref(ta))
+    sec = lib(native).orc_bench(arr, ptrs, n, int(moves), threads, ctypes.byref(tm), ctypes.byref(ta))
     return sec, tm.value, ta.value

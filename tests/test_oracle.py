@@ -247,3 +247,17 @@ def test_bf16_rounding_is_nearest_even():
     assert r[2] == 1.0 + 2 ** -7            # above the midpoint
     assert r[3] == 1.0 + 2 ** -6            # midpoint, ties to even (up)
     assert r[4] == -3.140625
+
+
+def test_native_build_is_the_checker(oracle):
+    """The host-tuned build of the oracle that the CPU baseline times (-mcpu/-march=native,
+    still without contraction) runs the same chains as the checker build, move for move."""
+    from helpers import sphere_configs
+    confs = sphere_configs(31, 2.5, 4, 5)
+    cfgs = [oracle.make_config(oracle.LJ, 31, radius=2.5, method=oracle.M_SAD, min_T=0.2,
+                               energy_bin=0.134, max_allowed=0.0, target_rate=0.5,
+                               translation_scale=0.1, seed=3, walker=w) for w in range(4)]
+    states = [c.reshape(-1) for c in confs]
+    _, m0, a0 = oracle.bench(cfgs, states, 50_000, 4)
+    _, m1, a1 = oracle.bench(cfgs, states, 50_000, 4, native=True)
+    assert (m0, a0) == (m1, a1)
