@@ -266,8 +266,10 @@ int32_t sadmc_surrogate_predict(sadmc_handle* h, const float* pos, int32_t confi
  * instructions (a diagnostic with no counterpart in the reference): over n seeded cases,
  * mismatches[0] counts divisions by a known reciprocal that differ from a / b,
  * mismatches[1] integer float-to-double conversions that differ from the cast (n bit
- * patterns), mismatches[2] binary32-first Metropolis tests that differ from the FP64 one;
- * first (optional) gets the first division mismatch (a, b). */
+ * patterns), mismatches[2] binary32-first Metropolis tests that differ from the FP64 one,
+ * mismatches[3] integer-instruction comparisons of finite doubles that differ from < or >,
+ * mismatches[4] integer-instruction conversions of integers below 2^53 that differ from the
+ * cast (5 entries); first (optional) gets the first division mismatch (a, b). */
 int32_t sadmc_check_numerics(uint64_t n, uint64_t seed, uint64_t* mismatches, double* first);
 
 /* The counter-based draws the kernels consume for moves t0 .. t0+count-1 of one walker

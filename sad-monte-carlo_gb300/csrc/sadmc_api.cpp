@@ -1445,12 +1445,12 @@ int32_t sadmc_check_numerics(uint64_t n, uint64_t seed, uint64_t* mismatches, do
   if (!mismatches) return fail(SADMC_ERR_INVALID, "null argument");
   unsigned long long* d = nullptr;
   double* df = nullptr;
-  cudaError_t e = cudaMalloc(&d, sizeof(unsigned long long) * 3);
+  cudaError_t e = cudaMalloc(&d, sizeof(unsigned long long) * 5);
   if (e == cudaSuccess) e = cudaMalloc(&df, sizeof(double) * 2);
-  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(unsigned long long) * 3);
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(unsigned long long) * 5);
   if (e == cudaSuccess) e = cudaMemset(df, 0, sizeof(double) * 2);
   if (e == cudaSuccess) e = launch_numerics_check(n, seed, d, df, 0);
-  if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof(unsigned long long) * 5, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && first) e = cudaMemcpy(first, df, sizeof(double) * 2, cudaMemcpyDeviceToHost);
   cudaFree(d);
   cudaFree(df);

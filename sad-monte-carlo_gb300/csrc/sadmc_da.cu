@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(32 * DA_WPB) lj_da_kernel(MoveLaunch m, LjSys 
   Fh<32> fh;
   fh.load(m.cores, m.P, m.B, w, 0xffffffffu, lane, true);
   LjWalker<32, APL> lj;
+  lj.set_radius2(s.radius2);
   lj.glane = lane;
   lj.gmask = 0xffffffffu;
   lj.n = fh.c.n;

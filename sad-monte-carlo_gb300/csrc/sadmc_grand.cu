@@ -35,6 +35,7 @@ __global__ void __launch_bounds__(128) lj_grand_kernel(GrandLaunch m) {
   GrandBook<LPW> bk;
   bk.load(m, w, glane, gmask);
   LjWalker<LPW, APL> lj;
+  lj.set_radius2(m.radius2);
   lj.glane = glane;
   lj.gmask = gmask;
   lj.n = bk.c.N;

@@ -14,6 +14,7 @@ __global__ void lj_energy_kernel(const WalkerCore* cores, LjSys s, int n_walkers
   const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (w >= n_walkers) return;
   LjWalker<32, APL> lj;
+  lj.set_radius2(s.radius2);
   lj.glane = lane;
   lj.gmask = 0xffffffffu;
   lj.n = cores[w].n;
@@ -27,6 +28,7 @@ __global__ void lj_plan_kernel(WalkerCore* cores, LjSys s, int w, int which, flo
                                float g2, double scale, int confirm, double* out) {
   const int lane = threadIdx.x & 31;
   LjWalker<32, APL> lj;
+  lj.set_radius2(s.radius2);
   lj.glane = lane;
   lj.gmask = 0xffffffffu;
   lj.n = cores[w].n;
@@ -48,8 +50,12 @@ __global__ void lj_plan_kernel(WalkerCore* cores, LjSys s, int w, int which, flo
 }  // namespace dev
 
 cudaError_t launch_lj_move(const MoveLaunch& m, const LjSys& s, int lpw, cudaStream_t st) {
-  if (m.method == M_SAD) return launch_lj_move_sad(m, s, lpw, st);
-  SADMC_LJ_ALL_SHAPES(dev::FAM_ANY)
+  if (m.method == M_SAD && !m.descent) return launch_lj_move_sad(m, s, lpw, st);
+  if (m.descent) {
+    SADMC_LJ_ALL_SHAPES(dev::FAM_ANY, true)
+  } else {
+    SADMC_LJ_ALL_SHAPES(dev::FAM_ANY, false)
+  }
   return cudaErrorInvalidConfiguration;
 }
 

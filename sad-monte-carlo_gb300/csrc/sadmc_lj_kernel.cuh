@@ -23,7 +23,9 @@
 namespace sadmc {
 namespace dev {
 
-template <int LPW, int APL, int FAM>
+// DESC: the initial descent (its own instantiation, so that the move kernel's code holds
+// only the move loop).
+template <int LPW, int APL, int FAM, bool DESC>
 __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
   constexpr int WPW = 32 / LPW;
   const int lane = threadIdx.x & 31;
@@ -38,13 +40,14 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
   Fh<LPW, FAM> fh;
   fh.load(m.cores, m.P, m.B, w, gmask, glane, wr);
   LjWalker<LPW, APL> lj;
+  lj.set_radius2(s.radius2);
   lj.glane = glane;
   lj.gmask = gmask;
   lj.n = fh.c.n;
   float* pw = s.pos + (size_t)w * 6 * (size_t)s.np;
   lj.load(pw, s.np);
 
-  if (m.descent) {
+  if (DESC) {
     // from_params descent (energy.rs:840-851): downhill-only proposals of rms 0.05 on
     // the descent stream until E < max_allowed_energy.
     const DS sc = ds_from_double(0.05);
@@ -127,17 +130,19 @@ __global__ void __launch_bounds__(128) lj_move_kernel(MoveLaunch m, LjSys s) {
 
 }  // namespace dev
 
-// Launch lj_move_kernel<LPW, APL, FAM> for the (lanes per walker, atoms per lane) shape.
-#define SADMC_LJ_CASE(L, A, F)                                                         \
+// Launch lj_move_kernel<LPW, APL, FAM, D> for the (lanes per walker, atoms per lane) shape;
+// D true only for the descent launches (method-generic translation unit).
+#define SADMC_LJ_CASE(L, A, F, D)                                                      \
   if (lpw == L && s.np == L * A) {                                                     \
     const int wpb = m.warps_per_block >= 1 && m.warps_per_block <= 4 ? m.warps_per_block : 4; \
     const int warps = (m.n_walkers + (32 / L) - 1) / (32 / L);                         \
-    dev::lj_move_kernel<L, A, F><<<(warps + wpb - 1) / wpb, 32 * wpb, 0, st>>>(m, s);  \
+    if (D) dev::lj_move_kernel<L, A, F, D><<<(warps + wpb - 1) / wpb, 32 * wpb, 0, st>>>(m, s); \
+    else dev::lj_move_kernel<L, A, F, false><<<(warps + wpb - 1) / wpb, 32 * wpb, 0, st>>>(m, s); \
     return cudaGetLastError();                                                         \
   }
-#define SADMC_LJ_ALL_SHAPES(F)                                                         \
-  SADMC_LJ_CASE(32, 1, F) SADMC_LJ_CASE(16, 2, F) SADMC_LJ_CASE(8, 4, F)               \
-  SADMC_LJ_CASE(4, 8, F) SADMC_LJ_CASE(32, 2, F) SADMC_LJ_CASE(16, 4, F)               \
-  SADMC_LJ_CASE(8, 8, F) SADMC_LJ_CASE(32, 4, F) SADMC_LJ_CASE(32, 8, F)
+#define SADMC_LJ_ALL_SHAPES(F, D)                                                      \
+  SADMC_LJ_CASE(32, 1, F, D) SADMC_LJ_CASE(16, 2, F, D) SADMC_LJ_CASE(8, 4, F, D)      \
+  SADMC_LJ_CASE(4, 8, F, D) SADMC_LJ_CASE(32, 2, F, D) SADMC_LJ_CASE(16, 4, F, D)      \
+  SADMC_LJ_CASE(8, 8, F, D) SADMC_LJ_CASE(32, 4, F, D) SADMC_LJ_CASE(32, 8, F, D)
 
 }  // namespace sadmc

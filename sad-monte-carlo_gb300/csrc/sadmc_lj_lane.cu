@@ -44,6 +44,7 @@ struct LjLaneWalker {
   int glane;
   unsigned gmask;
   int n;
+  float wall_r2f;  // binary32 R^2 of the wall, set once per launch
 
   __device__ float2& at(int c, int j) const { return sp[(c * NP + j) * WPW + slot]; }
   __device__ void load(const float* p) {
@@ -88,7 +89,7 @@ struct LjLaneWalker {
     // wall: impossible iff |to|^2 > R^2 and |to|^2 > |from|^2 (lj.rs:87-90)
     const float r2t = tx.h * tx.h + ty.h * ty.h + tz.h * tz.h;
     const float r2f = fx.h * fx.h + fy.h * fy.h + fz.h * fz.h;
-    const float R2 = (float)radius2;
+    const float R2 = wall_r2f;
     bool impossible;
     if (r2t < R2 * (1.0f - 1e-5f)) {
       impossible = false;
@@ -164,6 +165,7 @@ __global__ void __launch_bounds__(128) lj_lane_kernel(MoveLaunch m, LjSys s) {
   lj.glane = glane;
   lj.gmask = gmask;
   lj.n = fh.c.n;
+  lj.wall_r2f = __double2float_rn(s.radius2);
   float* pw = s.pos + (size_t)w * 6 * (size_t)NP;
   lj.load(pw);
   if (LPW > 1) __syncwarp();

@@ -5,7 +5,7 @@
 namespace sadmc {
 
 cudaError_t launch_lj_move_sad(const MoveLaunch& m, const LjSys& s, int lpw, cudaStream_t st) {
-  SADMC_LJ_ALL_SHAPES(M_SAD)
+  SADMC_LJ_ALL_SHAPES(M_SAD, false)
   return cudaErrorInvalidConfiguration;
 }
 

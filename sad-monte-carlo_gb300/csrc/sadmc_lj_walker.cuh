@@ -18,6 +18,8 @@ struct LjWalker {
   int n;
   int glane;
   unsigned gmask;
+  float wall_r2f;  // binary32 R^2 of the wall, set once per launch (set_radius2)
+  __device__ void set_radius2(double r2) { wall_r2f = __double2float_rn(r2); }
 
   __device__ void load(const float* p, int np) {
 #pragma unroll
@@ -71,7 +73,7 @@ struct LjWalker {
     // wall: impossible iff |to|^2 > R^2 and |to|^2 > |from|^2 (lj.rs:87-90)
     const float r2t = tx.h * tx.h + ty.h * ty.h + tz.h * tz.h;
     const float r2f = fx.h * fx.h + fy.h * fy.h + fz.h * fz.h;
-    const float R2 = (float)radius2;
+    const float R2 = wall_r2f;
     bool impossible;
     if (r2t < R2 * (1.0f - 1e-5f)) {
       impossible = false;

@@ -268,8 +268,10 @@ __device__ __forceinline__ double rnd_double(uint64_t r, int emin, int emax) {
 }
 
 // out[0]: div_by(a, b, 1/b) != a / b; out[1]: f2d(f) != (double)f over the 2^32 bit
-// patterns visited; out[2]: metropolis_reject2 != metropolis_reject; out[3..4]: the
-// first division mismatch (a, b).
+// patterns visited; out[2]: metropolis_reject2 != metropolis_reject; out[3]: dlt(x, y) !=
+// (x < y) on finite doubles (signed zeros, equal values, neighbours one ulp apart and
+// mixed signs among them); out[4]: u2d(k) != (double)k on integers below 2^53.  first:
+// the first division mismatch (a, b).
 __global__ void numerics_check_kernel(uint64_t n, uint64_t seed, unsigned long long* out, double* first) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
@@ -308,6 +310,22 @@ __global__ void numerics_check_kernel(uint64_t n, uint64_t seed, unsigned long l
     const double l2 = l1 + (double)((r2 >> 3) & 0xFFFF) * (1.0 / 4096.0) * ((r & 2) ? 1.0 : 1e-6);
     const uint64_t u53 = mix64(r ^ r2) >> 11;
     if (metropolis_reject2(l1, l2, u53) != metropolis_reject(l1 - l2, u53)) atomicAdd(&out[2], 1ull);
+    // ordered comparison by integer instructions
+    double x = rnd_double(r2 ^ 0x5DEECE66Dull, -1022, 1023) * ((r & 4) ? -1.0 : 1.0);
+    double y;
+    switch ((r >> 3) & 7) {
+      case 0: y = x; break;                                                      // equal
+      case 1: y = __longlong_as_double(__double_as_longlong(x) + 1); break;      // next ulp
+      case 2: y = __longlong_as_double(__double_as_longlong(x) - 1); break;      // previous ulp
+      case 3: y = -x; break;                                                     // sign flip
+      case 4: x = (r & 8) ? -0.0 : 0.0; y = (r & 16) ? -0.0 : 0.0; break;        // signed zeros
+      case 5: y = (r & 16) ? -0.0 : 0.0; break;                                  // against zero
+      default: y = rnd_double(mix64(r2), -1022, 1023) * ((r & 32) ? -1.0 : 1.0); break;
+    }
+    if (isfinite(x) && isfinite(y) && (dlt(x, y) != (x < y) || dgt(x, y) != (x > y))) atomicAdd(&out[3], 1ull);
+    // integer-to-double conversion below 2^53, all magnitudes
+    const uint64_t k = (r ^ r2) >> (11 + (int)((r >> 40) % 53));
+    if (__double_as_longlong(u2d(k)) != __double_as_longlong((double)k)) atomicAdd(&out[4], 1ull);
   }
 }
 

@@ -582,7 +582,7 @@ class GrandBatch:
 def check_numerics(n, seed=1):
     """Mismatch counts of the exact FP64 rewrites against CUDA's own operations (see
     sadmc_check_numerics) and the first mismatching division (a, b)."""
-    out = np.zeros(3, np.uint64)
+    out = np.zeros(5, np.uint64)
     first = np.zeros(2)
     _check(lib().sadmc_check_numerics(int(n), int(seed), _p(out), _p(first)))
     return out, first
