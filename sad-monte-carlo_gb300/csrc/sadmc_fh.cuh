@@ -127,6 +127,17 @@ __device__ __forceinline__ bool metropolis_reject2(double lnw1, double lnw2, uin
   return metropolis_reject(lnw1 - lnw2, u53);
 }
 
+// SadVersion::compute_gamma (energy.rs:22-38) for move count t and parameters (p, tF, ns),
+// with the same operations as Fh::gamma_at (reciprocals, Markstein divisions), so that a
+// lane filling a table computes the bits the walker's own lane would.
+__device__ __forceinline__ double sad_gamma_value(double p, uint64_t tF, uint64_t ns, uint64_t t) {
+  const double tF_d = u2d(tF), ns_d = u2d(ns);
+  if (p * tF_d * ns_d == 0.0) return 0.0;
+  const double td = u2d(t);
+  const double t_tF = div_by(td, tF_d, 1.0 / tF_d);
+  return (p + t_tF) / (p + div_by(td, ns_d, 1.0 / ns_d) * t_tF);
+}
+
 // FAM: the method a kernel is specialised for (M_SAD, ...), or FAM_ANY for the kind held
 // in each walker's state (WL and 1/t-WL, whose walkers switch to SAMC at run time).
 constexpr int FAM_ANY = -1;
@@ -173,6 +184,13 @@ struct Fh {
   uint64_t inv_tF_of, inv_ns_of;
   double tF_d, ns_d;    // (double) tF and num_states for the values above
   bool g_zero;          // latest_param * tF * num_states == 0 (SAD gamma is 0), per refresh
+  // A table of gamma for the moves [xg_t0, xg_t0 + 32), filled by a whole warp for a
+  // walker that one lane runs (the single-walker chain kernel); valid while xg_ok, that
+  // is until the method's parameters change.  Null for the other kernels.
+  const double* xg;
+  uint64_t xg_t0;
+  bool xg_ok;
+  __device__ void invalidate_gamma() { gb_ok = 0; xg_ok = false; }
   bool inverted;        // too_lo > too_hi (never true for SAD; kept exact)
 
   // ---- index helpers ---------------------------------------------------------------
@@ -283,6 +301,9 @@ struct Fh {
     inv_tF_of = 0; inv_ns_of = 0; inv_tF = inv_ns = 0.0;
     tF_d = ns_d = 0.0;
     g_zero = true;
+    xg = nullptr;
+    xg_t0 = 0;
+    xg_ok = false;
   }
   __device__ void store(WalkerCore* cores, int w) {
     if (c.kind != M_DESCENT) flush_cur();
@@ -317,8 +338,20 @@ struct Fh {
   // slot of the current move, one chain per lane for the next LPW moves, where other
   // walkers share the warp.  (The low 32
   // bits of the count suffice: a batch is replaced at least every 4*LPW moves.)
+  // tF_d, ns_d, their reciprocals and g_zero for the current SAD parameters
+  __device__ void refresh_sad_params() {
+    if (c.tF != inv_tF_of) { tF_d = u2d(c.tF); inv_tF = 1.0 / tF_d; inv_tF_of = c.tF; }
+    if (c.num_states != inv_ns_of) { ns_d = u2d(c.num_states); inv_ns = 1.0 / ns_d; inv_ns_of = c.num_states; }
+    g_zero = c.latest_param * tF_d * ns_d == 0.0;
+  }
   __device__ double gamma() {
     if (kind() != M_SAD && kind() != M_SAMC) return gamma_at(c.moves);
+    if (xg) {  // the warp's table, or this lane alone after a parameter change
+      const uint64_t k = c.moves - xg_t0;
+      if (xg_ok && k < 32) return xg[k];
+      if (kind() == M_SAD) refresh_sad_params();
+      return gamma_at(c.moves);
+    }
     constexpr uint32_t SPAN = 4 * LPW;
     const uint32_t m32 = (uint32_t)c.moves;
     const uint32_t base = m32 & ~(SPAN - 1);
@@ -329,11 +362,7 @@ struct Fh {
       gb_ok = 0;
     }
     if (SADMC_RARE(!((gb_ok >> qc) & 1u))) {
-      if (kind() == M_SAD) {
-        if (c.tF != inv_tF_of) { tF_d = u2d(c.tF); inv_tF = 1.0 / tF_d; inv_tF_of = c.tF; }
-        if (c.num_states != inv_ns_of) { ns_d = u2d(c.num_states); inv_ns = 1.0 / ns_d; inv_ns_of = c.num_states; }
-        g_zero = c.latest_param * tF_d * ns_d == 0.0;
-      }
+      if (kind() == M_SAD) refresh_sad_params();
       const uint64_t t0 = c.moves - (uint64_t)off;
       if (off == 0 || LPW == 32) {
         // the batch boundary, or a warp that holds one walker (its chains run in parallel,
@@ -527,7 +556,7 @@ struct Fh {
             c.latest_param = div_by(c.too_hi - c.too_lo, c.min_T, inv_minT);
             c.num_states += 1;
             c.tL = c.moves;
-            gb_ok = 0;
+            invalidate_gamma();
           }
         }
         break;
@@ -617,7 +646,7 @@ struct Fh {
           if (t > c.win_tmax) c.win_tmax = t;
         }
         win_hi = nhi;
-        gb_ok = 0;
+        invalidate_gamma();
       } else if (e_below) {
         const double base = ld_lnw(win_lo);
         const int jlo = cur > c.b_lo ? cur : c.b_lo;
@@ -645,13 +674,13 @@ struct Fh {
           if (t > c.win_tmax) c.win_tmax = t;
         }
         win_lo = nlo;
-        gb_ok = 0;
+        invalidate_gamma();
       }
     }
     if (SADMC_RARE(c.tL == c.moves)) {
       uint64_t old_tF = c.tF;
       c.tF = c.win_tmax;
-      gb_ok = 0;
+      invalidate_gamma();
       if (old_tF != c.tF && acc_mode) {  // energy.rs:600-609
         double s = c.acc_rate / target_rate;
         s = s < 0.8 ? 0.8 : (s > 1.2 ? 1.2 : s);
@@ -745,7 +774,7 @@ struct Fh {
       if (inv_t && c.gamma < c.wl_num_states / (double)c.moves) {  // energy.rs:747-750
         c.kind = M_SAMC;
         c.t0 = c.wl_num_states;
-        gb_ok = 0;
+        invalidate_gamma();
       }
     }
   }

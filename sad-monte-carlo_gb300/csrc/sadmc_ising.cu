@@ -3,10 +3,9 @@
 // Spins are int8 in global memory, index i + j*L (ising.rs:64).  A single-spin flip
 // changes E by -2 s_ij (sum of 4 periodic neighbours) (ising.rs:104-119); energies are
 // integers held in FP64, so the whole chain is bit-exact.  With LPW == 1 each lane is a
-// walker; with LPW == 32 one walker occupies a warp (the serial single-walker case).
-// STAGED (LPW == 32, one warp per block): the walker's bin planes and spins are copied
-// to shared memory for the launch and back at its end, so the serial chain of a lone
-// walker waits on shared-memory latency instead of L2 round trips after its own stores.
+// walker; with LPW == 32 one walker occupies a warp: its moves run as a serial chain on
+// one lane (sadmc_ising_chain.cu) when its planes fit in shared memory, here otherwise,
+// and its initial descent here.
 #include <cuda_runtime.h>
 
 #include "sadmc_common.cuh"
@@ -17,12 +16,7 @@
 namespace sadmc {
 namespace dev {
 
-// Bytes of shared memory a staged walker needs: 8 planes of 8 B per bin, then the spins.
-__host__ __device__ inline size_t ising_stage_bytes(int nbins, int L) {
-  return (size_t)nbins * 64 + (((size_t)L * (size_t)L + 15) & ~(size_t)15);
-}
-
-template <int LPW, bool STAGED>
+template <int LPW>
 __global__ void __launch_bounds__(128) ising_move_kernel(MoveLaunch m, IsingSys s) {
   constexpr int WPW = 32 / LPW;
   const int lane = threadIdx.x & 31;
@@ -69,26 +63,6 @@ __global__ void __launch_bounds__(128) ising_move_kernel(MoveLaunch m, IsingSys 
     if (wr && glane == 0) m.cores[w] = fh.c;
     return;
   }
-  extern __shared__ __align__(16) unsigned char stage[];
-  const int nb = m.P.nbins;
-  double* gp[3] = {fh.lnw, fh.sE, fh.sE2};
-  uint64_t* gq[5] = {fh.hist, fh.tf, fh.rt, fh.wlh, fh.stamp};
-  int8_t* gS = S;
-  if (STAGED) {
-    double* sd = reinterpret_cast<double*>(stage);
-    uint64_t* sq = reinterpret_cast<uint64_t*>(sd + 3 * (size_t)nb);
-    for (int a = 0; a < 3; ++a)
-      for (int k = glane; k < nb; k += LPW) sd[(size_t)a * nb + k] = gp[a][k];
-    for (int a = 0; a < 5; ++a)
-      for (int k = glane; k < nb; k += LPW) sq[(size_t)a * nb + k] = gq[a][k];
-    int8_t* sS = reinterpret_cast<int8_t*>(sq + 5 * (size_t)nb);
-    for (int k = glane; k < L * L; k += LPW) sS[k] = gS[k];
-    __syncwarp(gmask);
-    fh.lnw = sd; fh.sE = sd + nb; fh.sE2 = sd + 2 * (size_t)nb;
-    fh.hist = sq; fh.tf = sq + nb; fh.rt = sq + 2 * (size_t)nb; fh.wlh = sq + 3 * (size_t)nb;
-    fh.stamp = sq + 4 * (size_t)nb;
-    S = sS;
-  }
   RecentScale rsb;
   rsb.init();
   DrawCache<LPW, true> dc;
@@ -120,19 +94,6 @@ __global__ void __launch_bounds__(128) ising_move_kernel(MoveLaunch m, IsingSys 
     fh.finish_move(acc);
   }
   fh.store(m.cores, w);
-  if (STAGED) {
-    __syncwarp(gmask);
-    if (wr) {
-      for (int a = 0; a < 3; ++a) {
-        const double* src = a == 0 ? fh.lnw : (a == 1 ? fh.sE : fh.sE2);
-        for (int k = glane; k < nb; k += LPW) gp[a][k] = src[k];
-      }
-      const uint64_t* sq = fh.hist;
-      for (int a = 0; a < 5; ++a)
-        for (int k = glane; k < nb; k += LPW) gq[a][k] = sq[(size_t)a * nb + k];
-      for (int k = glane; k < L * L; k += LPW) gS[k] = S[k];
-    }
-  }
 }
 
 // compute_energy (ising.rs:59-75): sum over sites of s * (s_down + s_right), exact.
@@ -155,7 +116,7 @@ __global__ void ising_energy_kernel(IsingSys s, int n_walkers, double* out) {
 
 }  // namespace dev
 
-// Largest staged walker (bins and spins): 200 KB of the 227 KB a block may hold.
+// Largest single-walker chain (bins, spins, tables): 200 KB of the 227 KB a block may hold.
 constexpr size_t kIsingStageMax = 200 * 1024;
 
 cudaError_t launch_ising_move(const MoveLaunch& m, const IsingSys& s, int lpw, cudaStream_t st) {
@@ -164,25 +125,13 @@ cudaError_t launch_ising_move(const MoveLaunch& m, const IsingSys& s, int lpw, c
   const int wpb = m.warps_per_block >= 1 && m.warps_per_block <= 4 ? m.warps_per_block : 4;
   const int blocks = (warps + wpb - 1) / wpb;
   if (lpw == 1) {
-    dev::ising_move_kernel<1, false><<<blocks, 32 * wpb, 0, st>>>(m, s);
+    dev::ising_move_kernel<1><<<blocks, 32 * wpb, 0, st>>>(m, s);
   } else if (lpw == 32) {
-    // a lone walker per warp: stage its planes and spins when they fit in shared memory
-    const size_t bytes = dev::ising_stage_bytes(m.P.nbins, s.L);
-    if (!m.descent && bytes <= kIsingStageMax) {
-      static bool attr[64] = {};  // the attribute is set once per device
-      int device = 0;
-      cudaError_t e = cudaGetDevice(&device);
-      if (e != cudaSuccess) return e;
-      if (device < 0 || device >= 64 || !attr[device]) {
-        e = cudaFuncSetAttribute(dev::ising_move_kernel<32, true>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kIsingStageMax);
-        if (e != cudaSuccess) return e;
-        if (device >= 0 && device < 64) attr[device] = true;
-      }
-      dev::ising_move_kernel<32, true><<<warps, 32, bytes, st>>>(m, s);
-    } else {
-      dev::ising_move_kernel<32, false><<<blocks, 32 * wpb, 0, st>>>(m, s);
-    }
+    // a lone walker per warp: its moves as a serial chain on one lane when its planes and
+    // spins fit in shared memory
+    if (!m.descent && ising_chain_bytes(m.P.nbins, s.L) <= kIsingStageMax)
+      return launch_ising_chain(m, s, kIsingStageMax, st);
+    dev::ising_move_kernel<32><<<blocks, 32 * wpb, 0, st>>>(m, s);
   } else {
     return cudaErrorInvalidConfiguration;
   }

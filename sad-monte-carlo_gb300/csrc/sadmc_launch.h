@@ -61,6 +61,10 @@ struct IsingSys {
   int8_t* spins;
   int L;
 };
+// One Ising walker per block as a serial chain on one lane, planes and spins in shared
+// memory (sadmc_ising_chain.cu); moves only, up to max_bytes of shared memory.
+size_t ising_chain_bytes(int nbins, int L);
+cudaError_t launch_ising_chain(const MoveLaunch& m, const IsingSys& s, size_t max_bytes, cudaStream_t st);
 cudaError_t launch_ising_move(const MoveLaunch& m, const IsingSys& s, int lpw, cudaStream_t st);
 cudaError_t launch_ising_energy(const IsingSys& s, int n_walkers, double* out, cudaStream_t st);
 

@@ -31,8 +31,10 @@ def run_pair(gpu, oracle, L, W, moves, method, seed=17, lpw=0, chunks=1):
 @pytest.mark.parametrize("method", ["sad", "wl", "inv_t_wl", "samc", "canonical"])
 @pytest.mark.parametrize("lpw", [0, 32])
 def test_ising_batch_bit_exact(gpu, oracle, method, lpw):
-    """lpw 32: one walker per warp with its bins and spins staged in shared memory for each
-    of the three launches."""
+    """lpw 32: one walker per warp, run as a serial chain on one lane with its bins and spins
+    in shared memory and the warp filling draw and gamma tables 32 moves ahead, for each of
+    the three launches (SAD specialised; Wang-Landau, 1/t-WL switching to SAMC, SAMC and
+    canonical through the generic bookkeeping)."""
     b, ws = run_pair(gpu, oracle, L=8, W=40, moves=30000, method=method, chunks=3, lpw=lpw)
     for w in range(b.W):
         label = f"{method} walker {w}"
@@ -49,16 +51,17 @@ def test_ising_batch_bit_exact(gpu, oracle, method, lpw):
 
 
 def test_ising_single_walker_32x32(gpu, oracle):
-    """The one-walker 32x32 SAD chain (one warp per walker)."""
-    b, ws = run_pair(gpu, oracle, L=32, W=1, moves=200000, method="sad", lpw=32)
+    """The one-walker 32x32 SAD chain (the C1 shape), over launches whose move counts are
+    not multiples of the 32-move table batches."""
+    b, ws = run_pair(gpu, oracle, L=32, W=1, moves=200001, method="sad", lpw=32, chunks=3)
     assert_bins_equal(b.bins(0), ws[0].bins(), label="L32")
     assert_scalars_equal(b.scalars(0), ws[0].scalars(), label="L32")
     np.testing.assert_array_equal(b.state(0), ws[0].state())
 
 
 def test_ising_single_walker_unstaged(gpu, oracle):
-    """64x64: the bins and spins (about 266 KB) exceed the shared-memory stage, so the
-    lone walker runs on its planes in global memory."""
+    """64x64: the bins and spins (about 266 KB) exceed the shared memory of a block, so the
+    lone walker runs on its planes in global memory (the warp-per-walker kernel)."""
     b, ws = run_pair(gpu, oracle, L=64, W=1, moves=60000, method="sad", lpw=32, chunks=2)
     assert_bins_equal(b.bins(0), ws[0].bins(), label="L64")
     assert_scalars_equal(b.scalars(0), ws[0].scalars(), label="L64")
