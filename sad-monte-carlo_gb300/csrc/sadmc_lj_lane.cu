@@ -8,9 +8,11 @@
 // (or two), at full FP32 rate.
 //
 // Layout: each warp holds its walkers' double-single positions (hi, lo as a float2) in
-// shared memory as [coordinate][atom][walker of the warp], so that the 32 lanes of a
-// warp reading "their" atom j touch 32 consecutive 8-byte words (two wavefronts, no bank
-// conflict).  With two lanes per walker, lane g of a walker owns atoms j = g mod 2.
+// shared memory as [coordinate][atom slot][walker of the warp][lane of the walker], atom
+// j = lane + LPW * slot, so that the 32 lanes of a warp reading "their" atom of one slot
+// touch 32 consecutive 8-byte words (two wavefronts of 16 lanes, no bank conflict; with
+// the lanes of a walker 16 walkers apart instead, a wavefront's two halves met the same
+// banks).
 // Global memory keeps the register kernel's [walker][6][np] planes, so the two kernels
 // continue each other's runs.
 #include <cuda_runtime.h>
@@ -39,14 +41,16 @@ template <int LPW, int NP>
 struct LjLaneWalker {
   static constexpr int WPW = 32 / LPW;   // walkers per warp
   static constexpr int APL = NP / LPW;   // atom slots per lane
-  float2* sp;                            // this warp's [3][NP][WPW] (hi, lo)
+  float2* sp;                            // this warp's [3][APL][WPW][LPW] (hi, lo)
   int slot;                              // this lane's walker within the warp
   int glane;
   unsigned gmask;
   int n;
   float wall_r2f;  // binary32 R^2 of the wall, set once per launch
 
-  __device__ float2& at(int c, int j) const { return sp[(c * NP + j) * WPW + slot]; }
+  __device__ float2& at(int c, int j) const {
+    return sp[((c * APL + j / LPW) * WPW + slot) * LPW + j % LPW];
+  }
   __device__ void load(const float* p) {
 #pragma unroll
     for (int k = 0; k < APL; ++k) {

@@ -9,7 +9,13 @@ namespace dev {
 
 __device__ __forceinline__ float rbf_centre(int k) { return 0.8f + (2.2f / 31.0f) * (float)k; }
 
-__device__ __forceinline__ float silu32(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU z / (1 + e^-z) for the batched forward and the training kernels, with the hardware
+// reciprocal (__fdividef, a few ulp; 0 once the denominator passes 2^126, the SiLU's
+// limit for large negative z) in place of an IEEE division: the kernels evaluate a few
+// hundred SiLUs per thread in unrolled code, and the IEEE sequence's length made their
+// instruction fetch the limiter.  The error is far below the BF16 rounding of the
+// activations.
+__device__ __forceinline__ float silu32(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 // SiLU as z/2 (1 + tanh(z/2)) on the hardware tanh (tanh.approx.f32, absolute error about
 // 2^-11): one special-function operation and an FMA in place of an exponential and an
 // IEEE division.  Used by the delayed-acceptance screen only, whose value decides no
@@ -20,8 +26,8 @@ __device__ __forceinline__ float silu_fast(float z) {
   asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
   return __fmaf_rn(h, t, h);
 }
-__device__ __forceinline__ float dsilu32(float z) {
-  const float s = 1.0f / (1.0f + __expf(-z));
+__device__ __forceinline__ float dsilu32(float z) {  // SiLU'(z), reciprocal as in silu32
+  const float s = __fdividef(1.0f, 1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
 }
 
