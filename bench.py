@@ -274,7 +274,7 @@ def case_da(G, seed=11, walkers=8192, moves=100_000, **_):
     return da_compare(G, 0, walkers, moves)
 
 
-def case_north_star(G, seed=31, walkers=512, moves=1_000_000, **_):
+def case_north_star(G, seed=31, walkers=1024, moves=1_000_000, **_):
     """Plain against delayed acceptance at equal heat-capacity error (the benchmark spec), alone."""
     return north_star(G, walkers=walkers, warm=moves, seed=seed)
 
@@ -435,7 +435,7 @@ def lj31_reference_cv(T=CV_T):
     return CVM.interp_reference(T, [(g["curves"][k]["T"], g["curves"][k]["Cv"]) for k in ("RESTMC", "t-REM")])
 
 
-def north_star(G, walkers=512, warm=1_000_000, seconds=20.0, seed=31):
+def north_star(G, walkers=1024, warm=1_000_000, seconds=20.0, seed=31):
     """Plain against delayed-acceptance moves at equal heat-capacity error, on the LJ31
     workload's configuration (R = 2.5, SAD min_T 0.2, bins of 0.134), whose heat capacity
     the reference holds (its Rc = 2.5 curves, RESTMC and t-REM, T = 0.25-0.36).  Both arms
@@ -444,7 +444,10 @@ def north_star(G, walkers=512, warm=1_000_000, seconds=20.0, seed=31):
     segments, and after each segment every walker's Cv is rebuilt on the device from its
     own bins.  The error is that of the walker-median Cv curve against the reference
     (max over T of the relative error).  The comparison is the time each arm needs to
-    reach the error both reach (the larger of the two final errors)."""
+    reach the error both reach (the larger of the two arms' smallest errors), and at a
+    few coarser levels.  1024 walkers: the delayed-acceptance kernel (a warp per walker,
+    8 per SM) still runs them in one wave, and the median over walkers is steadier than
+    at fewer."""
     import tempfile
     import cv as CVM
     ref = lj31_reference_cv()
@@ -481,9 +484,16 @@ def north_star(G, walkers=512, warm=1_000_000, seconds=20.0, seed=31):
     d_rows = arm({"batch": b, "run": lambda k: b.run_online(k, True, collect_interval=100_000,
                                                              retrain_interval=100_000, train_steps=100,
                                                              batch=512, lr=1e-3, seed=10)}, 200_000)
-    eps = max(p_rows[-1]["err"], d_rows[-1]["err"])
-    tp = CVM.time_to_error([r["t"] for r in p_rows], [r["err"] for r in p_rows], eps)
-    td = CVM.time_to_error([r["t"] for r in d_rows], [r["err"] for r in d_rows], eps)
+    # the levels both arms reach: the larger final error (the common level), and coarser
+    # levels up to the larger first error, each crossed by the running minimum
+    eps = max(min(r["err"] for r in p_rows), min(r["err"] for r in d_rows))
+    top = min(max(r["err"] for r in p_rows), max(r["err"] for r in d_rows))
+    levels = [float(x) for x in np.geomspace(eps, max(top, eps), 4)]
+    tt = lambda rows, e: CVM.time_to_error([r["t"] for r in rows], [r["err"] for r in rows], e)
+    tp, td = tt(p_rows, eps), tt(d_rows, eps)
+    by_level = [{"cv_error": e, "plain_s": tt(p_rows, e), "da_s": tt(d_rows, e)} for e in levels]
+    for x in by_level:
+        x["da_speedup"] = (x["plain_s"] / x["da_s"]) if (x["plain_s"] and x["da_s"]) else None
     flagged = {"plain": status_summary(plain), "da": status_summary(b)}
     plain.close()
     b.close()
@@ -502,6 +512,7 @@ def north_star(G, walkers=512, warm=1_000_000, seconds=20.0, seed=31):
            "plain": summary(p_rows), "da": summary(d_rows), "equal_cv_error": eps,
            "plain_seconds_to_equal_error": tp, "da_seconds_to_equal_error": td,
            "da_speedup_at_equal_cv_error": (tp / td) if (tp and td) else None,
+           "by_error_level": by_level,
            "status": flagged}
     out["da_wins"] = bool(out["da_speedup_at_equal_cv_error"] and out["da_speedup_at_equal_cv_error"] > 1.0)
     for k in ("plain", "da"):
