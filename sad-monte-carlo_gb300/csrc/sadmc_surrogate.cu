@@ -33,35 +33,36 @@ namespace dev {
 constexpr uint32_t kPolls = 1u << 24;  // bounded mbarrier waits (never expected to run out)
 
 // Descriptors of rows [0, rows): row r = atom (r % n) of configuration (r / n); positions
-// [configs][n][3] binary32.  Writes bf16 G (the forward operand) and, if requested, FP32 G.
+// [configs][n][3] binary32.  Four threads per row, eight RBF columns each (one 16-byte
+// bf16 store per thread).  Writes bf16 G (the forward operand) and, if requested, FP32 G.
+constexpr int DESC_TPR = 4;
 __global__ void descriptor_kernel(const float* pos, int n, int rows, __nv_bfloat16* gq, float* gf) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = tid / DESC_TPR, part = tid % DESC_TPR;
   if (r >= rows) return;
+  constexpr int K = SG_RBF / DESC_TPR;
   const int c = r / n, i = r % n;
   const float* p = pos + (size_t)c * n * 3;
   const float xi = p[3 * i], yi = p[3 * i + 1], zi = p[3 * i + 2];
-  float g[SG_RBF];
+  float g[K];
 #pragma unroll
-  for (int k = 0; k < SG_RBF; ++k) g[k] = 0.0f;
+  for (int k = 0; k < K; ++k) g[k] = 0.0f;
   const float inv2w2 = 1.0f / (2.0f * 0.1f * 0.1f);
   for (int j = 0; j < n; ++j) {
     if (j == i) continue;
     const float dx = p[3 * j] - xi, dy = p[3 * j + 1] - yi, dz = p[3 * j + 2] - zi;
     const float rij = sqrtf(dx * dx + dy * dy + dz * dz);
 #pragma unroll
-    for (int k = 0; k < SG_RBF; ++k) {
-      const float d = rij - rbf_centre(k);
+    for (int k = 0; k < K; ++k) {
+      const float d = rij - rbf_centre(part * K + k);
       g[k] += __expf(-d * d * inv2w2);
     }
   }
-  uint4* out = reinterpret_cast<uint4*>(gq + (size_t)r * SG_RBF);
-#pragma unroll
-  for (int q = 0; q < SG_RBF / 8; ++q)
-    out[q] = make_uint4(pack_bf16(g[8 * q], g[8 * q + 1]), pack_bf16(g[8 * q + 2], g[8 * q + 3]),
-                        pack_bf16(g[8 * q + 4], g[8 * q + 5]), pack_bf16(g[8 * q + 6], g[8 * q + 7]));
+  *reinterpret_cast<uint4*>(gq + (size_t)r * SG_RBF + part * K) =
+      make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]), pack_bf16(g[4], g[5]), pack_bf16(g[6], g[7]));
   if (gf) {
 #pragma unroll
-    for (int k = 0; k < SG_RBF; ++k) gf[(size_t)r * SG_RBF + k] = g[k];
+    for (int k = 0; k < K; ++k) gf[(size_t)r * SG_RBF + part * K + k] = g[k];
   }
 }
 
@@ -544,8 +545,16 @@ __global__ void reduce_adam_kernel(const float* part, const double* lpart, int t
     *loss = l;
   }
   if (p >= SG_NPARAM) return;
-  float s = 0.f;
-  for (int t = 0; t < tiles; ++t) s += part[(size_t)t * SG_NPARAM + p];
+  // eight independent partial sums (tiles t = k mod 8), combined in a fixed order: the
+  // loads overlap, and the result depends only on the number of tiles
+  float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  int t = 0;
+  for (; t + 8 <= tiles; t += 8) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] += part[(size_t)(t + k) * SG_NPARAM + p];
+  }
+  for (int k = 0; t + k < tiles; ++k) a[k] += part[(size_t)(t + k) * SG_NPARAM + p];
+  const float s = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
   grad[p] = s;
   if (adam.step > 0) {
     const float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
@@ -605,7 +614,8 @@ __global__ void take_flag_kernel(unsigned int* flag, unsigned int* out) { *out =
 
 cudaError_t sg_descriptors(const float* pos, int n, int rows, __nv_bfloat16* gq, float* gf,
                            cudaStream_t st) {
-  dev::descriptor_kernel<<<(rows + 127) / 128, 128, 0, st>>>(pos, n, rows, gq, gf);
+  const long long threads = (long long)rows * dev::DESC_TPR;
+  dev::descriptor_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(pos, n, rows, gq, gf);
   return cudaGetLastError();
 }
 
