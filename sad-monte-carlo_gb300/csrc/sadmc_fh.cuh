@@ -307,7 +307,21 @@ struct Fh {
   }
   __device__ void store(WalkerCore* cores, int w) {
     if (c.kind != M_DESCENT) flush_cur();
-    if (wr && glane == 0) cores[w] = c;
+    if (!(wr && glane == 0)) return;
+    if (FAM == M_SAD) {
+      // the fields a SAD move can change; the other methods' fields keep the values the
+      // launch loaded, so a SAD kernel need not hold them in registers for the whole loop
+      WalkerCore* o = &cores[w];
+      o->E = c.E; o->acc_rate = c.acc_rate; o->tscale = c.tscale; o->cur_min = c.cur_min;
+      o->too_lo = c.too_lo; o->too_hi = c.too_hi; o->latest_param = c.latest_param;
+      o->max_S = c.max_S; o->drift = c.drift; o->win_tmax = c.win_tmax; o->moves = c.moves;
+      o->accepted = c.accepted; o->tL = c.tL; o->tF = c.tF; o->num_states = c.num_states;
+      o->highest_hist = c.highest_hist; o->b_lo = c.b_lo; o->b_hi = c.b_hi;
+      o->max_S_local = c.max_S_local; o->fill_val = c.fill_val; o->status = c.status;
+      o->fill_gen = c.fill_gen; o->pad1 = c.pad1; o->pad2 = c.pad2;
+    } else {
+      cores[w] = c;
+    }
   }
 
   // ---- gamma (energy.rs:799-825; SadVersion::compute_gamma energy.rs:22-38) -----------
