@@ -142,8 +142,13 @@ __device__ __forceinline__ double sad_gamma_value(double p, uint64_t tF, uint64_
 // in each walker's state (WL and 1/t-WL, whose walkers switch to SAMC at run time).
 constexpr int FAM_ANY = -1;
 
-template <int LPW, int FAM = FAM_ANY>
+// SPLIT: the bookkeeping that no decision reads -- the acceptance rate and translation
+// scale, the energy sums, and the max-entropy / round-trip stamps -- is left to another
+// warp, which replays it from a per-move record (out_li, out_i1l, tsc_event and the
+// state after the move); this object then holds neither those fields nor their planes.
+template <int LPW, int FAM = FAM_ANY, bool SPLIT = false>
 struct Fh {
+  static_assert(!SPLIT || (LPW == 1 && FAM == M_SAD), "the split bookkeeping is SAD on one lane");
   WalkerCore c;
   // launch constants
   double width, inv_width, min_allowed, max_allowed, target_rate;
@@ -190,7 +195,13 @@ struct Fh {
   const double* xg;
   uint64_t xg_t0;
   bool xg_ok;
-  __device__ void invalidate_gamma() { gb_ok = 0; xg_ok = false; }
+  uint32_t pgen;  // count of parameter changes (tables computed ahead carry the count they saw)
+  // SPLIT: the last move's local bin index, the local index of the bin it started from
+  // (energy.rs:950-965), and whether tF changed with the acceptance-rate mode on
+  // (energy.rs:600-609)
+  int out_li, out_i1l;
+  bool tsc_event;
+  __device__ void invalidate_gamma() { gb_ok = 0; xg_ok = false; ++pgen; }
   bool inverted;        // too_lo > too_hi (never true for SAD; kept exact)
 
   // ---- index helpers ---------------------------------------------------------------
@@ -219,18 +230,23 @@ struct Fh {
     else if (wr) lnw[g] = v;
   }
   __device__ void flush_cur() {
-    if (wr) { lnw[cur] = k_lnw; hist[cur] = k_hist; tf[cur] = k_tf; sE[cur] = k_sE; sE2[cur] = k_sE2; }
+    if (wr) {
+      lnw[cur] = k_lnw; hist[cur] = k_hist; tf[cur] = k_tf;
+      if (!SPLIT) { sE[cur] = k_sE; sE2[cur] = k_sE2; }
+    }
   }
   __device__ void load_cur(int g) {
     g = g < 0 ? 0 : (g >= nbins ? nbins - 1 : g);
     cur = g;
-    k_lnw = lnw[g]; k_hist = hist[g]; k_tf = tf[g]; k_sE = sE[g]; k_sE2 = sE2[g]; k_stamp = stamp[g];
+    k_lnw = lnw[g]; k_hist = hist[g]; k_tf = tf[g];
+    if (!SPLIT) { k_sE = sE[g]; k_sE2 = sE2[g]; k_stamp = stamp[g]; }
   }
   __device__ void fetch_pending(int g) {
     if (g == cur) {
       p_lnw = k_lnw; p_hist = k_hist; p_tf = k_tf; p_sE = k_sE; p_sE2 = k_sE2; p_stamp = k_stamp;
     } else {
-      p_lnw = lnw[g]; p_hist = hist[g]; p_tf = tf[g]; p_sE = sE[g]; p_sE2 = sE2[g]; p_stamp = stamp[g];
+      p_lnw = lnw[g]; p_hist = hist[g]; p_tf = tf[g];
+      if (!SPLIT) { p_sE = sE[g]; p_sE2 = sE2[g]; p_stamp = stamp[g]; }
     }
   }
   // adopt the prefetched fields of bin g (== i2) as the current bin
@@ -238,7 +254,8 @@ struct Fh {
     if (g == cur) return;
     flush_cur();
     cur = g;
-    k_lnw = p_lnw; k_hist = p_hist; k_tf = p_tf; k_sE = p_sE; k_sE2 = p_sE2; k_stamp = p_stamp;
+    k_lnw = p_lnw; k_hist = p_hist; k_tf = p_tf;
+    if (!SPLIT) { k_sE = p_sE; k_sE2 = p_sE2; k_stamp = p_stamp; }
   }
   __device__ void move_cur(int g) {
     if (g != cur) { flush_cur(); load_cur(g); }
@@ -304,6 +321,7 @@ struct Fh {
     xg = nullptr;
     xg_t0 = 0;
     xg_ok = false;
+    pgen = 0;
   }
   __device__ void store(WalkerCore* cores, int w) {
     if (c.kind != M_DESCENT) flush_cur();
@@ -311,14 +329,18 @@ struct Fh {
     if (FAM == M_SAD) {
       // the fields a SAD move can change; the other methods' fields keep the values the
       // launch loaded, so a SAD kernel need not hold them in registers for the whole loop
+      // (SPLIT: nor those of the other warp's bookkeeping, which stores them itself)
       WalkerCore* o = &cores[w];
-      o->E = c.E; o->acc_rate = c.acc_rate; o->tscale = c.tscale; o->cur_min = c.cur_min;
+      o->E = c.E; o->cur_min = c.cur_min;
       o->too_lo = c.too_lo; o->too_hi = c.too_hi; o->latest_param = c.latest_param;
-      o->max_S = c.max_S; o->drift = c.drift; o->win_tmax = c.win_tmax; o->moves = c.moves;
+      o->drift = c.drift; o->win_tmax = c.win_tmax; o->moves = c.moves;
       o->accepted = c.accepted; o->tL = c.tL; o->tF = c.tF; o->num_states = c.num_states;
       o->highest_hist = c.highest_hist; o->b_lo = c.b_lo; o->b_hi = c.b_hi;
-      o->max_S_local = c.max_S_local; o->fill_val = c.fill_val; o->status = c.status;
-      o->fill_gen = c.fill_gen; o->pad1 = c.pad1; o->pad2 = c.pad2;
+      o->status = c.status; o->pad1 = c.pad1; o->pad2 = c.pad2;
+      if (!SPLIT) {
+        o->acc_rate = c.acc_rate; o->tscale = c.tscale; o->max_S = c.max_S;
+        o->max_S_local = c.max_S_local; o->fill_val = c.fill_val; o->fill_gen = c.fill_gen;
+      }
     } else {
       cores[w] = c;
     }
@@ -408,8 +430,10 @@ struct Fh {
     while (e < c.cur_min) {
       if (c.b_lo == 0) return false;
       c.b_lo -= 1;
-      if (wr) stamp[c.b_lo] = c.fill_gen;  // inserted as visited, round_trips already 1
-      if (c.b_lo == cur) k_stamp = c.fill_gen;
+      if (!SPLIT) {
+        if (wr) stamp[c.b_lo] = c.fill_gen;  // inserted as visited, round_trips already 1
+        if (c.b_lo == cur) k_stamp = c.fill_gen;
+      }
       c.cur_min -= width;
       grew_front = true;
     }
@@ -417,8 +441,10 @@ struct Fh {
     while (e >= cur_max) {
       if (c.b_hi >= nbins - 1) return false;
       c.b_hi += 1;
-      if (wr) stamp[c.b_hi] = c.fill_gen;
-      if (c.b_hi == cur) k_stamp = c.fill_gen;
+      if (!SPLIT) {
+        if (wr) stamp[c.b_hi] = c.fill_gen;
+        if (c.b_hi == cur) k_stamp = c.fill_gen;
+      }
       cur_max = c.cur_min + width * (double)(c.b_hi - c.b_lo + 1);
     }
     cminf = f32_trunc(c.cur_min);
@@ -474,7 +500,7 @@ struct Fh {
   // ---- one move ----------------------------------------------------------------------
   __device__ void begin_move(double one_minus_rs) {
     c.moves += 1;                  // energy.rs:905
-    c.acc_rate *= one_minus_rs;    // energy.rs:913-914
+    if (!SPLIT) c.acc_rate *= one_minus_rs;    // energy.rs:913-914
     e1 = c.E;
     grew_front = false;
   }
@@ -496,7 +522,7 @@ struct Fh {
     bool have = false;
     const bool accepted = uni(!rejects(possible, de, u53, has_first, lnw_first, e2, have));
     if (accepted) {
-      if (c.kind != M_DESCENT) { c.accepted += 1; c.acc_rate += rs; }
+      if (c.kind != M_DESCENT) { c.accepted += 1; if (!SPLIT) c.acc_rate += rs; }
       set_E(have ? e2 : c.E + f2d(de));
     }
     return accepted;
@@ -607,10 +633,18 @@ struct Fh {
       if (kind() == M_SAD && cur >= win_lo && cur <= win_hi && c.moves > c.win_tmax) c.win_tmax = c.moves;
     }
     k_hist += 1;
-    k_sE += E;
-    k_sE2 += E2;  // E2 == E * E (set_E)
+    if (!SPLIT) {
+      k_sE += E;
+      k_sE2 += E2;  // E2 == E * E (set_E)
+    }
+    tsc_event = false;
     update_weights(E);
     const int li = cur - c.b_lo;
+    if (SPLIT) {
+      out_li = li;
+      out_i1l = (grew_front ? gidx_exact(e1) : old_cur) - c.b_lo;
+      return;
+    }
     if (dgt(k_lnw, c.max_S)) {
       c.max_S = k_lnw;
       c.max_S_local = li;
@@ -695,7 +729,9 @@ struct Fh {
       uint64_t old_tF = c.tF;
       c.tF = c.win_tmax;
       invalidate_gamma();
-      if (old_tF != c.tF && acc_mode) {  // energy.rs:600-609
+      if (SPLIT) {
+        tsc_event = old_tF != c.tF && acc_mode;
+      } else if (old_tF != c.tF && acc_mode) {  // energy.rs:600-609
         double s = c.acc_rate / target_rate;
         s = s < 0.8 ? 0.8 : (s > 1.2 ? 1.2 : s);
         c.tscale *= s;

@@ -1,15 +1,18 @@
-// One Ising walker as a serial chain on one lane (src/system/ising.rs with the bookkeeping
-// of src/mc/energy.rs), the shape of a single-walker run.
+// One Ising walker as a serial chain (src/system/ising.rs with the bookkeeping of
+// src/mc/energy.rs), the shape of a single-walker run.
 //
 // A lone walker's Markov chain is sequential: each move's decision reads the weights the
-// previous move updated.  Lane 0 runs that chain with the walker's bin planes and spins
-// in shared memory.  What does not depend on the chain is computed ahead by the whole
-// warp, 32 moves at a time, into shared-memory tables: the Philox draws of each move
-// (site and uniform), the acceptance-rate factor sqrt(1/t), and the SAD (or SAMC) gamma
-// for the walker's parameters at the start of the batch.  A parameter change inside a
-// batch (a SAD discovery, a window edge, a new tF) invalidates the gamma table, and lane 0
-// computes the remaining moves' gamma itself, so every value is the one the reference's
-// arithmetic gives.
+// previous move updated.  Two kernels run it with the walker's bin planes and spins in
+// shared memory:
+//  * ising_chain_kernel (Wang-Landau, 1/t-WL, SAMC, canonical): lane 0 runs the chain;
+//    what does not depend on it is computed ahead by the whole warp, 32 moves at a time,
+//    into shared-memory tables: the Philox draws of each move, the acceptance-rate factor
+//    sqrt(1/t) and the SAMC gamma;
+//  * ising_sad_pipe_kernel (SAD): three warps, one deciding, one filling the next
+//    batch's tables, one replaying the bookkeeping no decision reads (below).
+// A parameter change inside a batch (a SAD discovery, a window edge, a new tF)
+// invalidates the gamma table, and the deciding lane computes gamma itself until the next
+// valid table, so every value is the one the reference's arithmetic gives.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -121,6 +124,400 @@ __global__ void __launch_bounds__(32, 1) ising_chain_kernel(MoveLaunch m, IsingS
   for (int k = lane; k < L * L; k += 32) gS[k] = S[k];
 }
 
+// ---- SAD: the chain pipelined over three warps, with an integer fast path ---------------
+//
+// Warp 0's lane 0 runs the decisions and the state they read: the energy, the bins' ln w,
+// histogram and t_found, the SAD window and parameters.  It records each move (bin, local
+// indices, acceptance, energy, ln w after the update) in a log.  Warp 2's lane 0 replays
+// the log of the previous batch for the bookkeeping no decision reads: the acceptance
+// rate and translation scale (energy.rs:600-621, 913-914), the energy sums (energy.rs:
+// 941-942) and the max-entropy / round-trip stamps (energy.rs:950-965).  Warp 1 fills the
+// tables of the next batch of 32 moves: draws, the site and its four neighbours,
+// sqrt(1/t), and gamma for the SAD parameters at the start of the current batch (a table
+// whose parameters changed since is not used).  A batch boundary is one block barrier;
+// the three warps' dependent chains overlap instead of adding up.
+//
+// Ising energies, bin edges and (for power-of-two bin widths) the SAD window edges are
+// integers or half-integers, so the comparisons the reference makes on e2 = E + dE
+// (bounds, bin range, state_to_index, window) are integer comparisons against thresholds
+// derived exactly once per change (x < T <=> x < ceil(T) for an integer x).  The common
+// move -- its proposed bin already visited, no window or bin growth possible, gamma from
+// the table -- runs on those integers and the FP64 ln w; every other move (a possible
+// discovery, growth of the window or of the bins, a parameter change, a trace) takes the
+// generic bookkeeping.  The spins a move reads are loaded one move ahead, before the
+// previous flip, and reloaded when that flip touched them.
+struct PipeTables {
+  uint16_t site[32];
+  uint16_t nb[32][4];
+  uint32_t conflict;  // bit k: move k's site is move k+1's site or one of its neighbours
+  uint32_t gen;       // Fh::pgen the gamma values were computed for
+  uint64_t u53[32];
+  float lnu_lo[32], lnu_hi[32];  // bounds of ln u for the Metropolis uniform u
+  double rs[32], omrs[32];  // sqrt(1/t) and 1 - sqrt(1/t) (energy.rs:913)
+  double gamma[32];
+};
+struct PipeSnap {  // the walker's SAD parameters at a batch boundary
+  double p;
+  uint64_t tF, ns;
+  uint32_t gen;
+};
+struct PipeLog {  // one move, as the bookkeeping warp needs it
+  double lnw;          // ln w of the bin after the update
+  int32_t E;           // energy after the move (Ising energies are integers)
+  int16_t cur;         // bin after the move (plane index; the planes hold < 2^15 bins)
+  int16_t li, i1l;     // local indices of the bin after and before the move
+  int16_t b_lo, b_hi;  // allocated bins after the move (prepare_for_state)
+  uint16_t flags;      // bit 0: accepted; bit 1: tF changed with the acceptance-rate mode on
+};
+struct PipeBook {  // the bookkeeping warp's fields, handed back at the end of a launch
+  double acc_rate, tscale, max_S;
+  int32_t max_S_local, fill_val;
+  uint64_t fill_gen;
+};
+
+__host__ __device__ inline size_t ising_pipe_bytes(int nbins, int L) {
+  return (size_t)nbins * 64 + (((size_t)L * (size_t)L + 15) & ~(size_t)15) + 3 * sizeof(PipeTables) +
+         2 * 32 * sizeof(PipeLog) + 2 * sizeof(PipeSnap) + sizeof(uint64_t);
+}
+
+// rejected = lnw2 > lnw1 && u > exp(lnw1 - lnw2) (energy.rs:461-465).  The binary32
+// truncations a, b of the weights order them unless equal (truncation is monotone); the
+// test u > exp(d) <=> ln u > d is then taken against bounds [lo, hi] of ln u and the error
+// bound of a - b, and in FP64 where those cannot tell.
+__device__ __forceinline__ bool sad_reject(double lnw1, double lnw2, uint64_t u53, float lo, float hi) {
+  const float a = f32_trunc(lnw1), b = f32_trunc(lnw2);
+  if (b < a) return false;
+  if (b == a && !dgt(lnw2, lnw1)) return false;
+  const float df = a - b;
+  // |df - (lnw1 - lnw2)| <= (|a| + |b|) 2^-23 + |df| 2^-24; 1e-12 covers exp's FP64 rounding
+  const float dd = (fabsf(a) + fabsf(b)) * 1.2e-7f + fabsf(df) * 6.0e-8f + 1e-12f;
+  if (lo > df + dd) return true;
+  if (hi < df - dd) return false;
+  return u53_to_double(u53) > exp(lnw1 - lnw2);
+}
+
+using FhSplit = Fh<1, M_SAD, true>;
+
+// Integer view of a SAD walker: energy, bin range, window and bounds (see above).
+struct LeanSad {
+  bool ok;
+  int ws;            // log2 of the bin width, or -1 when it is not a power of two
+  int Ei, cmin, cmax, tlo, thi, mx, mn;
+  int cls;           // -1 / 0 / +1: E below / inside / above the window [too_lo, too_hi]
+  double lnw1c;      // ln w at E when cls != 0 (energy.rs:451-464)
+};
+
+__device__ __forceinline__ int clamp_floor(double x) {
+  const double c = 1073741824.0;  // 2^30
+  return x >= c ? (int)c : (x <= -c ? -(int)c : (int)floor(x));
+}
+__device__ __forceinline__ int clamp_ceil(double x) {
+  const double c = 1073741824.0;
+  return x >= c ? (int)c : (x <= -c ? -(int)c : (int)ceil(x));
+}
+
+// Re-derive the integer view from the walker state after a generic move or at a batch
+// start; z.ok = false keeps the walker on the generic bookkeeping.
+__device__ void lean_sync(const FhSplit& fh, LeanSad& z, bool traced) {
+  z.ok = false;
+  if (z.ws < 0 || traced || !fh.xg_ok || fh.inverted || fh.k_hist == 0 || fh.c.kind != M_SAD) return;
+  const double E = fh.c.E, cm = fh.c.cur_min, lim = 536870912.0;  // 2^29
+  if (!(E == floor(E) && fabs(E) < lim && cm == floor(cm) && fabs(cm) < lim)) return;
+  const double span = (double)(fh.c.b_hi - fh.c.b_lo + 1) * fh.width;
+  if (!(fabs(cm + span) < lim)) return;
+  if (is_nan64(fh.c.too_lo) || is_nan64(fh.c.too_hi) || is_nan64(fh.max_allowed) || is_nan64(fh.min_allowed))
+    return;
+  z.Ei = (int)E;
+  z.cmin = (int)cm;
+  z.cmax = (int)(cm + span);  // cur_max, exact
+  z.tlo = clamp_ceil(fh.c.too_lo);   // e < too_lo  <=> e < tlo
+  z.thi = clamp_floor(fh.c.too_hi);  // e > too_hi  <=> e > thi
+  z.mx = fh.has_max_allowed ? clamp_floor(fh.max_allowed) : (1 << 30);
+  z.mn = fh.has_min_allowed ? clamp_ceil(fh.min_allowed) : -(1 << 30);
+  z.cls = z.Ei < z.tlo ? -1 : (z.Ei > z.thi ? 1 : 0);
+  z.lnw1c = z.cls != 0 ? fh.sad_lnw(E, fh.cur) : 0.0;
+  z.ok = true;
+}
+
+// One common move on the integer view: bounds, reject_move and the decision-side
+// bookkeeping of move_once (energy.rs:904-974) for a move whose proposed bin was visited
+// before and which can neither grow the window nor the bins.  Returns 0 (rejected) or 1
+// (accepted) with fh.out_li / out_i1l set, or 2 without changing anything when the move
+// needs the generic path.
+__device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, uint64_t u53, float lo, float hi,
+                                         double g) {
+  const int e2 = z.Ei + de;
+  const bool oob = (e2 > z.mx && de > 0) || (e2 < z.mn && de < 0);
+  int i2 = fh.cur, cls2 = z.cls;
+  double p_lnw = fh.k_lnw;
+  uint64_t p_hist = fh.k_hist;
+  if (!oob) {
+    if (e2 < z.cmin || e2 >= z.cmax) return 2;  // prepare_for_state would grow the bins
+    i2 = fh.c.b_lo + ((e2 - z.cmin) >> z.ws);
+    if (i2 != fh.cur) { p_lnw = fh.lnw[i2]; p_hist = fh.hist[i2]; }
+    cls2 = e2 < z.tlo ? -1 : (e2 > z.thi ? 1 : 0);
+    // a first visit (energy.rs:466-483, 938-940) or a window edge (energy.rs:530-580)
+    if (p_hist == 0 || (cls2 != 0 && p_hist >= fh.c.highest_hist)) return 2;
+  }
+  if (z.cls != 0 && fh.k_hist >= fh.c.highest_hist) return 2;
+  fh.c.moves += 1;
+  bool rejected = oob;
+  double lnw2 = 0.0;
+  if (!oob) {
+    const double lnw1 = z.cls == 0 ? fh.k_lnw : z.lnw1c;
+    lnw2 = cls2 == 0 ? p_lnw
+                     : (cls2 > 0 ? fh.ld_lnw(fh.win_hi)
+                                 : fh.ld_lnw(fh.win_lo) + div_by((double)e2 - fh.c.too_lo, fh.c.min_T, fh.inv_minT));
+    rejected = sad_reject(lnw1, lnw2, u53, lo, hi);
+  }
+  const int old_cur = fh.cur;
+  if (!rejected) {
+    fh.c.accepted += 1;
+    z.Ei = e2;
+    fh.c.E = (double)e2;
+    if (i2 != fh.cur) {  // the cached bin moves: write back, take the new one's fields
+      fh.lnw[fh.cur] = fh.k_lnw;
+      fh.hist[fh.cur] = fh.k_hist;
+      fh.tf[fh.cur] = fh.k_tf;
+      fh.cur = i2;
+      fh.k_lnw = p_lnw;
+      fh.k_hist = p_hist;
+      fh.k_tf = fh.tf[i2];
+    }
+    z.cls = cls2;
+    z.lnw1c = lnw2;  // ln w at the new E when it lies outside the window
+  }
+  fh.k_hist += 1;
+  if (SADMC_RARE(is_nan64(g))) fh.c.status |= ST_NAN_GAMMA;
+  if (z.cls == 0) {  // SAD updates ln w inside the window only (energy.rs:523-529)
+    fh.k_lnw += g;
+    if (fh.k_hist > fh.c.highest_hist) fh.c.highest_hist = fh.k_hist;
+  }
+  fh.out_li = fh.cur - fh.c.b_lo;
+  fh.out_i1l = old_cur - fh.c.b_lo;
+  fh.tsc_event = false;
+  return rejected ? 0 : 1;
+}
+
+// The bookkeeping warp's replay of one logged move (energy.rs:913-914, 600-609, 941-942,
+// 950-965), in the order move_once applies it.
+struct Book {
+  PipeBook s;
+  double target_rate;
+  int kb_lo, kb_hi;  // allocated bins as last seen
+  int kcur;          // bin whose sums are held in ksE, ksE2
+  double ksE, ksE2;
+  double *sE, *sE2;
+  uint64_t *stamp, *rt;
+  __device__ void replay(const PipeLog& e, double rs, double omrs) {
+    s.acc_rate *= omrs;
+    if (e.flags & 1) s.acc_rate += rs;
+    while (kb_lo > e.b_lo) stamp[--kb_lo] = s.fill_gen;  // inserted as visited
+    while (kb_hi < e.b_hi) stamp[++kb_hi] = s.fill_gen;
+    if (SADMC_RARE(e.flags & 2)) {
+      double f = s.acc_rate / target_rate;
+      f = f < 0.8 ? 0.8 : (f > 1.2 ? 1.2 : f);
+      s.tscale *= f;
+    }
+    if (e.cur != kcur) {
+      if (kcur >= 0) { sE[kcur] = ksE; sE2[kcur] = ksE2; }
+      kcur = e.cur;
+      ksE = sE[kcur];
+      ksE2 = sE2[kcur];
+    }
+    const double E = (double)e.E;
+    ksE += E;
+    ksE2 += E * E;
+    if (dgt(e.lnw, s.max_S)) {
+      s.max_S = e.lnw;
+      s.max_S_local = e.li;
+      s.fill_gen += 1;
+      s.fill_val = 1;
+    } else if (e.li == s.max_S_local) {
+      if (e.i1l != e.li) { s.fill_gen += 1; s.fill_val = 0; }
+    } else if (!(stamp[e.cur] == s.fill_gen || s.fill_val != 0)) {
+      stamp[e.cur] = s.fill_gen;
+      rt[e.cur] = rt[e.cur] + 1;
+    }
+  }
+};
+
+__global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, IsingSys s) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int w = blockIdx.x;  // one walker per block of three warps
+  const int L = s.L;
+  const int nb = m.P.nbins;
+  int8_t* gS = s.spins + (size_t)w * (size_t)L * (size_t)L;
+  const size_t off = (size_t)w * (size_t)nb;
+  double* gp[3] = {m.B.lnw + off, m.B.sumE + off, m.B.sumE2 + off};
+  uint64_t* gq[5] = {m.B.hist + off, m.B.t_found + off, m.B.round_trips + off, m.B.wl_hist + off,
+                     m.B.visit_stamp + off};
+  double* sd = reinterpret_cast<double*>(stage);
+  uint64_t* sq = reinterpret_cast<uint64_t*>(sd + 3 * (size_t)nb);
+  int8_t* S = reinterpret_cast<int8_t*>(sq + 5 * (size_t)nb);
+  PipeTables* tbs = reinterpret_cast<PipeTables*>(S + (((size_t)L * (size_t)L + 15) & ~(size_t)15));
+  PipeLog* logs = reinterpret_cast<PipeLog*>(tbs + 3);
+  PipeSnap* snap = reinterpret_cast<PipeSnap*>(logs + 64);
+  uint64_t* t_launch = reinterpret_cast<uint64_t*>(snap + 2);
+  for (int a = 0; a < 3; ++a)
+    for (int k = tid; k < nb; k += 96) sd[(size_t)a * nb + k] = gp[a][k];
+  for (int a = 0; a < 5; ++a)
+    for (int k = tid; k < nb; k += 96) sq[(size_t)a * nb + k] = gq[a][k];
+  for (int k = tid; k < L * L; k += 96) S[k] = gS[k];
+  __syncthreads();
+
+  FhSplit fh;
+  LeanSad z;
+  Book bk;
+  if (tid == 0) {
+    fh.load(m.cores, m.P, m.B, w, 1u, 0, true);
+    fh.lnw = sd; fh.sE = sd + nb; fh.sE2 = sd + 2 * (size_t)nb;
+    fh.hist = sq; fh.tf = sq + nb; fh.rt = sq + 2 * (size_t)nb; fh.wlh = sq + 3 * (size_t)nb;
+    fh.stamp = sq + 4 * (size_t)nb;
+    fh.cur = -1;  // the cached bin is re-read from the staged planes
+    fh.load_cur(fh.gidx_exact(fh.c.E));
+    z.ws = -1;
+    for (int k = 0; k <= 20; ++k)
+      if (fh.width == (double)(1 << k)) z.ws = k;
+    snap[0] = PipeSnap{fh.c.latest_param, fh.c.tF, fh.c.num_states, fh.pgen};
+    *t_launch = fh.c.moves;
+  } else if (tid == 64) {
+    const WalkerCore& c = m.cores[w];
+    bk.s = PipeBook{c.acc_rate, c.tscale, c.max_S, c.max_S_local, c.fill_val, c.fill_gen};
+    bk.target_rate = m.P.target_rate;
+    bk.kb_lo = c.b_lo;
+    bk.kb_hi = c.b_hi;
+    bk.kcur = -1;
+    bk.ksE = bk.ksE2 = 0.0;
+    bk.sE = sd + nb; bk.sE2 = sd + 2 * (size_t)nb;
+    bk.stamp = sq + 4 * (size_t)nb; bk.rt = sq + 2 * (size_t)nb;
+  }
+  __syncthreads();
+  const uint64_t t0 = *t_launch;
+  const uint64_t n = m.n_moves;
+  const uint64_t nbatch = (n + 31) / 32;
+  // warp 1: the tables of batch c from the parameters in snap[q]
+  auto fill = [&](uint64_t c, int q) {
+    PipeTables* T = &tbs[c % 3];
+    const PipeSnap P = snap[q];
+    const uint64_t t = t0 + 32 * c + 1 + (uint64_t)lane;
+    const Draws d = draws_ising(m.seed, (uint32_t)w, t, (uint32_t)L);
+    const int i = (int)d.which, j = (int)d.j;
+    const int jp = j + 1 == L ? 0 : j + 1, jm = j == 0 ? L - 1 : j - 1;
+    const int ip = i + 1 == L ? 0 : i + 1, im = i == 0 ? L - 1 : i - 1;
+    const int site = i + j * L;
+    const int n0 = i + jp * L, n1 = i + jm * L, n2 = ip + j * L, n3 = im + j * L;
+    T->site[lane] = (uint16_t)site;
+    T->nb[lane][0] = (uint16_t)n0; T->nb[lane][1] = (uint16_t)n1;
+    T->nb[lane][2] = (uint16_t)n2; T->nb[lane][3] = (uint16_t)n3;
+    T->u53[lane] = d.u53;
+    {  // u lies in [top, top + 1) 2^-24; logf is within 1 ulp, widened by 2^-20
+      const uint32_t top = (uint32_t)(d.u53 >> 29);
+      const float uf = (float)top * (1.0f / 16777216.0f), uh = (float)(top + 1u) * (1.0f / 16777216.0f);
+      T->lnu_lo[lane] = top == 0u ? -INFINITY : logf(uf) * (1.0f + 9.6e-7f);
+      T->lnu_hi[lane] = logf(uh) * (1.0f - 9.6e-7f);
+    }
+    const double v = sqrt(1.0 / (double)t);  // RecentScale's expression
+    T->rs[lane] = v;
+    T->omrs[lane] = 1. - v;
+    T->gamma[lane] = sad_gamma_value(P.p, P.tF, P.ns, t);
+    const int prev = __shfl_up_sync(0xffffffffu, site, 1);
+    const bool hit = lane > 0 && (prev == site || prev == n0 || prev == n1 || prev == n2 || prev == n3);
+    const unsigned bal = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) { T->conflict = bal >> 1; T->gen = P.gen; }
+  };
+  if (warp == 1 && nbatch > 0) fill(0, 0);
+  __syncthreads();
+  const bool traced = m.trace != nullptr;
+  for (uint64_t b = 0; b <= nbatch; ++b) {
+    if (warp == 1) {
+      if (b + 1 < nbatch) fill(b + 1, (int)(b & 1));
+    } else if (warp == 2) {
+      if (lane == 0 && b > 0) {  // replay the previous batch
+        const PipeTables* T = &tbs[(b - 1) % 3];
+        const PipeLog* lg = &logs[((b - 1) & 1) * 32];
+        const int cnt = (int)(n - 32 * (b - 1) < 32 ? n - 32 * (b - 1) : 32);
+        for (int k = 0; k < cnt; ++k) bk.replay(lg[k], T->rs[k], T->omrs[k]);
+      }
+    } else if (lane == 0 && b < nbatch) {
+      const PipeTables* T = &tbs[b % 3];
+      PipeLog* lg = &logs[(b & 1) * 32];
+      const int cnt = (int)(n - 32 * b < 32 ? n - 32 * b : 32);
+      fh.xg = T->gamma;
+      fh.xg_t0 = fh.c.moves + 1;
+      fh.xg_ok = T->gen == fh.pgen;
+      lean_sync(fh, z, traced);
+      int sc = S[T->site[0]];
+      int ntc = S[T->nb[0][0]] + S[T->nb[0][1]] + S[T->nb[0][2]] + S[T->nb[0][3]];
+      double pend_lnw = 0.0;  // the previous move's ln w, logged one move late
+      for (int k = 0; k < cnt; ++k) {
+        const int site = T->site[k];
+        int sn = 0, ntn = 0;
+        if (k + 1 < cnt) {  // the next move's spins, read before this move's flip
+          sn = S[T->site[k + 1]];
+          ntn = S[T->nb[k + 1][0]] + S[T->nb[k + 1][1]] + S[T->nb[k + 1][2]] + S[T->nb[k + 1][3]];
+        }
+        const int de = -(ntc * sc * 2);  // exact: |de| <= 8
+        int r = z.ok ? lean_move(fh, z, de, T->u53[k], T->lnu_lo[k], T->lnu_hi[k], T->gamma[k]) : 2;
+        if (SADMC_RARE(r == 2)) {  // the generic bookkeeping
+          const uint64_t t = fh.c.moves + 1;
+          fh.Ef = f32_trunc(fh.c.E);
+          fh.begin_move(T->omrs[k]);
+          if (SADMC_RARE(traced && t > m.trace_t0 && t - m.trace_t0 <= m.trace_cap)) {
+            TraceRec rec;
+            rec.e1 = fh.c.E;
+            rec.e2 = fh.c.E + (double)de;
+            m.trace[(size_t)w * m.trace_cap + (t - m.trace_t0 - 1)] = rec;
+          }
+          r = fh.decide_de(true, (float)de, T->u53[k], T->rs[k]) ? 1 : 0;
+          fh.finish_move(r == 1);
+          lean_sync(fh, z, traced);
+        }
+        if (k > 0) lg[k - 1].lnw = pend_lnw;
+        pend_lnw = fh.k_lnw;
+        PipeLog& e = lg[k];
+        e.E = z.ok ? z.Ei : (int)fh.c.E;
+        e.cur = (int16_t)fh.cur;
+        e.li = (int16_t)fh.out_li;
+        e.i1l = (int16_t)fh.out_i1l;
+        e.b_lo = (int16_t)fh.c.b_lo;
+        e.b_hi = (int16_t)fh.c.b_hi;
+        e.flags = (uint16_t)(r | (fh.tsc_event ? 2 : 0));
+        if (r == 1) {
+          S[site] = (int8_t)(-sc);
+          if ((T->conflict >> k) & 1u) {  // the flip touched the next move's spins
+            if (k + 1 < cnt) {
+              sn = S[T->site[k + 1]];
+              ntn = S[T->nb[k + 1][0]] + S[T->nb[k + 1][1]] + S[T->nb[k + 1][2]] + S[T->nb[k + 1][3]];
+            }
+          }
+        }
+        sc = sn;
+        ntc = ntn;
+      }
+      if (cnt > 0) lg[cnt - 1].lnw = pend_lnw;
+      snap[(b + 1) & 1] = PipeSnap{fh.c.latest_param, fh.c.tF, fh.c.num_states, fh.pgen};
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    fh.store(m.cores, w);
+  } else if (tid == 64) {
+    if (bk.kcur >= 0) { bk.sE[bk.kcur] = bk.ksE; bk.sE2[bk.kcur] = bk.ksE2; }
+    WalkerCore* o = &m.cores[w];
+    o->acc_rate = bk.s.acc_rate; o->tscale = bk.s.tscale; o->max_S = bk.s.max_S;
+    o->max_S_local = bk.s.max_S_local; o->fill_val = bk.s.fill_val; o->fill_gen = bk.s.fill_gen;
+  }
+  __syncthreads();
+  for (int a = 0; a < 3; ++a)
+    for (int k = tid; k < nb; k += 96) gp[a][k] = sd[(size_t)a * nb + k];
+  for (int a = 0; a < 5; ++a)
+    for (int k = tid; k < nb; k += 96) gq[a][k] = sq[(size_t)a * nb + k];
+  for (int k = tid; k < L * L; k += 96) gS[k] = S[k];
+}
+
+
 template <int FAM>
 cudaError_t launch_chain(const MoveLaunch& m, const IsingSys& s, size_t bytes, size_t max_bytes,
                          cudaStream_t st) {
@@ -139,13 +536,33 @@ cudaError_t launch_chain(const MoveLaunch& m, const IsingSys& s, size_t bytes, s
 
 }  // namespace dev
 
-size_t ising_chain_bytes(int nbins, int L) { return dev::ising_chain_bytes(nbins, L); }
+// the larger of the two chain kernels' needs
+size_t ising_chain_bytes(int nbins, int L) {
+  const size_t a = dev::ising_chain_bytes(nbins, L), b = dev::ising_pipe_bytes(nbins, L);
+  return a > b ? a : b;
+}
 
 cudaError_t launch_ising_chain(const MoveLaunch& m, const IsingSys& s, size_t max_bytes, cudaStream_t st) {
+  if (m.descent) return cudaErrorInvalidConfiguration;
+  if (m.method == M_SAD) {
+    const size_t bytes = dev::ising_pipe_bytes(m.P.nbins, s.L);
+    if (bytes > max_bytes) return cudaErrorInvalidConfiguration;
+    static std::atomic<bool> attr[64] = {};  // the limit is raised once per device
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return e;
+    if (device < 0 || device >= 64 || !attr[device].load(std::memory_order_acquire)) {
+      e = cudaFuncSetAttribute(dev::ising_sad_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)max_bytes);
+      if (e != cudaSuccess) return e;
+      if (device >= 0 && device < 64) attr[device].store(true, std::memory_order_release);
+    }
+    dev::ising_sad_pipe_kernel<<<m.n_walkers, 96, bytes, st>>>(m, s);
+    return cudaGetLastError();
+  }
   const size_t bytes = dev::ising_chain_bytes(m.P.nbins, s.L);
-  if (bytes > max_bytes || m.descent) return cudaErrorInvalidConfiguration;
-  return m.method == M_SAD ? dev::launch_chain<M_SAD>(m, s, bytes, max_bytes, st)
-                           : dev::launch_chain<dev::FAM_ANY>(m, s, bytes, max_bytes, st);
+  if (bytes > max_bytes) return cudaErrorInvalidConfiguration;
+  return dev::launch_chain<dev::FAM_ANY>(m, s, bytes, max_bytes, st);
 }
 
 }  // namespace sadmc

@@ -8,8 +8,8 @@ from helpers import METHOD_KW, assert_bins_equal, assert_scalars_equal, ising_sp
 pytestmark = pytest.mark.gpu
 
 
-def run_pair(gpu, oracle, L, W, moves, method, seed=17, lpw=0, chunks=1):
-    kw = METHOD_KW[method]
+def run_pair(gpu, oracle, L, W, moves, method, seed=17, lpw=0, chunks=1, extra=None):
+    kw = dict(METHOD_KW[method], **(extra or {}))
     N = L * L
     cfg = gpu.make_config(gpu.ISING, W, L, e_lo=-2.0 * N - 4, e_hi=2.0 * N + 4, seed=seed,
                           lanes_per_walker=lpw, **kw)
@@ -57,6 +57,39 @@ def test_ising_single_walker_32x32(gpu, oracle):
     assert_bins_equal(b.bins(0), ws[0].bins(), label="L32")
     assert_scalars_equal(b.scalars(0), ws[0].scalars(), label="L32")
     np.testing.assert_array_equal(b.state(0), ws[0].state())
+
+
+def test_ising_single_walker_steady_state(gpu, oracle):
+    """Two million moves of the C1 walker: after the discovery phase nearly every move takes
+    the integer fast path of the pipelined SAD chain."""
+    b, ws = run_pair(gpu, oracle, L=32, W=1, moves=2_000_000, method="sad", lpw=32, chunks=2,
+                     seed=23)
+    assert_bins_equal(b.bins(0), ws[0].bins(), label="L32 steady")
+    assert_scalars_equal(b.scalars(0), ws[0].scalars(), label="L32 steady")
+    np.testing.assert_array_equal(b.state(0), ws[0].state())
+
+
+@pytest.mark.parametrize("energy_bin,bounds", [
+    (1.0, None),                  # half-integer bin centres: non-integer window edges
+    (2.0, (-400.0, 300.0)),       # both energy bounds
+    (8.0, None),                  # two energy levels per bin
+    (3.0, (-450.0, 420.0)),       # not a power of two: the generic bookkeeping throughout
+    (4.0, (-500.0, -100.0)),      # initial descent below max_allowed, then the chain
+])
+def test_ising_single_walker_chain_bins_and_bounds(gpu, oracle, energy_bin, bounds):
+    """The pipelined SAD chain with other bin widths and with min/max_allowed_energy, three
+    walkers of 16x16 over launches of uneven length."""
+    extra = {"energy_bin": energy_bin}
+    if bounds is not None:
+        extra.update(min_allowed=bounds[0], max_allowed=bounds[1])
+    b, ws = run_pair(gpu, oracle, L=16, W=3, moves=150_003, method="sad", lpw=32, chunks=3,
+                     seed=29, extra=extra)
+    for w in range(b.W):
+        label = f"bin {energy_bin} bounds {bounds} walker {w}"
+        assert_bins_equal(b.bins(w), ws[w].bins(), label=label)
+        assert_scalars_equal(b.scalars(w), ws[w].scalars(), label=label)
+        np.testing.assert_array_equal(b.state(w), ws[w].state())
+    assert not b.status().any()
 
 
 def test_ising_single_walker_unstaged(gpu, oracle):
