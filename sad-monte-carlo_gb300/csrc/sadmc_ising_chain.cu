@@ -144,30 +144,43 @@ __global__ void __launch_bounds__(32, 1) ising_chain_kernel(MoveLaunch m, IsingS
 // move -- its proposed bin already visited, no window or bin growth possible, gamma from
 // the table -- runs on those integers and the FP64 ln w; every other move (a possible
 // discovery, growth of the window or of the bins, a parameter change, a trace) takes the
-// generic bookkeeping.  The spins a move reads are loaded one move ahead, before the
-// previous flip, and reloaded when that flip touched them.
-struct PipeTables {
-  uint16_t site[32];
-  uint16_t nb[32][4];
-  uint32_t conflict;  // bit k: move k's site is move k+1's site or one of its neighbours
-  uint32_t gen;       // Fh::pgen the gamma values were computed for
+// generic bookkeeping.
+//
+// Per move the deciding lane reads one 32-byte table record (two 128-bit loads) and
+// writes one 16-byte log record; measured on the single-walker workload, loading the next
+// move's spins ahead of the flip (with a reload on conflicts) was slower than loading them
+// when needed.
+//
+// Table record of one move, as eight 32-bit words: site | n0 << 16, n1 | n2 << 16, n3,
+// bits of the binary32 lower and upper bounds of ln u for the Metropolis uniform u,
+// unused, and gamma (low word, high word).
+struct alignas(16) PipeTables {
+  uint4 mv[32][2];
   uint64_t u53[32];
-  float lnu_lo[32], lnu_hi[32];  // bounds of ln u for the Metropolis uniform u
+  double gamma[32];         // gamma again, as the generic bookkeeping's table
   double rs[32], omrs[32];  // sqrt(1/t) and 1 - sqrt(1/t) (energy.rs:913)
-  double gamma[32];
+  uint32_t gen;             // Fh::pgen the gamma values were computed for
+  uint32_t pad[3];
 };
 struct PipeSnap {  // the walker's SAD parameters at a batch boundary
   double p;
   uint64_t tF, ns;
   uint32_t gen;
 };
-struct PipeLog {  // one move, as the bookkeeping warp needs it
-  double lnw;          // ln w of the bin after the update
-  int32_t E;           // energy after the move (Ising energies are integers)
-  int16_t cur;         // bin after the move (plane index; the planes hold < 2^15 bins)
+// One move as the bookkeeping warp needs it: ln w of the bin after the update (written
+// one move late), and a record of the energy after the move (low 32 bits; Ising energies
+// are integers), the bin after the move (bits 32-47; the planes hold fewer than 2^15
+// bins) and flags (bits 48-63): 1 accepted, 2 tF changed with the acceptance-rate mode on,
+// 4 a generic move, whose PipeExt holds its local indices and allocated bins.  After a
+// fast-path move the local indices are the bins after and before it minus b_lo, and the
+// allocated bins are unchanged.
+struct PipeLog {
+  double lnw;
+  uint64_t rec;
+};
+struct PipeExt {
   int16_t li, i1l;     // local indices of the bin after and before the move
   int16_t b_lo, b_hi;  // allocated bins after the move (prepare_for_state)
-  uint16_t flags;      // bit 0: accepted; bit 1: tF changed with the acceptance-rate mode on
 };
 struct PipeBook {  // the bookkeeping warp's fields, handed back at the end of a launch
   double acc_rate, tscale, max_S;
@@ -177,14 +190,14 @@ struct PipeBook {  // the bookkeeping warp's fields, handed back at the end of a
 
 __host__ __device__ inline size_t ising_pipe_bytes(int nbins, int L) {
   return (size_t)nbins * 64 + (((size_t)L * (size_t)L + 15) & ~(size_t)15) + 3 * sizeof(PipeTables) +
-         2 * 32 * sizeof(PipeLog) + 2 * sizeof(PipeSnap) + sizeof(uint64_t);
+         2 * 32 * (sizeof(PipeLog) + sizeof(PipeExt)) + 2 * sizeof(PipeSnap) + 2 * sizeof(uint64_t);
 }
 
 // rejected = lnw2 > lnw1 && u > exp(lnw1 - lnw2) (energy.rs:461-465).  The binary32
 // truncations a, b of the weights order them unless equal (truncation is monotone); the
 // test u > exp(d) <=> ln u > d is then taken against bounds [lo, hi] of ln u and the error
 // bound of a - b, and in FP64 where those cannot tell.
-__device__ __forceinline__ bool sad_reject(double lnw1, double lnw2, uint64_t u53, float lo, float hi) {
+__device__ __forceinline__ bool sad_reject(double lnw1, double lnw2, const uint64_t* u53, float lo, float hi) {
   const float a = f32_trunc(lnw1), b = f32_trunc(lnw2);
   if (b < a) return false;
   if (b == a && !dgt(lnw2, lnw1)) return false;
@@ -193,7 +206,7 @@ __device__ __forceinline__ bool sad_reject(double lnw1, double lnw2, uint64_t u5
   const float dd = (fabsf(a) + fabsf(b)) * 1.2e-7f + fabsf(df) * 6.0e-8f + 1e-12f;
   if (lo > df + dd) return true;
   if (hi < df - dd) return false;
-  return u53_to_double(u53) > exp(lnw1 - lnw2);
+  return u53_to_double(*u53) > exp(lnw1 - lnw2);
 }
 
 using FhSplit = Fh<1, M_SAD, true>;
@@ -242,10 +255,9 @@ __device__ void lean_sync(const FhSplit& fh, LeanSad& z, bool traced) {
 // One common move on the integer view: bounds, reject_move and the decision-side
 // bookkeeping of move_once (energy.rs:904-974) for a move whose proposed bin was visited
 // before and which can neither grow the window nor the bins.  Returns 0 (rejected) or 1
-// (accepted) with fh.out_li / out_i1l set, or 2 without changing anything when the move
-// needs the generic path.
-__device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, uint64_t u53, float lo, float hi,
-                                         double g) {
+// (accepted), or 2 without changing anything when the move needs the generic path.
+__device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const uint64_t* u53, float lo,
+                                         float hi, double g) {
   const int e2 = z.Ei + de;
   const bool oob = (e2 > z.mx && de > 0) || (e2 < z.mn && de < 0);
   int i2 = fh.cur, cls2 = z.cls;
@@ -270,7 +282,6 @@ __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, uint64
                                  : fh.ld_lnw(fh.win_lo) + div_by((double)e2 - fh.c.too_lo, fh.c.min_T, fh.inv_minT));
     rejected = sad_reject(lnw1, lnw2, u53, lo, hi);
   }
-  const int old_cur = fh.cur;
   if (!rejected) {
     fh.c.accepted += 1;
     z.Ei = e2;
@@ -293,9 +304,6 @@ __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, uint64
     fh.k_lnw += g;
     if (fh.k_hist > fh.c.highest_hist) fh.c.highest_hist = fh.k_hist;
   }
-  fh.out_li = fh.cur - fh.c.b_lo;
-  fh.out_i1l = old_cur - fh.c.b_lo;
-  fh.tsc_event = false;
   return rejected ? 0 : 1;
 }
 
@@ -305,39 +313,52 @@ struct Book {
   PipeBook s;
   double target_rate;
   int kb_lo, kb_hi;  // allocated bins as last seen
+  int kprev;         // bin after the previous move
   int kcur;          // bin whose sums are held in ksE, ksE2
   double ksE, ksE2;
   double *sE, *sE2;
   uint64_t *stamp, *rt;
-  __device__ void replay(const PipeLog& e, double rs, double omrs) {
+  __device__ void replay(const PipeLog& e, const PipeExt& x, double rs, double omrs) {
+    const int Ei = (int)(uint32_t)e.rec;
+    const int cur = (int)((e.rec >> 32) & 0xffffu);
+    const unsigned flags = (unsigned)(e.rec >> 48);
+    int li, i1l;
+    if (flags & 4u) {
+      li = x.li;
+      i1l = x.i1l;
+      while (kb_lo > x.b_lo) stamp[--kb_lo] = s.fill_gen;  // inserted as visited
+      while (kb_hi < x.b_hi) stamp[++kb_hi] = s.fill_gen;
+    } else {
+      li = cur - kb_lo;
+      i1l = kprev - kb_lo;
+    }
+    kprev = cur;
     s.acc_rate *= omrs;
-    if (e.flags & 1) s.acc_rate += rs;
-    while (kb_lo > e.b_lo) stamp[--kb_lo] = s.fill_gen;  // inserted as visited
-    while (kb_hi < e.b_hi) stamp[++kb_hi] = s.fill_gen;
-    if (SADMC_RARE(e.flags & 2)) {
+    if (flags & 1u) s.acc_rate += rs;
+    if (SADMC_RARE(flags & 2u)) {
       double f = s.acc_rate / target_rate;
       f = f < 0.8 ? 0.8 : (f > 1.2 ? 1.2 : f);
       s.tscale *= f;
     }
-    if (e.cur != kcur) {
+    if (cur != kcur) {
       if (kcur >= 0) { sE[kcur] = ksE; sE2[kcur] = ksE2; }
-      kcur = e.cur;
+      kcur = cur;
       ksE = sE[kcur];
       ksE2 = sE2[kcur];
     }
-    const double E = (double)e.E;
+    const double E = (double)Ei;
     ksE += E;
     ksE2 += E * E;
     if (dgt(e.lnw, s.max_S)) {
       s.max_S = e.lnw;
-      s.max_S_local = e.li;
+      s.max_S_local = li;
       s.fill_gen += 1;
       s.fill_val = 1;
-    } else if (e.li == s.max_S_local) {
-      if (e.i1l != e.li) { s.fill_gen += 1; s.fill_val = 0; }
-    } else if (!(stamp[e.cur] == s.fill_gen || s.fill_val != 0)) {
-      stamp[e.cur] = s.fill_gen;
-      rt[e.cur] = rt[e.cur] + 1;
+    } else if (li == s.max_S_local) {
+      if (i1l != li) { s.fill_gen += 1; s.fill_val = 0; }
+    } else if (!(stamp[cur] == s.fill_gen || s.fill_val != 0)) {
+      stamp[cur] = s.fill_gen;
+      rt[cur] = rt[cur] + 1;
     }
   }
 };
@@ -358,8 +379,9 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
   int8_t* S = reinterpret_cast<int8_t*>(sq + 5 * (size_t)nb);
   PipeTables* tbs = reinterpret_cast<PipeTables*>(S + (((size_t)L * (size_t)L + 15) & ~(size_t)15));
   PipeLog* logs = reinterpret_cast<PipeLog*>(tbs + 3);
-  PipeSnap* snap = reinterpret_cast<PipeSnap*>(logs + 64);
-  uint64_t* t_launch = reinterpret_cast<uint64_t*>(snap + 2);
+  PipeExt* exts = reinterpret_cast<PipeExt*>(logs + 64);
+  PipeSnap* snap = reinterpret_cast<PipeSnap*>(exts + 64);
+  uint64_t* t_launch = reinterpret_cast<uint64_t*>(snap + 2);  // move count, first bin
   for (int a = 0; a < 3; ++a)
     for (int k = tid; k < nb; k += 96) sd[(size_t)a * nb + k] = gp[a][k];
   for (int a = 0; a < 5; ++a)
@@ -381,7 +403,8 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
     for (int k = 0; k <= 20; ++k)
       if (fh.width == (double)(1 << k)) z.ws = k;
     snap[0] = PipeSnap{fh.c.latest_param, fh.c.tF, fh.c.num_states, fh.pgen};
-    *t_launch = fh.c.moves;
+    t_launch[0] = fh.c.moves;
+    t_launch[1] = (uint64_t)fh.cur;
   } else if (tid == 64) {
     const WalkerCore& c = m.cores[w];
     bk.s = PipeBook{c.acc_rate, c.tscale, c.max_S, c.max_S_local, c.fill_val, c.fill_gen};
@@ -394,7 +417,8 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
     bk.stamp = sq + 4 * (size_t)nb; bk.rt = sq + 2 * (size_t)nb;
   }
   __syncthreads();
-  const uint64_t t0 = *t_launch;
+  const uint64_t t0 = t_launch[0];
+  if (tid == 64) bk.kprev = (int)t_launch[1];
   const uint64_t n = m.n_moves;
   const uint64_t nbatch = (n + 31) / 32;
   // warp 1: the tables of batch c from the parameters in snap[q]
@@ -406,26 +430,23 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
     const int i = (int)d.which, j = (int)d.j;
     const int jp = j + 1 == L ? 0 : j + 1, jm = j == 0 ? L - 1 : j - 1;
     const int ip = i + 1 == L ? 0 : i + 1, im = i == 0 ? L - 1 : i - 1;
-    const int site = i + j * L;
-    const int n0 = i + jp * L, n1 = i + jm * L, n2 = ip + j * L, n3 = im + j * L;
-    T->site[lane] = (uint16_t)site;
-    T->nb[lane][0] = (uint16_t)n0; T->nb[lane][1] = (uint16_t)n1;
-    T->nb[lane][2] = (uint16_t)n2; T->nb[lane][3] = (uint16_t)n3;
+    const unsigned site = (unsigned)(i + j * L);
+    const unsigned n0 = (unsigned)(i + jp * L), n1 = (unsigned)(i + jm * L), n2 = (unsigned)(ip + j * L),
+                   n3 = (unsigned)(im + j * L);
     T->u53[lane] = d.u53;
-    {  // u lies in [top, top + 1) 2^-24; logf is within 1 ulp, widened by 2^-20
-      const uint32_t top = (uint32_t)(d.u53 >> 29);
-      const float uf = (float)top * (1.0f / 16777216.0f), uh = (float)(top + 1u) * (1.0f / 16777216.0f);
-      T->lnu_lo[lane] = top == 0u ? -INFINITY : logf(uf) * (1.0f + 9.6e-7f);
-      T->lnu_hi[lane] = logf(uh) * (1.0f - 9.6e-7f);
-    }
+    // u lies in [top, top + 1) 2^-24; logf is within 1 ulp, widened by 2^-20
+    const uint32_t top = (uint32_t)(d.u53 >> 29);
+    const float uf = (float)top * (1.0f / 16777216.0f), uh = (float)(top + 1u) * (1.0f / 16777216.0f);
+    const float lo = top == 0u ? -INFINITY : logf(uf) * (1.0f + 9.6e-7f);
+    const float hi = logf(uh) * (1.0f - 9.6e-7f);
     const double v = sqrt(1.0 / (double)t);  // RecentScale's expression
     T->rs[lane] = v;
     T->omrs[lane] = 1. - v;
-    T->gamma[lane] = sad_gamma_value(P.p, P.tF, P.ns, t);
-    const int prev = __shfl_up_sync(0xffffffffu, site, 1);
-    const bool hit = lane > 0 && (prev == site || prev == n0 || prev == n1 || prev == n2 || prev == n3);
-    const unsigned bal = __ballot_sync(0xffffffffu, hit);
-    if (lane == 0) { T->conflict = bal >> 1; T->gen = P.gen; }
+    const double gm = sad_gamma_value(P.p, P.tF, P.ns, t);
+    T->gamma[lane] = gm;
+    T->mv[lane][0] = make_uint4(site | (n0 << 16), n1 | (n2 << 16), n3, __float_as_uint(lo));
+    T->mv[lane][1] = make_uint4(__float_as_uint(hi), 0u, (unsigned)__double2loint(gm), (unsigned)__double2hiint(gm));
+    if (lane == 0) T->gen = P.gen;
   };
   if (warp == 1 && nbatch > 0) fill(0, 0);
   __syncthreads();
@@ -437,29 +458,29 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
       if (lane == 0 && b > 0) {  // replay the previous batch
         const PipeTables* T = &tbs[(b - 1) % 3];
         const PipeLog* lg = &logs[((b - 1) & 1) * 32];
+        const PipeExt* xs = &exts[((b - 1) & 1) * 32];
         const int cnt = (int)(n - 32 * (b - 1) < 32 ? n - 32 * (b - 1) : 32);
-        for (int k = 0; k < cnt; ++k) bk.replay(lg[k], T->rs[k], T->omrs[k]);
+        for (int k = 0; k < cnt; ++k) bk.replay(lg[k], xs[k], T->rs[k], T->omrs[k]);
       }
     } else if (lane == 0 && b < nbatch) {
       const PipeTables* T = &tbs[b % 3];
       PipeLog* lg = &logs[(b & 1) * 32];
+      PipeExt* xs = &exts[(b & 1) * 32];
       const int cnt = (int)(n - 32 * b < 32 ? n - 32 * b : 32);
       fh.xg = T->gamma;
       fh.xg_t0 = fh.c.moves + 1;
       fh.xg_ok = T->gen == fh.pgen;
       lean_sync(fh, z, traced);
-      int sc = S[T->site[0]];
-      int ntc = S[T->nb[0][0]] + S[T->nb[0][1]] + S[T->nb[0][2]] + S[T->nb[0][3]];
       double pend_lnw = 0.0;  // the previous move's ln w, logged one move late
       for (int k = 0; k < cnt; ++k) {
-        const int site = T->site[k];
-        int sn = 0, ntn = 0;
-        if (k + 1 < cnt) {  // the next move's spins, read before this move's flip
-          sn = S[T->site[k + 1]];
-          ntn = S[T->nb[k + 1][0]] + S[T->nb[k + 1][1]] + S[T->nb[k + 1][2]] + S[T->nb[k + 1][3]];
-        }
-        const int de = -(ntc * sc * 2);  // exact: |de| <= 8
-        int r = z.ok ? lean_move(fh, z, de, T->u53[k], T->lnu_lo[k], T->lnu_hi[k], T->gamma[k]) : 2;
+        const uint4 qa = T->mv[k][0], qb = T->mv[k][1];
+        const int site = (int)(qa.x & 0xffffu);
+        const int sc = S[site];
+        const int nt = S[qa.x >> 16] + S[qa.y & 0xffffu] + S[qa.y >> 16] + S[qa.z];
+        const int de = -(nt * sc * 2);  // exact: |de| <= 8
+        const double g = __hiloint2double((int)qb.w, (int)qb.z);
+        int r = z.ok ? lean_move(fh, z, de, &T->u53[k], __uint_as_float(qa.w), __uint_as_float(qb.x), g) : 2;
+        unsigned flags = 0u;
         if (SADMC_RARE(r == 2)) {  // the generic bookkeeping
           const uint64_t t = fh.c.moves + 1;
           fh.Ef = f32_trunc(fh.c.E);
@@ -473,28 +494,15 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
           r = fh.decide_de(true, (float)de, T->u53[k], T->rs[k]) ? 1 : 0;
           fh.finish_move(r == 1);
           lean_sync(fh, z, traced);
+          xs[k] = PipeExt{(int16_t)fh.out_li, (int16_t)fh.out_i1l, (int16_t)fh.c.b_lo, (int16_t)fh.c.b_hi};
+          flags = 4u | (fh.tsc_event ? 2u : 0u);
         }
         if (k > 0) lg[k - 1].lnw = pend_lnw;
         pend_lnw = fh.k_lnw;
-        PipeLog& e = lg[k];
-        e.E = z.ok ? z.Ei : (int)fh.c.E;
-        e.cur = (int16_t)fh.cur;
-        e.li = (int16_t)fh.out_li;
-        e.i1l = (int16_t)fh.out_i1l;
-        e.b_lo = (int16_t)fh.c.b_lo;
-        e.b_hi = (int16_t)fh.c.b_hi;
-        e.flags = (uint16_t)(r | (fh.tsc_event ? 2 : 0));
-        if (r == 1) {
-          S[site] = (int8_t)(-sc);
-          if ((T->conflict >> k) & 1u) {  // the flip touched the next move's spins
-            if (k + 1 < cnt) {
-              sn = S[T->site[k + 1]];
-              ntn = S[T->nb[k + 1][0]] + S[T->nb[k + 1][1]] + S[T->nb[k + 1][2]] + S[T->nb[k + 1][3]];
-            }
-          }
-        }
-        sc = sn;
-        ntc = ntn;
+        const int Elog = z.ok ? z.Ei : (int)fh.c.E;
+        lg[k].rec = (uint64_t)(uint32_t)Elog | ((uint64_t)(uint32_t)fh.cur << 32) |
+                    ((uint64_t)(flags | (unsigned)r) << 48);
+        if (r == 1) S[site] = (int8_t)(-sc);
       }
       if (cnt > 0) lg[cnt - 1].lnw = pend_lnw;
       snap[(b + 1) & 1] = PipeSnap{fh.c.latest_param, fh.c.tF, fh.c.num_states, fh.pgen};

@@ -69,23 +69,27 @@ def test_ising_single_walker_steady_state(gpu, oracle):
     np.testing.assert_array_equal(b.state(0), ws[0].state())
 
 
-@pytest.mark.parametrize("energy_bin,bounds", [
-    (1.0, None),                  # half-integer bin centres: non-integer window edges
-    (2.0, (-400.0, 300.0)),       # both energy bounds
-    (8.0, None),                  # two energy levels per bin
-    (3.0, (-450.0, 420.0)),       # not a power of two: the generic bookkeeping throughout
-    (4.0, (-500.0, -100.0)),      # initial descent below max_allowed, then the chain
+@pytest.mark.parametrize("energy_bin,bounds,target_rate", [
+    (1.0, None, None),                  # half-integer bin centres: non-integer window edges
+    (2.0, (-400.0, 300.0), None),       # both energy bounds
+    (8.0, None, None),                  # two energy levels per bin
+    (3.0, (-450.0, 420.0), None),       # not a power of two: the generic bookkeeping throughout
+    (4.0, (-500.0, -100.0), None),      # initial descent below max_allowed, then the chain
+    (4.0, None, 0.3),                   # acceptance-rate mode: translation scale on tF changes
 ])
-def test_ising_single_walker_chain_bins_and_bounds(gpu, oracle, energy_bin, bounds):
-    """The pipelined SAD chain with other bin widths and with min/max_allowed_energy, three
-    walkers of 16x16 over launches of uneven length."""
+def test_ising_single_walker_chain_bins_and_bounds(gpu, oracle, energy_bin, bounds, target_rate):
+    """The pipelined SAD chain with other bin widths, with min/max_allowed_energy and with
+    the acceptance-rate mode (whose translation-scale updates the replay warp applies),
+    three walkers of 16x16 over launches of uneven length."""
     extra = {"energy_bin": energy_bin}
     if bounds is not None:
         extra.update(min_allowed=bounds[0], max_allowed=bounds[1])
+    if target_rate is not None:
+        extra.update(target_rate=target_rate)
     b, ws = run_pair(gpu, oracle, L=16, W=3, moves=150_003, method="sad", lpw=32, chunks=3,
                      seed=29, extra=extra)
     for w in range(b.W):
-        label = f"bin {energy_bin} bounds {bounds} walker {w}"
+        label = f"bin {energy_bin} bounds {bounds} rate {target_rate} walker {w}"
         assert_bins_equal(b.bins(w), ws[w].bins(), label=label)
         assert_scalars_equal(b.scalars(w), ws[w].scalars(), label=label)
         np.testing.assert_array_equal(b.state(w), ws[w].state())
