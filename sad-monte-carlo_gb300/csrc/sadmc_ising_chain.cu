@@ -311,7 +311,7 @@ __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const 
 // 950-965), in the order move_once applies it.
 struct Book {
   PipeBook s;
-  double target_rate;
+  double target_rate, inv_target;
   int kb_lo, kb_hi;  // allocated bins as last seen
   int kprev;         // bin after the previous move
   int kcur;          // bin whose sums are held in ksE, ksE2
@@ -336,7 +336,7 @@ struct Book {
     s.acc_rate *= omrs;
     if (flags & 1u) s.acc_rate += rs;
     if (SADMC_RARE(flags & 2u)) {
-      double f = s.acc_rate / target_rate;
+      double f = rate_ratio(s.acc_rate, target_rate, inv_target);
       f = f < 0.8 ? 0.8 : (f > 1.2 ? 1.2 : f);
       s.tscale *= f;
     }
@@ -409,6 +409,7 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
     const WalkerCore& c = m.cores[w];
     bk.s = PipeBook{c.acc_rate, c.tscale, c.max_S, c.max_S_local, c.fill_val, c.fill_gen};
     bk.target_rate = m.P.target_rate;
+    bk.inv_target = 1.0 / bk.target_rate;
     bk.kb_lo = c.b_lo;
     bk.kb_hi = c.b_hi;
     bk.kcur = -1;
