@@ -163,6 +163,7 @@ struct sadmc_handle {
     P.min_allowed = cfg.min_allowed;
     P.max_allowed = cfg.max_allowed;
     P.target_rate = cfg.target_rate;
+    P.inv_target = 1.0 / cfg.target_rate;
     return P;
   }
   int resum() const { return cfg.resum_interval > 0 ? cfg.resum_interval : 2048; }

@@ -159,7 +159,7 @@ struct Fh {
   static_assert(!SPLIT || (LPW == 1 && FAM == M_SAD), "the split bookkeeping is SAD on one lane");
   WalkerCore c;
   // launch constants
-  double width, inv_width, min_allowed, max_allowed, target_rate, inv_target;
+  double width, inv_width, min_allowed, max_allowed, target_rate;
   int nbins;
   bool has_min_allowed, has_max_allowed, acc_mode;
   // this walker's planes
@@ -297,7 +297,6 @@ struct Fh {
     has_min_allowed = P.has_min_allowed != 0; has_max_allowed = P.has_max_allowed != 0;
     acc_mode = P.acc_mode != 0;
     min_allowed = P.min_allowed; max_allowed = P.max_allowed; target_rate = P.target_rate;
-    inv_target = 1.0 / target_rate;
     size_t off = (size_t)w * (size_t)P.nbins;
     lnw = B.lnw + off; sE = B.sumE + off; sE2 = B.sumE2 + off;
     hist = B.hist + off; tf = B.t_found + off; rt = B.round_trips + off;
@@ -646,7 +645,7 @@ struct Fh {
       k_sE += E;
       k_sE2 += E2;  // E2 == E * E (set_E)
     }
-    tsc_event = false;
+    if (SPLIT) tsc_event = false;
     update_weights(E);
     const int li = cur - c.b_lo;
     if (SPLIT) {
@@ -712,7 +711,7 @@ struct Fh {
           double ej = center(j);
           if (ej < c.too_lo && ej >= energy) {
             if (ld_hist(j) != 0) {
-              double v = base + div_by(ej - c.too_lo, c.min_T, inv_minT);
+              double v = base + (ej - c.too_lo) / c.min_T;
               if (v < 0.0) v = 0.0;
               st_lnw(j, v);
               c.num_states += 1;
@@ -741,7 +740,8 @@ struct Fh {
       if (SPLIT) {
         tsc_event = old_tF != c.tF && acc_mode;
       } else if (old_tF != c.tF && acc_mode) {  // energy.rs:600-609
-        double s = rate_ratio(c.acc_rate, target_rate, inv_target);
+        // the division, not rate_ratio: its range test costs this kernel family registers
+        double s = c.acc_rate / target_rate;
         s = s < 0.8 ? 0.8 : (s > 1.2 ? 1.2 : s);
         c.tscale *= s;
         tscale_changed = true;

@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
     const WalkerCore& c = m.cores[w];
     bk.s = PipeBook{c.acc_rate, c.tscale, c.max_S, c.max_S_local, c.fill_val, c.fill_gen};
     bk.target_rate = m.P.target_rate;
-    bk.inv_target = 1.0 / bk.target_rate;
+    bk.inv_target = m.P.inv_target;
     bk.kb_lo = c.b_lo;
     bk.kb_hi = c.b_hi;
     bk.kcur = -1;

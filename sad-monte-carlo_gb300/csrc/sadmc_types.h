@@ -64,6 +64,7 @@ struct FhParams {
   int32_t acc_mode;    // MoveParams::AcceptanceRate
   double min_allowed, max_allowed;
   double target_rate;
+  double inv_target;   // 1/target_rate, correctly rounded (the translation-scale update)
 };
 
 // Bin planes, each [n_walkers][nbins].
