@@ -193,22 +193,6 @@ __host__ __device__ inline size_t ising_pipe_bytes(int nbins, int L) {
          2 * 32 * (sizeof(PipeLog) + sizeof(PipeExt)) + 2 * sizeof(PipeSnap) + 2 * sizeof(uint64_t);
 }
 
-// rejected = lnw2 > lnw1 && u > exp(lnw1 - lnw2) (energy.rs:461-465).  The binary32
-// truncations a, b of the weights order them unless equal (truncation is monotone); the
-// test u > exp(d) <=> ln u > d is then taken against bounds [lo, hi] of ln u and the error
-// bound of a - b, and in FP64 where those cannot tell.
-__device__ __forceinline__ bool sad_reject(double lnw1, double lnw2, const uint64_t* u53, float lo, float hi) {
-  const float a = f32_trunc(lnw1), b = f32_trunc(lnw2);
-  if (b < a) return false;
-  if (b == a && !dgt(lnw2, lnw1)) return false;
-  const float df = a - b;
-  // |df - (lnw1 - lnw2)| <= (|a| + |b|) 2^-23 + |df| 2^-24; 1e-12 covers exp's FP64 rounding
-  const float dd = (fabsf(a) + fabsf(b)) * 1.2e-7f + fabsf(df) * 6.0e-8f + 1e-12f;
-  if (lo > df + dd) return true;
-  if (hi < df - dd) return false;
-  return u53_to_double(*u53) > exp(lnw1 - lnw2);
-}
-
 using FhSplit = Fh<1, M_SAD, true>;
 
 // Integer view of a SAD walker: energy, bin range, window and bounds (see above).
@@ -254,57 +238,72 @@ __device__ void lean_sync(const FhSplit& fh, LeanSad& z, bool traced) {
 
 // One common move on the integer view: bounds, reject_move and the decision-side
 // bookkeeping of move_once (energy.rs:904-974) for a move whose proposed bin was visited
-// before and which can neither grow the window nor the bins.  Returns 0 (rejected) or 1
-// (accepted), or 2 without changing anything when the move needs the generic path.
+// before, lies inside or above the SAD window, and which can neither grow the window nor
+// the bins.  Returns 0 (rejected) or 1 (accepted), or 2 without changing anything when
+// the move needs the generic path.  The common path is straight-line code: the loads
+// are issued together and the outcomes merged by selection, so that the compiler can
+// overlap its independent parts.
 __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const uint64_t* u53, float lo,
                                          float hi, double g) {
   const int e2 = z.Ei + de;
   const bool oob = (e2 > z.mx && de > 0) || (e2 < z.mn && de < 0);
-  int i2 = fh.cur, cls2 = z.cls;
-  double p_lnw = fh.k_lnw;
-  uint64_t p_hist = fh.k_hist;
-  if (!oob) {
-    if (e2 < z.cmin || e2 >= z.cmax) return 2;  // prepare_for_state would grow the bins
-    i2 = fh.c.b_lo + ((e2 - z.cmin) >> z.ws);
-    if (i2 != fh.cur) { p_lnw = fh.lnw[i2]; p_hist = fh.hist[i2]; }
-    cls2 = e2 < z.tlo ? -1 : (e2 > z.thi ? 1 : 0);
-    // a first visit (energy.rs:466-483, 938-940) or a window edge (energy.rs:530-580)
-    if (p_hist == 0 || (cls2 != 0 && p_hist >= fh.c.highest_hist)) return 2;
-  }
-  if (z.cls != 0 && fh.k_hist >= fh.c.highest_hist) return 2;
+  // the proposed bin, clamped into the allocated range so that every load stays inside
+  // it; a proposal outside the range is a generic move
+  const int i2r = fh.c.b_lo + ((e2 - z.cmin) >> z.ws);
+  const int i2 = min(max(i2r, fh.c.b_lo), fh.c.b_hi);
+  const double l2m = fh.lnw[i2], lhm = fh.lnw[fh.win_hi];
+  const uint64_t h2m = fh.hist[i2];
+  const bool same = i2 == fh.cur;
+  const uint64_t hist2 = same ? fh.k_hist : h2m;
+  const int cls2 = e2 < z.tlo ? -1 : (e2 > z.thi ? 1 : 0);
+  const uint64_t top = fh.c.highest_hist;
+  // a bin growth (prepare_for_state), a first visit (energy.rs:466-483, 938-940), a
+  // proposal below the window (the FP64 extrapolation) or a window edge (energy.rs:530-580)
+  const bool rare_prop = !oob && (e2 < z.cmin || e2 >= z.cmax || hist2 == 0 || cls2 < 0 ||
+                                  (cls2 > 0 && hist2 >= top));
+  if (rare_prop || (z.cls != 0 && fh.k_hist >= top)) return 2;
   fh.c.moves += 1;
-  bool rejected = oob;
-  double lnw2 = 0.0;
-  if (!oob) {
-    const double lnw1 = z.cls == 0 ? fh.k_lnw : z.lnw1c;
-    lnw2 = cls2 == 0 ? p_lnw
-                     : (cls2 > 0 ? fh.ld_lnw(fh.win_hi)
-                                 : fh.ld_lnw(fh.win_lo) + div_by((double)e2 - fh.c.too_lo, fh.c.min_T, fh.inv_minT));
-    rejected = sad_reject(lnw1, lnw2, u53, lo, hi);
+  const double lnw1 = z.cls == 0 ? fh.k_lnw : z.lnw1c;
+  const double l2raw = same ? fh.k_lnw : l2m;
+  const double lnw2 = cls2 == 0 ? l2raw : (fh.win_hi == fh.cur ? fh.k_lnw : lhm);
+  // rejected = lnw2 > lnw1 && u > exp(lnw1 - lnw2) (energy.rs:461-465): the binary32
+  // truncations a, b order the weights unless equal (truncation is monotone), and the
+  // test u > exp(d) <=> ln u > d is taken against the bounds [lo, hi] of ln u and the
+  // error bound dd of a - b; the FP64 test where those cannot tell
+  const float a = f32_trunc(lnw1), b = f32_trunc(lnw2);
+  const float df = a - b;
+  // |df - (lnw1 - lnw2)| <= (|a| + |b|) 2^-23 + |df| 2^-24; 1e-12 covers exp's FP64 rounding
+  const float dd = (fabsf(a) + fabsf(b)) * 1.2e-7f + fabsf(df) * 6.0e-8f + 1e-12f;
+  const bool acc_sure = b < a || hi < df - dd;
+  const bool rej_sure = b > a && lo > df + dd;
+  bool rejected;
+  if (SADMC_RARE(!oob && !acc_sure && !rej_sure))
+    rejected = dgt(lnw2, lnw1) && u53_to_double(*u53) > exp(lnw1 - lnw2);
+  else
+    rejected = oob || rej_sure;
+  const bool acc = !rejected, moved = acc && !same;
+  if (moved) {  // the cached bin moves: write back, take the new one's fields
+    fh.lnw[fh.cur] = fh.k_lnw;
+    fh.hist[fh.cur] = fh.k_hist;
+    fh.tf[fh.cur] = fh.k_tf;
+    fh.k_tf = fh.tf[i2];
   }
-  if (!rejected) {
-    fh.c.accepted += 1;
-    z.Ei = e2;
-    fh.c.E = (double)e2;
-    if (i2 != fh.cur) {  // the cached bin moves: write back, take the new one's fields
-      fh.lnw[fh.cur] = fh.k_lnw;
-      fh.hist[fh.cur] = fh.k_hist;
-      fh.tf[fh.cur] = fh.k_tf;
-      fh.cur = i2;
-      fh.k_lnw = p_lnw;
-      fh.k_hist = p_hist;
-      fh.k_tf = fh.tf[i2];
-    }
-    z.cls = cls2;
-    z.lnw1c = lnw2;  // ln w at the new E when it lies outside the window
-  }
-  fh.k_hist += 1;
-  if (SADMC_RARE(is_nan64(g))) fh.c.status |= ST_NAN_GAMMA;
-  if (z.cls == 0) {  // SAD updates ln w inside the window only (energy.rs:523-529)
-    fh.k_lnw += g;
-    if (fh.k_hist > fh.c.highest_hist) fh.c.highest_hist = fh.k_hist;
-  }
-  return rejected ? 0 : 1;
+  fh.cur = moved ? i2 : fh.cur;
+  fh.k_lnw = moved ? l2m : fh.k_lnw;
+  const uint64_t kh = (moved ? h2m : fh.k_hist) + 1;
+  fh.k_hist = kh;
+  z.Ei = acc ? e2 : z.Ei;
+  fh.c.E = acc ? (double)e2 : fh.c.E;
+  fh.c.accepted += acc ? 1 : 0;
+  z.cls = acc ? cls2 : z.cls;
+  z.lnw1c = acc ? lnw2 : z.lnw1c;  // ln w at the new E when it lies outside the window
+  fh.c.status |= is_nan64(g) ? (uint32_t)ST_NAN_GAMMA : 0u;
+  // SAD updates ln w inside the window only (energy.rs:523-529)
+  const bool inw = z.cls == 0;
+  const double up = fh.k_lnw + g;
+  fh.k_lnw = inw ? up : fh.k_lnw;
+  fh.c.highest_hist = inw && kh > top ? kh : top;
+  return acc ? 1 : 0;
 }
 
 // The bookkeeping warp's replay of one logged move (energy.rs:913-914, 600-609, 941-942,
@@ -473,8 +472,10 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
       fh.xg_ok = T->gen == fh.pgen;
       lean_sync(fh, z, traced);
       double pend_lnw = 0.0;  // the previous move's ln w, logged one move late
+      uint4 nx0 = T->mv[0][0], nx1 = T->mv[0][1];  // the next move's table record
       for (int k = 0; k < cnt; ++k) {
-        const uint4 qa = T->mv[k][0], qb = T->mv[k][1];
+        const uint4 qa = nx0, qb = nx1;
+        if (k + 1 < cnt) { nx0 = T->mv[k + 1][0]; nx1 = T->mv[k + 1][1]; }
         const int site = (int)(qa.x & 0xffffu);
         const int sc = S[site];
         const int nt = S[qa.x >> 16] + S[qa.y & 0xffffu] + S[qa.y >> 16] + S[qa.z];
