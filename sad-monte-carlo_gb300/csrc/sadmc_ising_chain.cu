@@ -160,7 +160,8 @@ struct alignas(16) PipeTables {
   double gamma[32];         // gamma again, as the generic bookkeeping's table
   double rs[32], omrs[32];  // sqrt(1/t) and 1 - sqrt(1/t) (energy.rs:913)
   uint32_t gen;             // Fh::pgen the gamma values were computed for
-  uint32_t pad[3];
+  uint32_t nan_gamma;       // some gamma of the batch is NaN (the generic path reports it)
+  uint32_t pad[2];
 };
 struct PipeSnap {  // the walker's SAD parameters at a batch boundary
   double p;
@@ -240,7 +241,8 @@ __device__ void lean_sync(const FhSplit& fh, LeanSad& z, bool traced) {
 // bookkeeping of move_once (energy.rs:904-974) for a move whose proposed bin was visited
 // before, lies inside or above the SAD window, and which can neither grow the window nor
 // the bins.  Returns 0 (rejected) or 1 (accepted), or 2 without changing anything when
-// the move needs the generic path.  The common path is straight-line code: the loads
+// the move needs the generic path.  The move and acceptance counts and the FP64 energy
+// are the caller's to bring up to date (from z.Ei) when the fast path is left.  The common path is straight-line code: the loads
 // are issued together and the outcomes merged by selection, so that the compiler can
 // overlap its independent parts.
 __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const uint64_t* u53, float lo,
@@ -262,7 +264,6 @@ __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const 
   const bool rare_prop = !oob && (e2 < z.cmin || e2 >= z.cmax || hist2 == 0 || cls2 < 0 ||
                                   (cls2 > 0 && hist2 >= top));
   if (rare_prop || (z.cls != 0 && fh.k_hist >= top)) return 2;
-  fh.c.moves += 1;
   const double lnw1 = z.cls == 0 ? fh.k_lnw : z.lnw1c;
   const double l2raw = same ? fh.k_lnw : l2m;
   const double lnw2 = cls2 == 0 ? l2raw : (fh.win_hi == fh.cur ? fh.k_lnw : lhm);
@@ -293,11 +294,8 @@ __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const 
   const uint64_t kh = (moved ? h2m : fh.k_hist) + 1;
   fh.k_hist = kh;
   z.Ei = acc ? e2 : z.Ei;
-  fh.c.E = acc ? (double)e2 : fh.c.E;
-  fh.c.accepted += acc ? 1 : 0;
   z.cls = acc ? cls2 : z.cls;
   z.lnw1c = acc ? lnw2 : z.lnw1c;  // ln w at the new E when it lies outside the window
-  fh.c.status |= is_nan64(g) ? (uint32_t)ST_NAN_GAMMA : 0u;
   // SAD updates ln w inside the window only (energy.rs:523-529)
   const bool inw = z.cls == 0;
   const double up = fh.k_lnw + g;
@@ -446,7 +444,8 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
     T->gamma[lane] = gm;
     T->mv[lane][0] = make_uint4(site | (n0 << 16), n1 | (n2 << 16), n3, __float_as_uint(lo));
     T->mv[lane][1] = make_uint4(__float_as_uint(hi), 0u, (unsigned)__double2loint(gm), (unsigned)__double2hiint(gm));
-    if (lane == 0) T->gen = P.gen;
+    const unsigned nan_any = __ballot_sync(0xffffffffu, is_nan64(gm));
+    if (lane == 0) { T->gen = P.gen; T->nan_gamma = nan_any != 0u ? 1u : 0u; }
   };
   if (warp == 1 && nbatch > 0) fill(0, 0);
   __syncthreads();
@@ -469,8 +468,10 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
       const int cnt = (int)(n - 32 * b < 32 ? n - 32 * b : 32);
       fh.xg = T->gamma;
       fh.xg_t0 = fh.c.moves + 1;
-      fh.xg_ok = T->gen == fh.pgen;
+      fh.xg_ok = T->gen == fh.pgen && T->nan_gamma == 0u;
       lean_sync(fh, z, traced);
+      const uint64_t mbase = fh.c.moves;  // fast-path moves leave the counts to this loop
+      unsigned lacc = 0;                  // fast-path acceptances not yet counted
       double pend_lnw = 0.0;  // the previous move's ln w, logged one move late
       uint4 nx0 = T->mv[0][0], nx1 = T->mv[0][1];  // the next move's table record
       for (int k = 0; k < cnt; ++k) {
@@ -484,6 +485,10 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
         int r = z.ok ? lean_move(fh, z, de, &T->u53[k], __uint_as_float(qa.w), __uint_as_float(qb.x), g) : 2;
         unsigned flags = 0u;
         if (SADMC_RARE(r == 2)) {  // the generic bookkeeping
+          fh.c.moves = mbase + (uint64_t)k;
+          fh.c.accepted += lacc;
+          lacc = 0;
+          if (z.ok) fh.c.E = (double)z.Ei;
           const uint64_t t = fh.c.moves + 1;
           fh.Ef = f32_trunc(fh.c.E);
           fh.begin_move(T->omrs[k]);
@@ -498,6 +503,8 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
           lean_sync(fh, z, traced);
           xs[k] = PipeExt{(int16_t)fh.out_li, (int16_t)fh.out_i1l, (int16_t)fh.c.b_lo, (int16_t)fh.c.b_hi};
           flags = 4u | (fh.tsc_event ? 2u : 0u);
+        } else {
+          lacc += (unsigned)r;
         }
         if (k > 0) lg[k - 1].lnw = pend_lnw;
         pend_lnw = fh.k_lnw;
@@ -507,6 +514,9 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
         if (r == 1) S[site] = (int8_t)(-sc);
       }
       if (cnt > 0) lg[cnt - 1].lnw = pend_lnw;
+      fh.c.moves = mbase + (uint64_t)cnt;
+      fh.c.accepted += lacc;
+      if (z.ok) fh.c.E = (double)z.Ei;
       snap[(b + 1) & 1] = PipeSnap{fh.c.latest_param, fh.c.tF, fh.c.num_states, fh.pgen};
     }
     __syncthreads();
