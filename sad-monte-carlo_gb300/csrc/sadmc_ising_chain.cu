@@ -223,6 +223,7 @@ __device__ void lean_sync(const FhSplit& fh, LeanSad& z, bool traced) {
   if (!(E == floor(E) && fabs(E) < lim && cm == floor(cm) && fabs(cm) < lim)) return;
   const double span = (double)(fh.c.b_hi - fh.c.b_lo + 1) * fh.width;
   if (!(fabs(cm + span) < lim)) return;
+  if (fh.c.highest_hist >= 0x7fffffffull) return;  // the fast path counts in 32 bits
   if (is_nan64(fh.c.too_lo) || is_nan64(fh.c.too_hi) || is_nan64(fh.max_allowed) || is_nan64(fh.min_allowed))
     return;
   z.Ei = (int)E;
@@ -239,8 +240,7 @@ __device__ void lean_sync(const FhSplit& fh, LeanSad& z, bool traced) {
 
 // One common move on the integer view: bounds, reject_move and the decision-side
 // bookkeeping of move_once (energy.rs:904-974) for a move whose proposed bin was visited
-// before, lies inside or above the SAD window, and which can neither grow the window nor
-// the bins.  Returns 0 (rejected) or 1 (accepted), or 2 without changing anything when
+// before and which can neither grow the window nor the bins.  Returns 0 (rejected) or 1 (accepted), or 2 without changing anything when
 // the move needs the generic path.  The move and acceptance counts and the FP64 energy
 // are the caller's to bring up to date (from z.Ei) when the fast path is left.  The common path is straight-line code: the loads
 // are issued together and the outcomes merged by selection, so that the compiler can
@@ -256,17 +256,18 @@ __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const 
   const double l2m = fh.lnw[i2], lhm = fh.lnw[fh.win_hi];
   const uint64_t h2m = fh.hist[i2];
   const bool same = i2 == fh.cur;
-  const uint64_t hist2 = same ? fh.k_hist : h2m;
+  const uint32_t hist2 = (uint32_t)(same ? fh.k_hist : h2m);
   const int cls2 = e2 < z.tlo ? -1 : (e2 > z.thi ? 1 : 0);
-  const uint64_t top = fh.c.highest_hist;
-  // a bin growth (prepare_for_state), a first visit (energy.rs:466-483, 938-940), a
-  // proposal below the window (the FP64 extrapolation) or a window edge (energy.rs:530-580)
-  const bool rare_prop = !oob && (e2 < z.cmin || e2 >= z.cmax || hist2 == 0 || cls2 < 0 ||
-                                  (cls2 > 0 && hist2 >= top));
-  if (rare_prop || (z.cls != 0 && fh.k_hist >= top)) return 2;
+  const uint32_t top = (uint32_t)fh.c.highest_hist;
+  // a bin growth (prepare_for_state), a first visit (energy.rs:466-483, 938-940) or a
+  // window edge (energy.rs:530-580)
+  const bool rare_prop = !oob && (e2 < z.cmin || e2 >= z.cmax || hist2 == 0 || (cls2 != 0 && hist2 >= top));
+  if (rare_prop || (z.cls != 0 && (uint32_t)fh.k_hist >= top)) return 2;
   const double lnw1 = z.cls == 0 ? fh.k_lnw : z.lnw1c;
   const double l2raw = same ? fh.k_lnw : l2m;
-  const double lnw2 = cls2 == 0 ? l2raw : (fh.win_hi == fh.cur ? fh.k_lnw : lhm);
+  double lnw2 = cls2 == 0 ? l2raw : (fh.win_hi == fh.cur ? fh.k_lnw : lhm);
+  if (cls2 < 0)  // below the window: the linear extrapolation at min_T (energy.rs:461-462)
+    lnw2 = fh.ld_lnw(fh.win_lo) + div_by((double)e2 - fh.c.too_lo, fh.c.min_T, fh.inv_minT);
   // rejected = lnw2 > lnw1 && u > exp(lnw1 - lnw2) (energy.rs:461-465): the binary32
   // truncations a, b order the weights unless equal (truncation is monotone), and the
   // test u > exp(d) <=> ln u > d is taken against the bounds [lo, hi] of ln u and the
@@ -291,7 +292,7 @@ __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const 
   }
   fh.cur = moved ? i2 : fh.cur;
   fh.k_lnw = moved ? l2m : fh.k_lnw;
-  const uint64_t kh = (moved ? h2m : fh.k_hist) + 1;
+  const uint32_t kh = (uint32_t)(moved ? h2m : fh.k_hist) + 1u;
   fh.k_hist = kh;
   z.Ei = acc ? e2 : z.Ei;
   z.cls = acc ? cls2 : z.cls;
@@ -484,6 +485,7 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
         const double g = __hiloint2double((int)qb.w, (int)qb.z);
         int r = z.ok ? lean_move(fh, z, de, &T->u53[k], __uint_as_float(qa.w), __uint_as_float(qb.x), g) : 2;
         unsigned flags = 0u;
+        int Elog = z.Ei;
         if (SADMC_RARE(r == 2)) {  // the generic bookkeeping
           fh.c.moves = mbase + (uint64_t)k;
           fh.c.accepted += lacc;
@@ -503,12 +505,12 @@ __global__ void __launch_bounds__(96, 1) ising_sad_pipe_kernel(MoveLaunch m, Isi
           lean_sync(fh, z, traced);
           xs[k] = PipeExt{(int16_t)fh.out_li, (int16_t)fh.out_i1l, (int16_t)fh.c.b_lo, (int16_t)fh.c.b_hi};
           flags = 4u | (fh.tsc_event ? 2u : 0u);
+          Elog = (int)fh.c.E;
         } else {
           lacc += (unsigned)r;
         }
         if (k > 0) lg[k - 1].lnw = pend_lnw;
         pend_lnw = fh.k_lnw;
-        const int Elog = z.ok ? z.Ei : (int)fh.c.E;
         lg[k].rec = (uint64_t)(uint32_t)Elog | ((uint64_t)(uint32_t)fh.cur << 32) |
                     ((uint64_t)(flags | (unsigned)r) << 48);
         if (r == 1) S[site] = (int8_t)(-sc);
