@@ -75,7 +75,7 @@ typedef struct sadmc_config {
   double e_lo, e_hi;         /* energies the preallocated bins must cover */
   int32_t acceptance_rate_mode; /* MoveParams::AcceptanceRate(target_rate) */
   int32_t pad2;
-  double target_rate;
+  double target_rate;        /* in acceptance-rate mode a positive number (else refused) */
   double translation_scale;  /* initial rms step (MoveParams::TranslationScale, 0.05) */
   double well_width;         /* square-well lambda (optsquare default 1.3) */
   uint64_t seed;             /* Philox key; walker w draws from stream (seed, w) */

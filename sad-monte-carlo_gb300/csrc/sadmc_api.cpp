@@ -362,6 +362,9 @@ int32_t sadmc_create(const sadmc_config* cfg, const sadmc_geometry* geom, sadmc_
   if (c.system < SADMC_ISING || c.system > SADMC_SW) return fail(SADMC_ERR_INVALID, "unknown system");
   if (c.method < SADMC_SAD || c.method > SADMC_CANONICAL) return fail(SADMC_ERR_INVALID, "unknown method");
   if (!(c.e_hi > c.e_lo)) return fail(SADMC_ERR_INVALID, "e_hi must exceed e_lo");
+  // the translation-scale update divides by target_rate through its reciprocal
+  if (c.acceptance_rate_mode && !(c.target_rate >= 0x1p-1000 && c.target_rate <= 0x1p+1000))
+    return fail(SADMC_ERR_INVALID, "target_rate must be a positive number");
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
     return fail(SADMC_ERR_CUDA, "no CUDA device");

@@ -108,13 +108,14 @@ __device__ __forceinline__ double div_by(double a, double b, double y) {
   const double r = __fma_rn(-b, q, a);
   return __fma_rn(r, y, q);
 }
-// acceptance_rate / target_rate of the translation-scale update (energy.rs:600-609), by
-// the reciprocal y = 1/target_rate where div_by is exact (normal operands, quotient far
-// from the subnormal range), by division otherwise.
-__device__ __forceinline__ double rate_ratio(double rate, double target, double y) {
-  if (rate >= 0x1p-1000 && rate <= 0x1p+1000 && target >= 0x1p-1000 && target <= 0x1p+1000)
-    return div_by(rate, target, y);
-  return rate / target;
+// The translation-scale factor clamp(acceptance_rate / target_rate, 0.8, 1.2)
+// (energy.rs:600-609), the quotient taken by div_by with y = 1/target_rate.  The clamped
+// value equals the reference's: where the quotient lies in [0.8, 1.2] the rate (at most 1)
+// and target are normal numbers and div_by is correctly rounded; below 0.8 (the rate
+// tiny or zero included) div_by's value stays below 0.8, and both clamp to 0.8.
+__device__ __forceinline__ double rate_factor(double rate, double target, double y) {
+  const double s = div_by(rate, target, y);
+  return s < 0.8 ? 0.8 : (s > 1.2 ? 1.2 : s);
 }
 // rejected = (u > exp(lnw1 - lnw2)) for lnw1 - lnw2 <= 0, taken on the binary32 copies
 // of the two weights when far enough from the threshold; otherwise the FP64 difference
@@ -159,7 +160,7 @@ struct Fh {
   static_assert(!SPLIT || (LPW == 1 && FAM == M_SAD), "the split bookkeeping is SAD on one lane");
   WalkerCore c;
   // launch constants
-  double width, inv_width, min_allowed, max_allowed, target_rate;
+  double width, inv_width, min_allowed, max_allowed, target_rate, inv_target;
   int nbins;
   bool has_min_allowed, has_max_allowed, acc_mode;
   // this walker's planes
@@ -297,6 +298,7 @@ struct Fh {
     has_min_allowed = P.has_min_allowed != 0; has_max_allowed = P.has_max_allowed != 0;
     acc_mode = P.acc_mode != 0;
     min_allowed = P.min_allowed; max_allowed = P.max_allowed; target_rate = P.target_rate;
+    inv_target = P.inv_target;
     size_t off = (size_t)w * (size_t)P.nbins;
     lnw = B.lnw + off; sE = B.sumE + off; sE2 = B.sumE2 + off;
     hist = B.hist + off; tf = B.t_found + off; rt = B.round_trips + off;
@@ -740,10 +742,7 @@ struct Fh {
       if (SPLIT) {
         tsc_event = old_tF != c.tF && acc_mode;
       } else if (old_tF != c.tF && acc_mode) {  // energy.rs:600-609
-        // the division, not rate_ratio: its range test costs this kernel family registers
-        double s = c.acc_rate / target_rate;
-        s = s < 0.8 ? 0.8 : (s > 1.2 ? 1.2 : s);
-        c.tscale *= s;
+        c.tscale *= rate_factor(c.acc_rate, target_rate, inv_target);
         tscale_changed = true;
       }
     }

@@ -334,9 +334,7 @@ struct Book {
     s.acc_rate *= omrs;
     if (flags & 1u) s.acc_rate += rs;
     if (SADMC_RARE(flags & 2u)) {
-      double f = rate_ratio(s.acc_rate, target_rate, inv_target);
-      f = f < 0.8 ? 0.8 : (f > 1.2 ? 1.2 : f);
-      s.tscale *= f;
+      s.tscale *= rate_factor(s.acc_rate, target_rate, inv_target);
     }
     if (cur != kcur) {
       if (kcur >= 0) { sE[kcur] = ksE; sE2[kcur] = ksE2; }

@@ -47,3 +47,21 @@ def test_no_oracle_in_product():
                 text = open(os.path.join(root, f)).read()
                 for pat in (r"import\s+oracle", r"from\s+oracle", r"liboracle", r"#include\s+\S*oracle"):
                     assert not re.search(pat, text), (f, pat)
+
+
+def test_create_refuses_a_target_rate_it_cannot_divide_by():
+    """In acceptance-rate mode the translation-scale update divides by target_rate through
+    its reciprocal; sadmc_create refuses a target rate that is not a positive number before
+    it touches the device (so this runs without a GPU)."""
+    import ctypes
+    import sadmc_gb300 as G
+    for bad in (0.0, -0.5, float("nan")):
+        cfg = G.make_config(G.LJ, 4, 13, method=G.SAD, e_lo=-50.0, e_hi=0.0, target_rate=0.5)
+        cfg.target_rate = bad
+        geom = (G.Geometry * 4)()
+        for g in geom:
+            g.n, g.radius = 13, 2.5
+        h = ctypes.c_void_p()
+        rc = G.lib().sadmc_create(ctypes.byref(cfg), geom, ctypes.byref(h))
+        assert rc == -1 and not h.value, (bad, rc)
+        assert b"target_rate" in G.lib().sadmc_last_error()
