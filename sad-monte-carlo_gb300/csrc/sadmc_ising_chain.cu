@@ -127,8 +127,9 @@ __global__ void __launch_bounds__(32, 1) ising_chain_kernel(MoveLaunch m, IsingS
 // ---- SAD: the chain pipelined over three warps, with an integer fast path ---------------
 //
 // Warp 0's lane 0 runs the decisions and the state they read: the energy, the bins' ln w,
-// histogram and t_found, the SAD window and parameters.  It records each move (bin, local
-// indices, acceptance, energy, ln w after the update) in a log.  Warp 2's lane 0 replays
+// histogram and t_found, the SAD window and parameters.  It records each move (bin,
+// acceptance, energy, ln w after the update; the local indices and allocated bins of a
+// generic move) in a log.  Warp 2's lane 0 replays
 // the log of the previous batch for the bookkeeping no decision reads: the acceptance
 // rate and translation scale (energy.rs:600-621, 913-914), the energy sums (energy.rs:
 // 941-942) and the max-entropy / round-trip stamps (energy.rs:950-965).  Warp 1 fills the
@@ -170,8 +171,8 @@ struct PipeSnap {  // the walker's SAD parameters at a batch boundary
 };
 // One move as the bookkeeping warp needs it: ln w of the bin after the update (written
 // one move late), and a record of the energy after the move (low 32 bits; Ising energies
-// are integers), the bin after the move (bits 32-47; the planes hold fewer than 2^15
-// bins) and flags (bits 48-63): 1 accepted, 2 tF changed with the acceptance-rate mode on,
+// are integers), the bin after the move (bits 32-47; the shared-memory planes of this
+// kernel hold at most 3200 bins) and flags (bits 48-63): 1 accepted, 2 tF changed with the acceptance-rate mode on,
 // 4 a generic move, whose PipeExt holds its local indices and allocated bins.  After a
 // fast-path move the local indices are the bins after and before it minus b_lo, and the
 // allocated bins are unchanged.
@@ -240,11 +241,12 @@ __device__ void lean_sync(const FhSplit& fh, LeanSad& z, bool traced) {
 
 // One common move on the integer view: bounds, reject_move and the decision-side
 // bookkeeping of move_once (energy.rs:904-974) for a move whose proposed bin was visited
-// before and which can neither grow the window nor the bins.  Returns 0 (rejected) or 1 (accepted), or 2 without changing anything when
-// the move needs the generic path.  The move and acceptance counts and the FP64 energy
-// are the caller's to bring up to date (from z.Ei) when the fast path is left.  The common path is straight-line code: the loads
-// are issued together and the outcomes merged by selection, so that the compiler can
-// overlap its independent parts.
+// before and which can neither grow the window nor the bins.  Returns 0 (rejected) or 1
+// (accepted), or 2 without changing anything when the move needs the generic path.  The
+// move and acceptance counts and the FP64 energy are the caller's to bring up to date
+// (from z.Ei) when the fast path is left.  The common path is straight-line code: the
+// loads are issued together and the outcomes merged by selection, so that the compiler
+// can overlap its independent parts.
 __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const uint64_t* u53, float lo,
                                          float hi, double g) {
   const int e2 = z.Ei + de;
@@ -261,7 +263,8 @@ __device__ __forceinline__ int lean_move(FhSplit& fh, LeanSad& z, int de, const 
   const uint32_t top = (uint32_t)fh.c.highest_hist;
   // a bin growth (prepare_for_state), a first visit (energy.rs:466-483, 938-940) or a
   // window edge (energy.rs:530-580)
-  const bool rare_prop = !oob && (e2 < z.cmin || e2 >= z.cmax || hist2 == 0 || (cls2 != 0 && hist2 >= top));
+  const bool rare_prop =
+      !oob && (e2 < z.cmin || e2 >= z.cmax || hist2 == 0 || (cls2 != 0 && hist2 >= top));
   if (rare_prop || (z.cls != 0 && (uint32_t)fh.k_hist >= top)) return 2;
   const double lnw1 = z.cls == 0 ? fh.k_lnw : z.lnw1c;
   const double l2raw = same ? fh.k_lnw : l2m;
