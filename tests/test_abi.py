@@ -65,3 +65,22 @@ def test_create_refuses_a_target_rate_it_cannot_divide_by():
         rc = G.lib().sadmc_create(ctypes.byref(cfg), geom, ctypes.byref(h))
         assert rc == -1 and not h.value, (bad, rc)
         assert b"target_rate" in G.lib().sadmc_last_error()
+
+
+def test_create_refuses_malformed_configurations_before_touching_the_device():
+    """sadmc_create checks the configuration before it looks for a device (so this runs
+    without a GPU): walker count, system, method and energy range."""
+    import ctypes
+    import sadmc_gb300 as G
+    cases = [("n_walkers", 0, b"n_walkers"), ("system", 9, b"system"), ("method", 7, b"method"),
+             ("e_hi", -60.0, b"e_hi")]
+    for field, value, word in cases:
+        cfg = G.make_config(G.LJ, 4, 13, method=G.SAD, e_lo=-50.0, e_hi=0.0)
+        setattr(cfg, field, value)
+        geom = (G.Geometry * 4)()
+        for g in geom:
+            g.n, g.radius = 13, 2.5
+        h = ctypes.c_void_p()
+        rc = G.lib().sadmc_create(ctypes.byref(cfg), geom, ctypes.byref(h))
+        assert rc == -1 and not h.value, (field, rc)
+        assert word in G.lib().sadmc_last_error(), (field, G.lib().sadmc_last_error())
